@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Benchmark of the brute-force search path on one GB300 (or N replicas).
+
+Workload (the configuration the headline metric is quoted on): a
+BruteForceIndex over 1,000,000 x 128 float32 vectors from a Gaussian mixture
+(1,024 centres ~ 3*N(0,I), points = centre + N(0,I)), 10,000 queries from the
+same mixture, k = 100, Euclidean.  A step is one batched search of all
+10,000 queries.  The base (512 MB) is larger than L2 (129 MB), so every step
+streams it from HBM; no L2 flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is queries/s of the headline form with queries and outputs resident
+in HBM; `e2e` is the same through the public API with host buffers (H2D of the
+queries and D2H of ids + distances inside the timed region).  The headline
+form is the fastest form whose recall@10 against the exact FP32 result is
+>= 0.95; every form's QPS and recall is listed under "forms".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_BASE, DIM, N_Q, K, N_CENTERS = 1_000_000, 128, 10_000, 100, 1024
+WORKLOAD = "BruteForceIndex 1Mx128 f32 gaussian-mixture(1024), 10k queries, k=100, Euclidean"
+
+
+def args_parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--forms", default="fp32,bf16,fp8")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="queries in the CPU baseline sample")
+    ap.add_argument("--small", action="store_true", help="tiny workload for a quick check")
+    return ap.parse_args()
+
+
+# ---- distributed plumbing (replicas: one process per GPU, no data exchange) ----
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t)
+        return float(t.item())
+
+
+# ---- clocks sampled during the timed region --------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.p = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-i", str(self.idx), "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if not self.p:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        sm, mx, reasons = [], 0.0, set()
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                "sw_power_cap"), f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+            "source": "fallback"}
+
+
+def make_data(small: bool):
+    from hora_gb300 import synth
+    n, nq = (20_000, 512) if small else (N_BASE, N_Q)
+    base = synth.mixture(n, DIM, N_CENTERS, stream=1)
+    q = synth.mixture(nq, DIM, N_CENTERS, stream=2)
+    return base, q
+
+
+def recall_at(ids, exact, r=10):
+    hit = 0
+    for a, b in zip(ids[:, :r], exact[:, :r]):
+        hit += len(set(a.tolist()) & set(b.tolist()))
+    return hit / (ids.shape[0] * r)
+
+
+def cpu_sample_qps(base, q, k, n_sample, threads):
+    """The oracle (C port of the reference's scan) on a bounded query sample."""
+    from oracle import oracle as O
+    O.build()
+    qs = q[:n_sample]
+    t0 = time.perf_counter()
+    O.bf_search(base, qs, k, O.EUCLIDEAN, threads=threads)
+    dt = time.perf_counter() - t0
+    return n_sample / dt, dt
+
+
+# ---- our implementation ------------------------------------------------------------
+def run_ours(a, dist: Dist):
+    import torch
+
+    import hora_gb300 as H
+    from hora_gb300 import build as B
+
+    torch.cuda.set_device(dist.local)
+    B.build()
+    base, q = make_data(a.small)
+    n, nq = base.shape[0], q.shape[0]
+    ix = H.BruteForceIndex(DIM)
+    ix.madd(torch.from_numpy(base).cuda(), None)
+    ix.build(H.Metric.Euclidean)
+    dq = torch.from_numpy(q).cuda()
+    ids_d = torch.empty((nq, K), dtype=torch.int64, device="cuda")
+    dist_d = torch.empty((nq, K), dtype=torch.float32, device="cuda")
+
+    # exact FP32 result (reference semantics) and per-form recall
+    forms = {}
+    exact = None
+    order = [f for f in a.forms.split(",") if f]
+    for form in order:
+        prec = {"fp32": H.Precision.FP32, "bf16": H.Precision.BF16, "fp8": H.Precision.FP8}[form]
+        try:
+            ix.set_option(H.Option.PRECISION, prec)
+            ix.search_batch(dq, K, ids_out=ids_d, dist_out=dist_d)
+        except H.HoraError as e:
+            forms[form] = {"error": str(e)}
+            continue
+        torch.cuda.synchronize()
+        ids = ids_d.cpu().numpy()
+        if form == "fp32":
+            exact = ids
+        rec10 = recall_at(ids, exact, 10) if exact is not None else None
+        rec100 = recall_at(ids, exact, K) if exact is not None else None
+        # warm-up and timing with device-resident inputs
+        for _ in range(a.warmup):
+            ix.search_batch(dq, K, ids_out=ids_d, dist_out=dist_d)
+        torch.cuda.synchronize()
+        dist.barrier()
+        step_ms = []
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            ix.search_batch(dq, K, ids_out=ids_d, dist_out=dist_d)
+            step_ms.append(json.loads(ix.idx_info())["last_search_ms"])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        dist.barrier()
+        dev = sum(step_ms) / 1e3
+        forms[form] = {"qps": nq * a.steps / dev, "wall_qps": nq * a.steps / wall,
+                       "recall@10": rec10, "recall@100": rec100,
+                       "p50_ms": float(np.percentile(step_ms, 50)),
+                       "p99_ms": float(np.percentile(step_ms, 99))}
+
+    ok = [f for f in order if "qps" in forms.get(f, {}) and (forms[f]["recall@10"] or 0) >= 0.95]
+    head = max(ok, key=lambda f: forms[f]["qps"]) if ok else "fp32"
+    prec = {"fp32": H.Precision.FP32, "bf16": H.Precision.BF16, "fp8": H.Precision.FP8}[head]
+    ix.set_option(H.Option.PRECISION, prec)
+
+    # ---- headline timed region: device-resident inputs, kernel timing on ----
+    for _ in range(a.warmup):
+        ix.search_batch(dq, K, ids_out=ids_d, dist_out=dist_d)
+    torch.cuda.synchronize()
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    H._lib.profile_report()
+    H._lib.profile(True)
+    l0 = H.launches()
+    clocks.start()
+    step_ms = []
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        ix.search_batch(dq, K, ids_out=ids_d, dist_out=dist_d)
+        step_ms.append(json.loads(ix.idx_info())["last_search_ms"])
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t0
+    launches = H.launches() - l0
+    clk = clocks.stop()
+    H._lib.profile(False)
+    prof = H._lib.profile_report()
+    dist.barrier()
+    t_dev = sum(step_ms) / 1e3
+    t_max = dist.max(t_dev)
+    value = nq * a.steps * dist.world / t_max
+
+    # ---- e2e through the public API with host buffers ----
+    qh = torch.from_numpy(q).pin_memory().numpy()
+    ids_h = torch.empty((nq, K), dtype=torch.int64).pin_memory().numpy().view(np.uint64)
+    dist_h = torch.empty((nq, K), dtype=torch.float32).pin_memory().numpy()
+    ix.search_batch(qh, K, ids_out=ids_h, dist_out=dist_h)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        ix.search_batch(qh, K, ids_out=ids_h, dist_out=dist_h)
+    t_e2e = dist.max(time.perf_counter() - t0)
+    e2e = {"value": nq * a.steps * dist.world / t_e2e, "unit": "queries/s",
+           "h2d_bytes_per_step": int(q.nbytes), "d2h_bytes_per_step": int(ids_h.nbytes + dist_h.nbytes)}
+
+    # ---- roofline of the dominant kernel (live CUDA-event timing) ----
+    pk = peaks()
+    top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else (None, (0, 0.0))
+    name, (nl, ms) = top
+    roof = None
+    if name:
+        if name.startswith("fp32_tile"):
+            # exact form: sub + mul + add per (query, row, dim), 1 FP32 op/lane/clk
+            work = 3.0 * nq * n * DIM * a.steps
+            peak_t = 152 * 128 * 2.07e9 / 1e12
+            roof = {"bound": "fp32", "achieved": work / (ms / 1e3) / 1e12, "peak": peak_t,
+                    "unit": "TFLOP/s", "peak_source": "nominal FP32 issue rate (152 SMs x 128 lanes x 2.07 GHz)"}
+        else:
+            work = 2.0 * nq * n * DIM * a.steps
+            peak_t = pk["bf16_tflops"] * (2.0 if name.startswith("fp8") else 1.0)
+            roof = {"bound": "tensor", "achieved": work / (ms / 1e3) / 1e12, "peak": peak_t,
+                    "unit": "TFLOP/s", "peak_source": pk["source"] + (" bf16 x2 (fp8)" if name.startswith("fp8") else " bf16")}
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        roof["kernel"] = name
+        roof["launches"] = nl
+        roof["kernel_ms_per_step"] = ms / a.steps
+        roof["traffic"] = None
+        roof["share_of_step"] = ms / (t_dev * 1e3)
+
+    cpu = None
+    if dist.rank == 0:
+        ns = a.cpu_sample or (32 if a.small else 192)
+        threads = os.cpu_count() or 1
+        qps_cpu, dt = cpu_sample_qps(base, q, K, ns, threads)
+        cpu = {"value": qps_cpu, "unit": "queries/s", "cores": threads, "kind": "port",
+               "sample": f"{ns} of the 10k queries against the full 1Mx128 base, k=100, "
+                         f"{threads} threads, {dt:.1f} s"}
+
+    if dist.rank == 0:
+        line = {
+            "metric": "QPS at recall@10>=0.95 (brute force, 1Mx128, k=100)",
+            "value": value, "unit": "queries/s", "n_gpus": dist.world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": t_max / a.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "bf16": "bf16", "fp8": "e4m3"}[head],
+            "data": "synthetic (seeded gaussian mixture; ann-benchmarks sets unavailable offline)",
+            "config": {"workload": WORKLOAD if not a.small else "small check", "n": n, "dim": DIM,
+                       "queries": nq, "k": K, "form": head, "l2_policy": "inputs larger than L2 (512 MB base)",
+                       "parallelism": f"replicas x{dist.world}"},
+            "forms": forms, "p50_ms": float(np.percentile(step_ms, 50)),
+            "p99_ms": float(np.percentile(step_ms, 99)), "wall_s": t_wall,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": launches, "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
+        }
+        print(json.dumps(line), flush=True)
+
+
+# ---- reference arm: the reference's CPU path (C port) on the host cores ------------
+def run_reference(a, dist: Dist):
+    if dist.rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    base, q = make_data(a.small)
+    threads = os.cpu_count() or 1
+    ns = a.cpu_sample or max(threads * 2, 16)
+    for i in range(a.warmup):
+        O.bf_search(base, q[:threads], K, O.EUCLIDEAN, threads=threads)
+    times = []
+    for s in range(a.steps):
+        qs = q[(s * ns) % q.shape[0]:][:ns]
+        t0 = time.perf_counter()
+        O.bf_search(base, qs, K, O.EUCLIDEAN, threads=threads)
+        times.append(time.perf_counter() - t0)
+    qps = ns * a.steps / sum(times)
+    sample = f"{ns} queries per step of the 10k against the full 1Mx128 base, k=100, {threads} threads"
+    print(json.dumps({
+        "impl": "reference", "metric": "QPS at recall@10>=0.95 (brute force, 1Mx128, k=100)",
+        "value": qps, "unit": "queries/s", "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": sum(times) / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded gaussian mixture)",
+        "config": {"workload": WORKLOAD, "n": base.shape[0], "dim": DIM, "queries": ns, "k": K,
+                   "form": "reference CPU scan (C port of src/index/bruteforce_idx.rs:47-73)"},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    a = args_parse()
+    dist = Dist()
+    if a.impl == "reference":
+        run_reference(a, dist)
+    else:
+        run_ours(a, dist)
+
+
+if __name__ == "__main__":
+    main()

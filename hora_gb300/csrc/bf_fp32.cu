@@ -1,0 +1,188 @@
+// bf_fp32.cu — exact FP32 scoring kernels on the CUDA cores.
+//
+// dist_tile_kernel is the workhorse of every exact path:
+//   TILE_FILTER  brute-force scan (BruteForceIndex::node_search_k,
+//                src/index/bruteforce_idx.rs:47-73): a row becomes a
+//                candidate of query q when its (distance, row) key beats the
+//                k-th best key found so far for q;
+//   TILE_DENSE   the first chunk of a scan: every row is a candidate;
+//   TILE_ARGMIN  k-means assignment (Kmeans::search_data, src/core/kmeans.rs:
+//                127-148): strict '<' from centre 0 == smallest (d, row) key;
+//   TILE_DIST    dense distances (coarse-centre probing, pq_idx.rs:416-421).
+#include <algorithm>
+
+#include "dist_tile.cuh"
+#include "internal.h"
+
+namespace hora {
+
+template <int MT, int MODE>
+__global__ void __launch_bounds__(kTileThreads, 1) dist_tile_kernel(TileParams p) {
+  extern __shared__ __align__(16) float smem[];
+  const int tid = threadIdx.x, tq = tid >> 4, tn = tid & 15;
+  const int64_t q0 = (int64_t)blockIdx.x * kTileQ;
+  float acc[8][8];
+
+  // query ids and per-query state of this thread's 8 queries
+  int64_t qid[8];
+  float qn[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    int64_t q = q0 + tq + 16 * i;
+    qid[i] = q < p.nq ? (p.qmap ? p.qmap[q] : q) : -1;
+    qn[i] = (MT == M_COS && qid[i] >= 0) ? p.qnorm[qid[i]] : 0.0f;
+  }
+
+  if (MODE == TILE_ARGMIN) {
+    uint64_t best[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) best[i] = kEmptyKey;
+    for (int64_t r0 = p.r_begin; r0 < p.r_end; r0 += kTileN) {
+      score_tile<MT>(acc, smem, p.Q, p.ldq, p.nq, q0, p.qmap, p.X, p.ldx, p.r_end, r0, p.ld);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        int64_t row = r0 + tn + 16 * j;
+        if (row >= p.r_end) continue;
+        float xn = MT == M_COS ? p.xnorm[row] : 0.0f;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          float d = MT == M_COS ? cosine_from_dot(acc[i][j], qn[i], xn) : acc[i][j];
+          uint64_t key = make_key(d, (uint32_t)row);
+          best[i] = key < best[i] ? key : best[i];
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+#pragma unroll
+      for (int off = 8; off >= 1; off >>= 1) {
+        uint64_t o = __shfl_xor_sync(0xffffffffu, best[i], off);
+        best[i] = o < best[i] ? o : best[i];
+      }
+      if (tn == 0 && qid[i] >= 0) p.out_key[qid[i]] = best[i];
+    }
+    return;
+  }
+
+  const int64_t r0 = p.r_begin + (int64_t)blockIdx.y * kTileN;
+  score_tile<MT>(acc, smem, p.Q, p.ldq, p.nq, q0, p.qmap, p.X, p.ldx, p.r_end, r0, p.ld);
+
+  uint64_t tau[8];
+  if (MODE == TILE_FILTER) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) tau[i] = qid[i] >= 0 ? p.best[qid[i] * p.k + (p.k - 1)] : 0ull;
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    int64_t row = r0 + tn + 16 * j;
+    if (row >= p.r_end) continue;
+    float xn = MT == M_COS ? p.xnorm[row] : 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (qid[i] < 0) continue;
+      float d = MT == M_COS ? cosine_from_dot(acc[i][j], qn[i], xn) : acc[i][j];
+      if (MODE == TILE_DIST) {
+        p.out_dist[qid[i] * p.ldo + (row - p.r_begin)] = d;
+      } else {
+        uint64_t key = make_key(d, (uint32_t)row);
+        if (MODE == TILE_DENSE) {
+          p.cand[qid[i] * p.cap + (row - p.r_begin)] = key;
+        } else if (key < tau[i]) {
+          uint32_t slot = atomicAdd(p.count + qid[i], 1u);
+          if (slot < (uint32_t)p.cap) p.cand[qid[i] * p.cap + slot] = key;
+        }
+      }
+    }
+  }
+}
+
+template <int MT, int MODE>
+static int launch_one(const TileParams &p, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    HORA_CUDA_TRY(cudaFuncSetAttribute(dist_tile_kernel<MT, MODE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem));
+    attr_set = true;
+  }
+  dim3 grid(ceil_div(p.nq, kTileQ), 1);
+  if (MODE != TILE_ARGMIN) grid.y = ceil_div(p.r_end - p.r_begin, kTileN);
+  if (grid.x == 0 || grid.y == 0) return HORA_OK;
+  if (grid.y > 65535) return fail(HORA_ECAP, "dist_tile: chunk too large for one launch");
+  ProfScope ps(MODE == TILE_ARGMIN ? "fp32_tile_argmin"
+               : MODE == TILE_DIST ? "fp32_tile_dist" : "fp32_tile_scan", s);
+  dist_tile_kernel<MT, MODE><<<grid, kTileThreads, kTileSmem, s>>>(p);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+template <int MT>
+static int launch_mode(int mode, const TileParams &p, cudaStream_t s) {
+  switch (mode) {
+    case TILE_FILTER: return launch_one<MT, TILE_FILTER>(p, s);
+    case TILE_DENSE: return launch_one<MT, TILE_DENSE>(p, s);
+    case TILE_ARGMIN: return launch_one<MT, TILE_ARGMIN>(p, s);
+    case TILE_DIST: return launch_one<MT, TILE_DIST>(p, s);
+  }
+  return fail(HORA_EINVAL, "dist_tile: bad mode");
+}
+
+int launch_dist_tile(int metric, int mode, const TileParams &p, cudaStream_t s) {
+  if (p.ld % 4 || p.ldq % 4 || p.ldx % 4) return fail(HORA_EINVAL, "dist_tile: pitch not a multiple of 4");
+  switch (metric) {
+    case M_L2: return launch_mode<M_L2>(mode, p, s);
+    case M_L1: return launch_mode<M_L1>(mode, p, s);
+    case M_IP: return launch_mode<M_IP>(mode, p, s);
+    case M_COS: return launch_mode<M_COS>(mode, p, s);
+  }
+  return fail(HORA_EMETRIC, "unknown method");
+}
+
+// ---- row norms: f32 sqrt(sum x^2) in reference order, and f64 sum x^2 ----------
+__global__ void row_norms_kernel(const float *X, int64_t n, int64_t ld, int64_t dim, float *nf,
+                                 double *sq) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const float *x = X + r * ld;
+  float s = 0.0f;
+  double s64 = 0.0;
+  for (int64_t t = 0; t < dim; ++t) {
+    float v = x[t];
+    s = __fadd_rn(s, __fmul_rn(v, v));
+    s64 += (double)v * (double)v;
+  }
+  if (nf) nf[r] = __fsqrt_rn(s);
+  if (sq) sq[r] = s64;
+}
+
+int launch_row_norms(const float *X, int64_t n, int64_t ld, int64_t dim, float *nf, double *sq,
+                     cudaStream_t s) {
+  if (n <= 0) return HORA_OK;
+  row_norms_kernel<<<ceil_div(n, 256), 256, 0, s>>>(X, n, ld, dim, nf, sq);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+__global__ void check_finite_kernel(const float *X, int64_t n, int64_t ld, int64_t dim,
+                                    uint32_t *flag) {
+  int64_t total = n * dim;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float v = X[(i / dim) * ld + (i % dim)];
+    if (!isfinite(v)) {
+      atomicOr(flag, 1u);
+      return;
+    }
+  }
+}
+
+int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint32_t *flag,
+                        cudaStream_t s) {
+  if (n <= 0) return HORA_OK;
+  int64_t total = n * dim;
+  int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 152 * 16);
+  check_finite_kernel<<<blocks, 256, 0, s>>>(X, n, ld, dim, flag);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+}  // namespace hora

@@ -1,0 +1,159 @@
+// common.cuh — shared device helpers and host plumbing for libhora_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/hora_gb300.h"
+
+namespace hora {
+
+// ---- errors ---------------------------------------------------------------
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+extern std::atomic<uint64_t> g_launches;
+
+#define HORA_CUDA_TRY(expr)                                                        \
+  do {                                                                             \
+    cudaError_t e__ = (expr);                                                      \
+    if (e__ != cudaSuccess)                                                        \
+      return ::hora::fail(e__ == cudaErrorMemoryAllocation ? HORA_EOOM : HORA_ECUDA, \
+                          std::string(#expr) + ": " + cudaGetErrorString(e__));    \
+  } while (0)
+
+#define HORA_TRY(expr)           \
+  do {                           \
+    int rc__ = (expr);           \
+    if (rc__ != HORA_OK) return rc__; \
+  } while (0)
+
+// Counts a launch and checks the launch error.
+#define HORA_LAUNCHED()                                                           \
+  do {                                                                            \
+    ::hora::g_launches.fetch_add(1, std::memory_order_relaxed);                   \
+    cudaError_t e__ = cudaGetLastError();                                         \
+    if (e__ != cudaSuccess)                                                       \
+      return ::hora::fail(HORA_ECUDA, std::string("launch: ") + cudaGetErrorString(e__)); \
+  } while (0)
+
+// ---- kernel timing ----------------------------------------------------------
+// While profiling is on, a ProfScope records CUDA events around one launch on
+// the launching stream; hora_profile_report() turns them into per-kernel time.
+extern std::atomic<int> g_profile;
+void prof_record(const char *name, cudaEvent_t a, cudaEvent_t b);
+struct ProfScope {
+  const char *name;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(const char *n, cudaStream_t st) : name(n), s(st) {
+    if (g_profile.load(std::memory_order_relaxed)) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, s);
+    }
+  }
+  ~ProfScope() {
+    if (a) {
+      cudaEventRecord(b, s);
+      prof_record(name, a, b);
+    }
+  }
+};
+
+// ---- metric ids ------------------------------------------------------------
+enum MetricId : int {
+  M_UNKNOWN = HORA_METRIC_UNKNOWN,
+  M_L1 = HORA_METRIC_MANHATTAN,
+  M_IP = HORA_METRIC_DOT_PRODUCT,
+  M_L2 = HORA_METRIC_EUCLIDEAN,
+  M_COS = HORA_METRIC_COSINE_SIMILARITY,
+};
+
+// ---- sort keys ---------------------------------------------------------------
+// A candidate is one 64-bit key: the order-preserving image of its f32
+// distance in the high word and its row number in the low word, so that an
+// unsigned compare orders by (distance, row) — ties go to the lower row.
+constexpr uint64_t kEmptyKey = ~0ull;
+
+__host__ __device__ __forceinline__ uint32_t f2ord(float f) {
+  uint32_t u;
+#ifdef __CUDA_ARCH__
+  u = __float_as_uint(f);
+#else
+  memcpy(&u, &f, 4);
+#endif
+  if (u == 0x80000000u) u = 0;                             // -0 == +0
+  if ((u & 0x7f800000u) == 0x7f800000u && (u & 0x007fffffu)) u = 0x7fc00000u;  // one NaN, after +inf
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__host__ __device__ __forceinline__ float ord2f(uint32_t o) {
+  uint32_t u = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+  float f;
+#ifdef __CUDA_ARCH__
+  f = __uint_as_float(u);
+#else
+  memcpy(&f, &u, 4);
+#endif
+  return f;
+}
+
+__host__ __device__ __forceinline__ uint64_t make_key(float d, uint32_t row) {
+  return ((uint64_t)f2ord(d) << 32) | row;
+}
+__host__ __device__ __forceinline__ float key_dist(uint64_t k) { return ord2f((uint32_t)(k >> 32)); }
+__host__ __device__ __forceinline__ uint32_t key_row(uint64_t k) { return (uint32_t)k; }
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+// ---- device memory -------------------------------------------------------------
+// Grow-only device buffer owned by an index or a search context.
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  // Ensures capacity; contents are not preserved unless keep is set.
+  int reserve(size_t want, cudaStream_t s = 0, bool keep = false) {
+    if (want <= bytes) return HORA_OK;
+    size_t cap = want < 256 ? 256 : want;
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, cap);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(HORA_EOOM, std::string("cudaMalloc(") + std::to_string(cap) + "): " + cudaGetErrorString(e));
+    }
+    if (keep && ptr && bytes) {
+      e = cudaMemcpyAsync(p, ptr, bytes, cudaMemcpyDeviceToDevice, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) {
+        cudaFree(p);
+        return fail(HORA_ECUDA, std::string("grow copy: ") + cudaGetErrorString(e));
+      }
+    }
+    release();
+    ptr = p;
+    bytes = cap;
+    return HORA_OK;
+  }
+  template <class T>
+  T *as() const { return reinterpret_cast<T *>(ptr); }
+};
+
+// True when p is device (or managed) memory visible to the current device.
+bool is_device_ptr(const void *p);
+
+}  // namespace hora

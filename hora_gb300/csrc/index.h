@@ -1,0 +1,91 @@
+// index.h — the handle behind hora_index* (shared by the translation units).
+#pragma once
+
+#include <memory>
+#include <mutex>
+
+#include "internal.h"
+
+namespace hora {
+
+struct IvfState;   // ivfpq.cu
+struct LowpState;  // bf_lowp.cu
+struct NprobeModel;  // nprobe_mlp.cu
+
+void ivf_state_free(IvfState *);
+void lowp_state_free(LowpState *);
+void nprobe_model_free(NprobeModel *);
+struct IvfDeleter { void operator()(IvfState *p) const { ivf_state_free(p); } };
+struct LowpDeleter { void operator()(LowpState *p) const { lowp_state_free(p); } };
+struct NprobeDeleter { void operator()(NprobeModel *p) const { nprobe_model_free(p); } };
+
+}  // namespace hora
+
+struct hora_index {
+  int kind = HORA_INDEX_BRUTE_FORCE;
+  uint64_t dim = 0, ld = 0;  // ld: row pitch in floats (dim rounded up to 4, zero padded)
+  hora_ivfpq_params ivf{};
+  int metric = HORA_METRIC_UNKNOWN;
+  bool built = false;
+  int64_t n = 0, cap_rows = 0;
+  hora::DevBuf base;  // cap_rows x ld f32, insertion order
+  hora::DevBuf ids;   // cap_rows u64 user ids
+  hora::DevBuf xnorm; // n f32 sqrt norms (cosine)
+  hora::DevBuf xsq64; // n f64 squared norms (GEMM forms)
+  bool norms_valid = false;
+
+  // GPU-only options
+  int precision = HORA_PREC_FP32;
+  int rerank = 0;
+  int cand_cap = 4096;
+  int accum_f64 = 1;
+  uint64_t seed = 0x686f7261ull;
+  uint64_t train_size = 0;
+  int learned_nprobe = 0;
+  double nprobe_margin = 0.0;
+  int nprobe_max = 0;
+  int ivf_rerank = 0;
+
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  hora::SearchWorkspace ws;
+  std::unique_ptr<hora::IvfState, hora::IvfDeleter> ivfs;
+  std::unique_ptr<hora::LowpState, hora::LowpDeleter> lowp;
+  std::unique_ptr<hora::NprobeModel, hora::NprobeDeleter> nprobe;
+  // last search diagnostics
+  int last_retries = 0;
+  double last_ms = 0.0;
+};
+
+namespace hora {
+
+BaseView base_view(hora_index *h);
+int ensure_norms(hora_index *h, cudaStream_t s);
+// Copies nq x dim queries (host or device) into ws.q with pitch h->ld, checks
+// finiteness and computes f32 norms when the metric needs them.
+int stage_queries(hora_index *h, const float *queries, int64_t nq, SearchWorkspace &ws,
+                  cudaStream_t s);
+
+// Brute force with the handle's precision option; writes nq x k keys.
+int bf_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
+                   cudaStream_t s);
+
+// Low-precision scoring + FP32 rerank (bf_lowp.cu).
+int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
+                     cudaStream_t s);
+
+// IVF-PQ (ivfpq.cu)
+int ivf_build(hora_index *h);
+int ivf_search_keys(hora_index *h, int64_t nq, int k, int64_t nprobe, const uint32_t *d_nprobe,
+                    SearchWorkspace &ws, uint64_t *d_best, cudaStream_t s);
+int ivf_layout(const hora_index *h, uint64_t *n_list, uint64_t *n_sub, uint64_t *sub_bits,
+               uint64_t *dmax);
+int ivf_export(const hora_index *h, float *centers, int64_t *offsets, int64_t *items,
+               float *codebooks, uint8_t *codes, uint8_t *trained);
+int ivf_set_codebooks(hora_index *h, const float *centers, const float *codebooks);
+int ivf_dump(const hora_index *h, FILE *f);
+int ivf_load(hora_index *h, FILE *f);
+size_t ivf_device_bytes(const hora_index *h);
+int ivf_info(const hora_index *h, std::string &out);
+
+}  // namespace hora

@@ -1,0 +1,85 @@
+// internal.h — host-side interfaces between the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace hora {
+
+// ---- exact FP32 distance tiles (bf_fp32.cu) ----------------------------------
+enum TileMode : int { TILE_FILTER = 0, TILE_DENSE = 1, TILE_ARGMIN = 2, TILE_DIST = 3 };
+
+struct TileParams {
+  const float *Q = nullptr;  // query rows (pitch ldq floats), row i read as qmap[i] if qmap
+  int64_t ldq = 0;
+  int64_t nq = 0;            // rows of the tile's query list
+  const int *qmap = nullptr; // list slot -> query id (nullptr: identity)
+  const float *X = nullptr;  // base rows (pitch ldx floats)
+  int64_t ldx = 0;
+  int64_t r_begin = 0, r_end = 0;  // base rows scored
+  int64_t ld = 0;                  // columns scored (padded dimension)
+  const float *qnorm = nullptr, *xnorm = nullptr;  // cosine only
+  // TILE_FILTER / TILE_DENSE: candidate append against best[qid*k + k-1]
+  uint64_t *best = nullptr;
+  int k = 0;
+  uint64_t *cand = nullptr;
+  int cap = 0;
+  uint32_t *count = nullptr;
+  // TILE_ARGMIN: per query smallest (distance,row) key
+  uint64_t *out_key = nullptr;
+  // TILE_DIST: dense f32 distances out[qid*ldo + (row - r_begin)]
+  float *out_dist = nullptr;
+  int64_t ldo = 0;
+};
+
+int launch_dist_tile(int metric, int mode, const TileParams &p, cudaStream_t s);
+int launch_row_norms(const float *X, int64_t n, int64_t ld, int64_t dim, float *norm_f32,
+                     double *sq_f64, cudaStream_t s);
+int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint32_t *flag,
+                        cudaStream_t s);
+
+// ---- selection (topk.cu) ------------------------------------------------------
+// Merges each query's candidates into its sorted k-best key list (dedup by
+// key).  dense_n > 0: candidates are the first dense_n slots, count ignored.
+int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap,
+                      int dense_n, const int *qlist, int64_t nlist, uint8_t *ovf_flag,
+                      uint32_t *ovf_counter, cudaStream_t s);
+int merge_smem_bytes(int k, int cap);
+// Sorted keys -> (ids via the id table, distances); empty keys -> NO_ID, +inf.
+int launch_keys_to_results(const uint64_t *keys, int64_t n_keys, const uint64_t *id_table,
+                           uint64_t *ids_out, float *dist_out, cudaStream_t s);
+// Gathers result rows for search_nodes.
+int launch_gather_rows(const uint64_t *keys, int64_t n_keys, const float *base, int64_t ld,
+                       int64_t dim, float *out, cudaStream_t s);
+// Per-row top-k of a dense f32 matrix (rows x cols): k <= 1024.
+int launch_rows_topk(const float *D, int64_t rows, int64_t cols, int64_t ldd, int k,
+                     uint64_t *out_keys, cudaStream_t s);
+
+// ---- brute force (bf_search.cu) ---------------------------------------------------
+struct SearchWorkspace {
+  DevBuf q, qnorm, best, cand, count, ovf_flag, ovf_counter, qlist, out_ids, out_dist, rows,
+      keys2, tmp;
+  std::vector<uint8_t> h_flags;
+};
+
+struct BaseView {
+  const float *X;  // n x ld
+  int64_t n, ld, dim;
+  const float *xnorm;  // f32 norms (cosine)
+};
+
+// Exact k-best keys for nq staged queries (pitch ld) against the base.
+int bf_topk_exact(const BaseView &b, int metric, const float *dQ, const float *dqnorm, int64_t nq,
+                  int k, int cand_cap, SearchWorkspace &ws, uint64_t *d_best, cudaStream_t s,
+                  int *retries_out);
+
+// ---- error helpers ------------------------------------------------------------------
+const char *metric_name(int m);
+
+}  // namespace hora

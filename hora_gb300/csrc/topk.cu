@@ -1,0 +1,200 @@
+// topk.cu — k-best selection.
+//
+// The reference keeps a bounded std BinaryHeap per query (push, pop when
+// longer than k: src/index/bruteforce_idx.rs:49-61, pq_idx.rs:181-191,
+// 429-436) and returns it ascending.  Here every query owns a sorted list of
+// k (distance,row) keys in HBM; candidates found by the scoring kernels are
+// merged into it by one CTA per query with a shared-memory bitonic sort.
+// Ties in distance resolve to the lower row, a deterministic order (the
+// reference's order at exact ties depends on heap positions).
+#include <algorithm>
+
+#include "internal.h"
+
+namespace hora {
+
+constexpr int kMergeThreads = 512;
+
+__device__ __forceinline__ void block_bitonic_sort(uint64_t *sk, int P) {
+  for (int size = 2; size <= P; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < (P >> 1); i += blockDim.x) {
+        int lo = 2 * i - (i & (stride - 1));
+        int hi = lo + stride;
+        bool asc = (lo & size) == 0;
+        uint64_t a = sk[lo], b = sk[hi];
+        if ((a > b) == asc) {
+          sk[lo] = b;
+          sk[hi] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Exclusive block scan of one int per thread (blockDim.x <= 1024).
+__device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int *total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) warp_sums[lane] = w;
+  }
+  __syncthreads();
+  int base = wid ? warp_sums[wid - 1] : 0;
+  *total = warp_sums[nw - 1];
+  __syncthreads();
+  return base + x - v;
+}
+
+__global__ void __launch_bounds__(kMergeThreads) merge_topk_kernel(
+    uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n,
+    const int *qlist, uint8_t *ovf_flag, uint32_t *ovf_counter) {
+  extern __shared__ uint64_t sk[];
+  __shared__ int warp_sums[32];
+  const int64_t q = qlist ? qlist[blockIdx.x] : blockIdx.x;
+  uint32_t c = dense_n > 0 ? (uint32_t)dense_n : count[q];
+  if (c == 0) return;
+  const bool ovf = c > (uint32_t)cap;
+  if (ovf) c = cap;
+  const int total = (int)c + k;
+  int P = 1;
+  while (P < total) P <<= 1;
+  const uint64_t *cq = cand + q * cap;
+  uint64_t *bq = best + q * k;
+  for (int i = threadIdx.x; i < P; i += blockDim.x)
+    sk[i] = i < (int)c ? cq[i] : (i < total ? bq[i - c] : kEmptyKey);
+  __syncthreads();
+  block_bitonic_sort(sk, P);
+  // keep the first occurrence of each key (a row can be offered twice when a
+  // scan is repeated after a capacity overflow), compact the first k
+  const int per = (P + blockDim.x - 1) / blockDim.x;
+  const int beg = threadIdx.x * per, end = min(P, beg + per);
+  int mine = 0;
+  for (int i = beg; i < end; ++i) mine += (sk[i] != kEmptyKey && (i == 0 || sk[i] != sk[i - 1]));
+  int tot;
+  int pos = block_exclusive_scan(mine, warp_sums, &tot);
+  for (int i = beg; i < end && pos < k; ++i) {
+    if (sk[i] != kEmptyKey && (i == 0 || sk[i] != sk[i - 1])) {
+      bq[pos] = sk[i];
+      ++pos;
+    }
+  }
+  for (int i = tot + threadIdx.x; i < k; i += blockDim.x) bq[i] = kEmptyKey;
+  if (threadIdx.x == 0) {
+    if (dense_n <= 0) count[q] = 0;
+    if (ovf) {
+      ovf_flag[q] = 1;
+      atomicAdd(ovf_counter, 1u);
+    }
+  }
+}
+
+int merge_smem_bytes(int k, int cap) {
+  int P = 1;
+  while (P < k + cap) P <<= 1;
+  return P * 8;
+}
+
+int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap,
+                      int dense_n, const int *qlist, int64_t nlist, uint8_t *ovf_flag,
+                      uint32_t *ovf_counter, cudaStream_t s) {
+  if (nlist <= 0) return HORA_OK;
+  int smem = merge_smem_bytes(k, dense_n > 0 ? dense_n : cap);
+  if (smem > 200 * 1024) return fail(HORA_ECAP, "merge: k + candidate capacity too large");
+  static int attr = 0;
+  if (smem > attr) {
+    HORA_CUDA_TRY(cudaFuncSetAttribute(merge_topk_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = 200 * 1024;
+  }
+  ProfScope ps("topk_merge", s);
+  merge_topk_kernel<<<(unsigned)nlist, kMergeThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
+                                                                qlist, ovf_flag, ovf_counter);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+__global__ void keys_to_results_kernel(const uint64_t *keys, int64_t n, const uint64_t *idt,
+                                       uint64_t *ids, float *dist) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t k = keys[i];
+  if (k == kEmptyKey) {
+    if (ids) ids[i] = HORA_NO_ID;
+    if (dist) dist[i] = __int_as_float(0x7f800000);
+  } else {
+    if (ids) ids[i] = idt ? idt[key_row(k)] : key_row(k);
+    if (dist) dist[i] = key_dist(k);
+  }
+}
+
+int launch_keys_to_results(const uint64_t *keys, int64_t n, const uint64_t *idt, uint64_t *ids,
+                           float *dist, cudaStream_t s) {
+  if (n <= 0) return HORA_OK;
+  ProfScope ps("keys_to_results", s);
+  keys_to_results_kernel<<<ceil_div(n, 256), 256, 0, s>>>(keys, n, idt, ids, dist);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+__global__ void gather_rows_kernel(const uint64_t *keys, int64_t n, const float *base, int64_t ld,
+                                   int64_t dim, float *out) {
+  int64_t r = blockIdx.x;
+  uint64_t k = keys[r];
+  for (int64_t t = threadIdx.x; t < dim; t += blockDim.x)
+    out[r * dim + t] = k == kEmptyKey ? 0.0f : base[(int64_t)key_row(k) * ld + t];
+}
+
+int launch_gather_rows(const uint64_t *keys, int64_t n, const float *base, int64_t ld,
+                       int64_t dim, float *out, cudaStream_t s) {
+  if (n <= 0) return HORA_OK;
+  gather_rows_kernel<<<(unsigned)n, 128, 0, s>>>(keys, n, base, ld, dim, out);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+__global__ void __launch_bounds__(kMergeThreads) rows_topk_kernel(const float *D, int64_t cols,
+                                                                  int64_t ldd, int k, int P,
+                                                                  uint64_t *out) {
+  extern __shared__ uint64_t sk[];
+  const int64_t r = blockIdx.x;
+  for (int i = threadIdx.x; i < P; i += blockDim.x)
+    sk[i] = i < cols ? make_key(D[r * ldd + i], (uint32_t)i) : kEmptyKey;
+  __syncthreads();
+  block_bitonic_sort(sk, P);
+  for (int i = threadIdx.x; i < k; i += blockDim.x) out[r * k + i] = sk[i];
+}
+
+int launch_rows_topk(const float *D, int64_t rows, int64_t cols, int64_t ldd, int k,
+                     uint64_t *out, cudaStream_t s) {
+  if (rows <= 0) return HORA_OK;
+  int P = 1;
+  while (P < cols || P < k) P <<= 1;
+  if (P * 8 > 200 * 1024) return fail(HORA_ECAP, "rows_topk: too many columns");
+  static bool attr = false;
+  if (!attr) {
+    HORA_CUDA_TRY(cudaFuncSetAttribute(rows_topk_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  ProfScope ps("rows_topk", s);
+  rows_topk_kernel<<<(unsigned)rows, kMergeThreads, P * 8, s>>>(D, cols, ldd, k, P, out);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+}  // namespace hora
