@@ -45,6 +45,7 @@ def args_parse():
     ap.add_argument("--forms", default="fp32,bf16,fp8")
     ap.add_argument("--cpu-sample", type=int, default=0, help="queries in the CPU baseline sample")
     ap.add_argument("--small", action="store_true", help="tiny workload for a quick check")
+    ap.add_argument("--nq", type=int, default=0, help="override the number of queries (profiling)")
     return ap.parse_args()
 
 
@@ -145,9 +146,11 @@ def peaks() -> dict:
             "source": "fallback"}
 
 
-def make_data(small: bool):
+def make_data(small: bool, nq_override: int = 0):
     from hora_gb300 import synth
     n, nq = (20_000, 512) if small else (N_BASE, N_Q)
+    if nq_override:
+        nq = nq_override
     base = synth.mixture(n, DIM, N_CENTERS, stream=1)
     q = synth.mixture(nq, DIM, N_CENTERS, stream=2)
     return base, q
@@ -180,7 +183,7 @@ def run_ours(a, dist: Dist):
 
     torch.cuda.set_device(dist.local)
     B.build()
-    base, q = make_data(a.small)
+    base, q = make_data(a.small, a.nq)
     n, nq = base.shape[0], q.shape[0]
     ix = H.BruteForceIndex(DIM)
     ix.madd(torch.from_numpy(base).cuda(), None)
@@ -297,7 +300,7 @@ def run_ours(a, dist: Dist):
 
     cpu = None
     if dist.rank == 0:
-        ns = a.cpu_sample or (32 if a.small else 192)
+        ns = min(q.shape[0], a.cpu_sample or (32 if a.small else 2048))
         threads = os.cpu_count() or 1
         qps_cpu, dt = cpu_sample_qps(base, q, K, ns, threads)
         cpu = {"value": qps_cpu, "unit": "queries/s", "cores": threads, "kind": "port",
@@ -328,7 +331,7 @@ def run_reference(a, dist: Dist):
         return
     from oracle import oracle as O
     O.build()
-    base, q = make_data(a.small)
+    base, q = make_data(a.small, a.nq)
     threads = os.cpu_count() or 1
     ns = a.cpu_sample or max(threads * 2, 16)
     for i in range(a.warmup):

@@ -204,6 +204,10 @@ int hora_index_create(int kind, uint64_t dim, const void *params, hora_index **o
     hora_ivfpq_params_default(&h->ivf);
     if (params) h->ivf = *reinterpret_cast<const hora_ivfpq_params *>(params);
     const hora_ivfpq_params &p = h->ivf;
+    if (dim > 1024) {
+      delete h;
+      return fail(HORA_ECAP, "IVF-PQ supports dimension <= 1024");
+    }
     if (p.n_sub == 0 || p.n_sub > dim) {
       delete h;
       return fail(HORA_EINVAL, "n_sub must be in [1, dim]");

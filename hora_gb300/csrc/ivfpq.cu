@@ -1,15 +1,1225 @@
-// ivfpq.cu — placeholder, replaced by the IVF-PQ implementation.
+// ivfpq.cu — IVFPQIndex ("PQIVFIndex") build and search on the GPU.
+//
+// Build (IVFPQIndex::train, src/index/pq_idx.rs:357-396):
+//   coarse k-means over the (training) items with the index metric
+//   (Kmeans::train, src/core/kmeans.rs:195-207): init_center, then per epoch
+//   assign (exact FP32 tile kernel, strict '<' = smallest (d,row) key),
+//   update (centroid sums in FP64 or FP32 in item order, empty -> zero) and
+//   split_center (seeded splitmix64 stream, one thread: the reference's
+//   walk is sequential);  assign every item -> inverted lists in item order;
+//   per (list, subspace) PQ k-means on the residuals x - c_list with 2^bits
+//   centres and Euclidean distance (PQIndex::train_center, pq_idx.rs:122-149),
+//   one CTA per instance running all epochs;  encode (pq_idx.rs:143-144).
+// Search (IVFPQIndex::search_knn_adc, pq_idx.rs:408-439):
+//   coarse distances (exact FP32 tile kernel) -> the nprobe nearest lists;
+//   (query, list) pairs sorted by list so consecutive CTAs reuse the list's
+//   codebook from L1/L2; per pair the LUT (pq_idx.rs:170-179) in shared
+//   memory, the ADC scan (pq_idx.rs:182-188, sequential f32 sum over
+//   subspaces) and a radix select of the pair's k best; a final per-query
+//   merge keeps the k smallest (distance,row) keys.  Optional exact FP32
+//   rerank of a widened ADC shortlist (not in the reference; off by default).
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "dist_tile.cuh"
 #include "index.h"
+
 namespace hora {
-struct IvfState {};
+
+struct IvfState {
+  int64_t n_list = 0, n_sub = 0, K = 0, dmax = 0, sub_bits = 0, n_items = 0;
+  std::vector<int> sub_begin, sub_len;
+  DevBuf sub_begin_d, sub_len_d;
+  DevBuf centers;  // n_list x ld (zero padded)
+  DevBuf cnorm;    // n_list f32 (cosine)
+  DevBuf offsets;  // n_list + 1 int64
+  DevBuf items;    // n u32 rows, list order
+  DevBuf codes;    // n x n_sub u8, list order
+  DevBuf books;    // n_list x n_sub x K x dmax f32
+  DevBuf trained;  // n_list u8
+  std::vector<int64_t> h_offsets;
+  std::vector<uint8_t> h_trained;
+  int64_t max_list = 0;
+  // search scratch
+  DevBuf coarse, probes, pair_q, pair_c, pair_slot, pair_cnt, pair_off, cand, best_r, nprobe_q;
+  DevBuf tmp_keys;
+};
+
 void ivf_state_free(IvfState *p) { delete p; }
-int ivf_build(hora_index *) { return fail(HORA_ENOTIMPL, "ivfpq: not built yet"); }
-int ivf_search_keys(hora_index *, int64_t, int, int64_t, const uint32_t *, SearchWorkspace &, uint64_t *, cudaStream_t) { return fail(HORA_ENOTIMPL, "ivfpq"); }
-int ivf_layout(const hora_index *, uint64_t *, uint64_t *, uint64_t *, uint64_t *) { return fail(HORA_ENOTIMPL, "ivfpq"); }
-int ivf_export(const hora_index *, float *, int64_t *, int64_t *, float *, uint8_t *, uint8_t *) { return fail(HORA_ENOTIMPL, "ivfpq"); }
-int ivf_set_codebooks(hora_index *, const float *, const float *) { return fail(HORA_ENOTIMPL, "ivfpq"); }
-int ivf_dump(const hora_index *, FILE *) { return fail(HORA_ENOTIMPL, "ivfpq"); }
-int ivf_load(hora_index *, FILE *) { return fail(HORA_ENOTIMPL, "ivfpq"); }
-size_t ivf_device_bytes(const hora_index *) { return 0; }
-int ivf_info(const hora_index *, std::string &out) { out = "{}"; return HORA_OK; }
+
+// ---------------------------------------------------------------------------
+// device RNG: the splitmix64 stream shared with the oracle
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
 }
+__host__ __device__ __forceinline__ uint64_t instance_seed(uint64_t seed, uint64_t inst) {
+  return mix64(seed ^ mix64(inst * 0xD1B54A32D192ED03ull + 0x9E3779B97F4A7C15ull));
+}
+__device__ __forceinline__ double rng_unit(uint64_t &s) {
+  s += 0x9E3779B97F4A7C15ull;
+  return (double)(mix64(s) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// ---------------------------------------------------------------------------
+// k-means pieces (coarse, full dimension)
+
+// Kmeans::init_center (kmeans.rs:50-86): column means accumulated in item
+// order, then mean +1 / -1 with the reference's (i & (1 << j)) == 1 test.
+__global__ void coarse_init_kernel(const float *X, int64_t ld, int64_t n, int64_t dim,
+                                   int64_t n_center, int accum_f64, float *centers) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= dim) return;
+  float mean;
+  if (accum_f64) {
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += (double)X[i * ld + j];
+    mean = (float)(s / (double)n);
+  } else {
+    float s = 0.0f;
+    for (int64_t i = 0; i < n; ++i) s = __fadd_rn(s, X[i * ld + j]);
+    mean = __fdiv_rn(s, (float)n);
+  }
+  for (int64_t i = 0; i < n_center; ++i) {
+    bool plus = ((uint64_t)i & ((uint64_t)1 << ((uint64_t)j & 63))) == 1;
+    centers[i * ld + j] = plus ? __fadd_rn(mean, 1.0f) : __fsub_rn(mean, 1.0f);
+  }
+}
+
+// Stable counting sort of n labels in [0, C): block histograms, per-label
+// block prefix, then an in-order warp scatter inside each block.
+constexpr int kSortBlock = 1024;
+
+__global__ void label_hist_kernel(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
+                                  uint32_t *block_counts) {
+  extern __shared__ uint32_t hist[];
+  for (int c = threadIdx.x; c < C; c += blockDim.x) hist[c] = 0;
+  __syncthreads();
+  int64_t lo = (int64_t)blockIdx.x * kSortBlock;
+  for (int64_t i = lo + threadIdx.x; i < min(n, lo + kSortBlock); i += blockDim.x) {
+    uint32_t l = keys ? key_row(keys[i]) : labels[i];
+    atomicAdd(&hist[l], 1u);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) block_counts[(int64_t)blockIdx.x * C + c] = hist[c];
+}
+
+// per label: running offsets over blocks; totals -> counts[c]
+__global__ void label_block_scan_kernel(uint32_t *block_counts, int64_t nblocks, int C,
+                                        int64_t *counts) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  uint32_t run = 0;
+  for (int64_t b = 0; b < nblocks; ++b) {
+    uint32_t v = block_counts[b * C + c];
+    block_counts[b * C + c] = run;
+    run += v;
+  }
+  counts[c] = run;
+}
+
+// exclusive scan of C counts into offsets[0..C] (one CTA)
+__global__ void offsets_scan_kernel(const int64_t *counts, int C, int64_t *offsets) {
+  __shared__ int64_t part[1024];
+  int t = threadIdx.x;
+  int per = (C + blockDim.x - 1) / blockDim.x;
+  int lo = t * per, hi = min(C, lo + per);
+  int64_t s = 0;
+  for (int c = lo; c < hi; ++c) s += counts[c];
+  part[t] = s;
+  __syncthreads();
+  if (t == 0) {
+    int64_t run = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      int64_t v = part[i];
+      part[i] = run;
+      run += v;
+    }
+    offsets[C] = run;
+  }
+  __syncthreads();
+  int64_t run = part[t];
+  for (int c = lo; c < hi; ++c) {
+    offsets[c] = run;
+    run += counts[c];
+  }
+}
+
+__global__ void label_scatter_kernel(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
+                                     const uint32_t *block_counts, const int64_t *offsets,
+                                     uint32_t *members) {
+  extern __shared__ uint32_t rank[];
+  for (int c = threadIdx.x; c < C; c += blockDim.x) rank[c] = 0;
+  __syncthreads();
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  int64_t lo = (int64_t)blockIdx.x * kSortBlock;
+  int64_t hi = min(n, lo + kSortBlock);
+  for (int64_t base = lo; base < hi; base += 32) {
+    int64_t i = base + lane;
+    bool ok = i < hi;
+    uint32_t l = ok ? (keys ? key_row(keys[i]) : labels[i]) : 0xffffffffu;
+    unsigned peers = __match_any_sync(0xffffffffu, l);
+    unsigned lower = peers & ((1u << lane) - 1u);
+    uint32_t r0 = ok ? rank[l] : 0;
+    __syncwarp();
+    if (ok) {
+      uint32_t pos = r0 + __popc(lower);
+      members[offsets[l] + block_counts[(int64_t)blockIdx.x * C + l] + pos] = (uint32_t)i;
+      if (lower == 0) rank[l] = r0 + __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+// new centres: per (centre, column) sequential sum over members in item order
+__global__ void center_sum_kernel(const float *X, int64_t ld, const uint32_t *members,
+                                  const int64_t *offsets, int C, int64_t dim, int accum_f64,
+                                  float *centers) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)C * dim) return;
+  int c = (int)(t / dim);
+  int64_t j = t % dim;
+  int64_t lo = offsets[c], hi = offsets[c + 1];
+  float out = 0.0f;
+  if (hi > lo) {
+    if (accum_f64) {
+      double s = 0.0;
+      for (int64_t p = lo; p < hi; ++p) s += (double)X[(int64_t)members[p] * ld + j];
+      out = (float)(s / (double)(hi - lo));
+    } else {
+      float s = 0.0f;
+      for (int64_t p = lo; p < hi; ++p) s = __fadd_rn(s, X[(int64_t)members[p] * ld + j]);
+      out = __fdiv_rn(s, (float)(hi - lo));
+    }
+  }
+  centers[(int64_t)c * ld + j] = out;
+}
+
+// Kmeans::split_center (kmeans.rs:150-193), sequential like the reference.
+// A draw at pick_percent == 0 can never accept, so none is taken there (the
+// oracle does the same).  The walk is bounded; status 1 = gave up.
+__global__ void split_kernel(float *centers, int64_t ld, int64_t dim, int64_t *counts, int C,
+                             int64_t batch, uint64_t *rng_state, int *status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  uint64_t s = *rng_state;
+  const float lo = 1.0f - 1.0f / 1024.0f, hi = 1.0f + 1.0f / 1024.0f;
+  for (int i = 0; i < C; ++i) {
+    if (counts[i] != 0) continue;
+    int sc = (i + 1) % C;
+    int64_t guard = 0;
+    for (;;) {
+      double p = (double)counts[sc] / (double)batch;
+      if (p > 0.0 && rng_unit(s) < p) break;
+      sc = (sc + 1) % C;
+      if (++guard > ((int64_t)1 << 26)) {
+        *status = 1;
+        *rng_state = s;
+        return;
+      }
+    }
+    for (int64_t j = 0; j < dim; ++j) {
+      float v = centers[(int64_t)sc * ld + j];
+      if (j % 2 == 0) {
+        centers[(int64_t)i * ld + j] = __fmul_rn(v, lo);
+        centers[(int64_t)sc * ld + j] = __fmul_rn(v, hi);
+      } else {
+        centers[(int64_t)i * ld + j] = __fmul_rn(v, hi);
+        centers[(int64_t)sc * ld + j] = __fmul_rn(v, lo);
+      }
+    }
+    counts[i] = counts[sc] / 2;
+    counts[sc] -= counts[i];
+  }
+  *rng_state = s;
+}
+
+// ---------------------------------------------------------------------------
+// PQ: residual sub-vectors, per-instance k-means, encode
+
+// Z[m][p][t] = x[row_p][b_m + t] - c_list[b_m + t]  (kmeans.rs:37-41 order)
+__global__ void residual_gather_kernel(const float *X, int64_t ld, const float *centers,
+                                       const uint32_t *rows, const uint32_t *row_list,
+                                       int64_t npos, int M, int dmax, const int *sb,
+                                       const int *sl, float *Z) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npos * M) return;
+  int m = (int)(t % M);
+  int64_t p = t / M;
+  int64_t r = rows[p];
+  int64_t c = row_list[p];
+  float *z = Z + ((int64_t)m * npos + p) * dmax;
+  for (int u = 0; u < dmax; ++u)
+    z[u] = u < sl[m] ? __fsub_rn(X[r * ld + sb[m] + u], centers[c * ld + sb[m] + u]) : 0.0f;
+}
+
+template <int DM>
+__device__ __forceinline__ float l2_sub(const float *a, const float *b) {
+  float s = 0.0f;
+#pragma unroll
+  for (int u = 0; u < DM; ++u) {
+    float t = __fsub_rn(a[u], b[u]);
+    s = __fadd_rn(s, __fmul_rn(t, t));
+  }
+  return s;
+}
+
+// One CTA per (list, subspace) instance: Kmeans::train on the list's
+// residual sub-vectors (PQIndex::train_center, pq_idx.rs:125-146).
+template <int DM>
+__global__ void __launch_bounds__(256) pq_kmeans_kernel(
+    const float *Z, int64_t npos, const int64_t *toff, int M, int K, const int *sl, int epochs,
+    uint64_t seed, int accum_f64, uint8_t *asg_g, float *books, uint8_t *trained, int *status) {
+  extern __shared__ __align__(16) float sm[];
+  float *cent = sm;                                  // K x DM
+  int64_t *cnt = reinterpret_cast<int64_t *>(cent + K * DM + (K * DM) % 2);  // K
+  __shared__ float mean[DM];
+  const int c = blockIdx.x / M, m = blockIdx.x % M;
+  const int64_t lo = toff[c], n = toff[c + 1] - lo;
+  const int len = sl[m];
+  float *book = books + ((int64_t)c * M + m) * K * DM;
+  if (n == 0) {
+    for (int i = threadIdx.x; i < K * DM; i += blockDim.x) book[i] = 0.0f;
+    if (threadIdx.x == 0 && m == 0) trained[c] = 0;
+    return;
+  }
+  const float *z = Z + ((int64_t)m * npos + lo) * DM;
+  uint8_t *asg = asg_g + (int64_t)m * npos + lo;
+  // init_center
+  if (threadIdx.x < DM) {
+    int u = threadIdx.x;
+    float mu = 0.0f;
+    if (u < len) {
+      if (accum_f64) {
+        double s = 0.0;
+        for (int64_t i = 0; i < n; ++i) s += (double)z[i * DM + u];
+        mu = (float)(s / (double)n);
+      } else {
+        float s = 0.0f;
+        for (int64_t i = 0; i < n; ++i) s = __fadd_rn(s, z[i * DM + u]);
+        mu = __fdiv_rn(s, (float)n);
+      }
+    }
+    mean[u] = mu;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < K * DM; e += blockDim.x) {
+    int j = e / DM, u = e % DM;
+    bool plus = ((uint64_t)j & ((uint64_t)1 << ((uint64_t)u & 63))) == 1;
+    cent[e] = u < len ? (plus ? __fadd_rn(mean[u], 1.0f) : __fsub_rn(mean[u], 1.0f)) : 0.0f;
+  }
+  __syncthreads();
+  uint64_t rng = instance_seed(seed, 1 + (uint64_t)c * M + m);
+  for (int ep = 0; ep < epochs; ++ep) {
+    // search_data: strict '<' from centre 0
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      float zi[DM];
+#pragma unroll
+      for (int u = 0; u < DM; ++u) zi[u] = z[i * DM + u];
+      int best = 0;
+      float bd = l2_sub<DM>(zi, cent);
+      for (int j = 1; j < K; ++j) {
+        float d = l2_sub<DM>(zi, cent + j * DM);
+        if (d < bd) {
+          bd = d;
+          best = j;
+        }
+      }
+      asg[i] = (uint8_t)best;
+    }
+    __syncthreads();
+    // update_center: per centre, members in item order
+    for (int j = threadIdx.x; j < K; j += blockDim.x) {
+      int64_t cn = 0;
+      float out[DM];
+      if (accum_f64) {
+        double s[DM];
+#pragma unroll
+        for (int u = 0; u < DM; ++u) s[u] = 0.0;
+        for (int64_t i = 0; i < n; ++i)
+          if (asg[i] == j) {
+            ++cn;
+#pragma unroll
+            for (int u = 0; u < DM; ++u) s[u] += (double)z[i * DM + u];
+          }
+#pragma unroll
+        for (int u = 0; u < DM; ++u) out[u] = cn ? (float)(s[u] / (double)cn) : 0.0f;
+      } else {
+        float s[DM];
+#pragma unroll
+        for (int u = 0; u < DM; ++u) s[u] = 0.0f;
+        for (int64_t i = 0; i < n; ++i)
+          if (asg[i] == j) {
+            ++cn;
+#pragma unroll
+            for (int u = 0; u < DM; ++u) s[u] = __fadd_rn(s[u], z[i * DM + u]);
+          }
+#pragma unroll
+        for (int u = 0; u < DM; ++u) out[u] = cn ? __fdiv_rn(s[u], (float)cn) : 0.0f;
+      }
+      cnt[j] = cn;
+      // no thread reads the centres during the update, so write in place
+#pragma unroll
+      for (int u = 0; u < DM; ++u) cent[j * DM + u] = out[u];
+    }
+    __syncthreads();
+    if (ep < epochs - 1 && threadIdx.x == 0) {
+      const float lo_ = 1.0f - 1.0f / 1024.0f, hi_ = 1.0f + 1.0f / 1024.0f;
+      for (int i = 0; i < K; ++i) {
+        if (cnt[i] != 0) continue;
+        int sc = (i + 1) % K;
+        int64_t guard = 0;
+        bool gave_up = false;
+        for (;;) {
+          double p = (double)cnt[sc] / (double)n;
+          if (p > 0.0 && rng_unit(rng) < p) break;
+          sc = (sc + 1) % K;
+          if (++guard > ((int64_t)1 << 24)) {
+            gave_up = true;
+            break;
+          }
+        }
+        if (gave_up) {
+          atomicExch(status, 1);
+          break;
+        }
+        for (int u = 0; u < len; ++u) {
+          float v = cent[sc * DM + u];
+          if (u % 2 == 0) {
+            cent[i * DM + u] = __fmul_rn(v, lo_);
+            cent[sc * DM + u] = __fmul_rn(v, hi_);
+          } else {
+            cent[i * DM + u] = __fmul_rn(v, hi_);
+            cent[sc * DM + u] = __fmul_rn(v, lo_);
+          }
+        }
+        cnt[i] = cnt[sc] / 2;
+        cnt[sc] -= cnt[i];
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < K * DM; e += blockDim.x) book[e] = cent[e];
+  if (threadIdx.x == 0 && m == 0) trained[c] = 1;
+}
+
+// codes of every list member (pq_idx.rs:143-144): strict '<' argmin per subspace
+template <int DM>
+__global__ void __launch_bounds__(256) pq_encode_kernel(
+    const float *X, int64_t ld, const float *centers, const uint32_t *items, const int64_t *offs,
+    const float *books, int M, int K, const int *sb, const int *sl, uint8_t *codes) {
+  extern __shared__ __align__(16) float cb[];  // K x DM
+  const int c = blockIdx.x, m = blockIdx.y;
+  const int64_t lo = offs[c], n = offs[c + 1] - lo;
+  if (n == 0) return;
+  const float *book = books + ((int64_t)c * M + m) * K * DM;
+  for (int e = threadIdx.x; e < K * DM; e += blockDim.x) cb[e] = book[e];
+  __syncthreads();
+  const int b = sb[m], len = sl[m];
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    int64_t r = items[lo + i];
+    float zi[DM];
+#pragma unroll
+    for (int u = 0; u < DM; ++u)
+      zi[u] = u < len ? __fsub_rn(X[r * ld + b + u], centers[(int64_t)c * ld + b + u]) : 0.0f;
+    int best = 0;
+    float bd = l2_sub<DM>(zi, cb);
+    for (int j = 1; j < K; ++j) {
+      float d = l2_sub<DM>(zi, cb + j * DM);
+      if (d < bd) {
+        bd = d;
+        best = j;
+      }
+    }
+    codes[(lo + i) * M + m] = (uint8_t)best;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// search
+
+// Pairs (query, probe slot) grouped by list: histogram / scan / scatter.
+__global__ void pair_hist_kernel(const uint64_t *probes, int64_t nq, int pmax,
+                                 const uint32_t *nprobe_q, int C, int64_t *cnt) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nq * pmax) return;
+  int64_t q = t / pmax;
+  int j = (int)(t % pmax);
+  int p = nprobe_q ? (int)nprobe_q[q] : pmax;
+  uint64_t k = probes[t];
+  if (j >= p || k == kEmptyKey) return;
+  atomicAdd(reinterpret_cast<unsigned long long *>(cnt + key_row(k)), 1ull);
+}
+
+__global__ void pair_scatter_kernel(const uint64_t *probes, int64_t nq, int pmax,
+                                    const uint32_t *nprobe_q, int C, const int64_t *off,
+                                    int64_t *cursor, uint32_t *pq, uint32_t *pc, uint32_t *pslot) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nq * pmax) return;
+  int64_t q = t / pmax;
+  int j = (int)(t % pmax);
+  int p = nprobe_q ? (int)nprobe_q[q] : pmax;
+  uint64_t k = probes[t];
+  if (j >= p || k == kEmptyKey) return;
+  uint32_t c = key_row(k);
+  int64_t pos = off[c] + (int64_t)atomicAdd(reinterpret_cast<unsigned long long *>(cursor + c), 1ull);
+  pq[pos] = (uint32_t)q;
+  pc[pos] = c;
+  pslot[pos] = (uint32_t)j;
+}
+
+// CTA-wide selection of the k smallest of L 32-bit order keys held in smem
+// (radix select on 8-bit digits; ties at the k-th key go to the lowest
+// positions).  sel receives k positions (unordered).  L, k uniform.
+__device__ void cta_select_k(const uint32_t *keys, int L, int k, int *sel, uint32_t *hist,
+                             int *scratch) {
+  // scratch: [0] prefix bits, [1] remaining k, [2] count below, [3] digit, [4..] scan
+  if (threadIdx.x == 0) {
+    scratch[0] = 0;
+    scratch[1] = k;
+  }
+  __syncthreads();
+  uint32_t prefix = 0, mask = 0;
+  for (int shift = 24; shift >= 0; shift -= 8) {
+    for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+      uint32_t v = keys[i];
+      if ((v & mask) == prefix) atomicAdd(&hist[(v >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int rem = scratch[1];
+      uint32_t run = 0;
+      int d = 0;
+      for (; d < 256; ++d) {
+        if (run + hist[d] >= (uint32_t)rem) break;
+        run += hist[d];
+      }
+      scratch[1] = rem - (int)run;
+      scratch[3] = d;
+    }
+    __syncthreads();
+    prefix |= ((uint32_t)scratch[3]) << shift;
+    mask |= 255u << shift;
+    __syncthreads();
+  }
+  const uint32_t kth = prefix;
+  const int need_eq = scratch[1];  // how many keys equal to kth are taken
+  // positions of keys < kth (any order) and the first need_eq keys == kth
+  __shared__ int n_lt, n_eq;
+  if (threadIdx.x == 0) {
+    n_lt = 0;
+    n_eq = 0;
+  }
+  __syncthreads();
+  // keys < kth
+  for (int i = threadIdx.x; i < L; i += blockDim.x)
+    if (keys[i] < kth) sel[atomicAdd(&n_lt, 1)] = i;
+  __syncthreads();
+  const int base_lt = n_lt;
+  // keys == kth in position order: chunked block scan
+  for (int c0 = 0; c0 < L; c0 += blockDim.x) {
+    int i = c0 + threadIdx.x;
+    int f = (i < L && keys[i] == kth) ? 1 : 0;
+    unsigned b = __ballot_sync(0xffffffffu, f);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) scratch[4 + w] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int run = n_eq;
+      for (int x = 0; x < (int)(blockDim.x >> 5); ++x) {
+        int v = scratch[4 + x];
+        scratch[4 + x] = run;
+        run += v;
+      }
+      n_eq = run;
+    }
+    __syncthreads();
+    if (f) {
+      int r = scratch[4 + w] + __popc(b & ((1u << lane) - 1u));
+      if (r < need_eq) sel[base_lt + r] = i;
+    }
+    __syncthreads();
+  }
+}
+
+constexpr int kAdcThreads = 256;
+constexpr int kAdcChunk = 4096;
+
+// One CTA handles `per` consecutive (query, list) pairs (sorted by list).
+template <int DM>
+__global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
+    const float *Q, int64_t ldq, const float *centers, int64_t ldc, const float *books,
+    const uint8_t *codes, const uint32_t *items, const int64_t *offs, const uint8_t *trained,
+    const uint32_t *pq, const uint32_t *pc, const uint32_t *pslot, int64_t npairs, int per, int M,
+    int K, const int *sb, const int *sl, int kk, int pmax, uint64_t *cand) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float *lut = reinterpret_cast<float *>(smraw);                       // M x K
+  uint32_t *dkeys = reinterpret_cast<uint32_t *>(lut + M * K);         // kAdcChunk + kk
+  int *sel = reinterpret_cast<int *>(dkeys + kAdcChunk + 1024);        // kk
+  uint32_t *hist = reinterpret_cast<uint32_t *>(sel + 1024);           // 256
+  int *scratch = reinterpret_cast<int *>(hist + 256);                  // 4 + 32
+  uint32_t *rows = reinterpret_cast<uint32_t *>(scratch + 40);         // kAdcChunk + kk (row ids)
+  __shared__ float zq[1024];
+  for (int64_t pi = (int64_t)blockIdx.x * per; pi < min(npairs, (int64_t)(blockIdx.x + 1) * per); ++pi) {
+    const int64_t q = pq[pi];
+    const int c = (int)pc[pi];
+    const int slot = (int)pslot[pi];
+    uint64_t *out = cand + (q * pmax + slot) * kk;
+    const int64_t lo = offs[c], L = offs[c + 1] - lo;
+    if (!trained[c] || L == 0) {
+      for (int r = threadIdx.x; r < kk; r += blockDim.x) out[r] = kEmptyKey;
+      __syncthreads();
+      continue;
+    }
+    // z = q - c_list over the covered dimensions (pq_idx.rs:158-161)
+    int dcov = sb[M - 1] + sl[M - 1];
+    for (int t = threadIdx.x; t < dcov; t += blockDim.x)
+      zq[t] = __fsub_rn(Q[q * ldq + t], centers[(int64_t)c * ldc + t]);
+    __syncthreads();
+    // LUT[m][j] = sum_t (z_t - C[m][j][t])^2 (pq_idx.rs:170-179)
+    const float *book = books + (int64_t)c * M * K * DM;
+    for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
+      int m = e / K;
+      const float *cj = book + (int64_t)e * DM;
+      const int b = sb[m], len = sl[m];
+      float s = 0.0f;
+#pragma unroll
+      for (int u = 0; u < DM; ++u) {
+        if (u < len) {
+          float t = __fsub_rn(zq[b + u], cj[u]);
+          s = __fadd_rn(s, __fmul_rn(t, t));
+        }
+      }
+      lut[e] = s;
+    }
+    __syncthreads();
+    // scan in chunks; running k best kept at the head of dkeys/rows
+    int held = 0;
+    for (int64_t c0 = 0; c0 < L; c0 += kAdcChunk - kk) {
+      const int ch = (int)((int64_t)(kAdcChunk - kk) < L - c0 ? (int64_t)(kAdcChunk - kk) : L - c0);
+      for (int i = threadIdx.x; i < ch; i += blockDim.x) {
+        const uint8_t *code = codes + (lo + c0 + i) * M;
+        float d = 0.0f;
+        for (int m = 0; m < M; ++m) d = __fadd_rn(d, lut[m * K + code[m]]);
+        dkeys[held + i] = f2ord(d);
+        rows[held + i] = items[lo + c0 + i];
+      }
+      __syncthreads();
+      const int tot = held + ch;
+      if (tot <= kk) {
+        held = tot;
+        __syncthreads();
+        continue;
+      }
+      cta_select_k(dkeys, tot, kk, sel, hist, scratch);
+      __syncthreads();
+      // gather the selection to the head (through registers: sel is unordered)
+      uint32_t kv[4], rv[4];
+      int nmine = 0;
+      for (int r = threadIdx.x; r < kk; r += blockDim.x) {
+        kv[nmine] = dkeys[sel[r]];
+        rv[nmine] = rows[sel[r]];
+        ++nmine;
+      }
+      __syncthreads();
+      nmine = 0;
+      for (int r = threadIdx.x; r < kk; r += blockDim.x) {
+        dkeys[r] = kv[nmine];
+        rows[r] = rv[nmine];
+        ++nmine;
+      }
+      held = kk;
+      __syncthreads();
+    }
+    for (int r = threadIdx.x; r < kk; r += blockDim.x)
+      out[r] = r < held ? (((uint64_t)dkeys[r] << 32) | rows[r]) : kEmptyKey;
+    __syncthreads();
+  }
+}
+
+// Exact FP32 rerank of each query's R best ADC rows with the index metric.
+template <int MT>
+__global__ void rerank_kernel(const float *Q, int64_t ld, const float *X, int64_t dim,
+                              const float *qnorm, const float *xnorm, const uint64_t *in, int R,
+                              uint64_t *outk) {
+  const int64_t q = blockIdx.x;
+  for (int r = threadIdx.x; r < R; r += blockDim.x) {
+    uint64_t key = in[q * R + r];
+    if (key == kEmptyKey) {
+      outk[q * R + r] = kEmptyKey;
+      continue;
+    }
+    uint32_t row = key_row(key);
+    const float *x = X + (int64_t)row * ld;
+    const float *qq = Q + q * ld;
+    float s = 0.0f;
+    for (int64_t t = 0; t < dim; ++t) s = dist_op<MT == M_COS ? M_IP : MT>(s, qq[t], x[t]);
+    if (MT == M_COS) s = cosine_from_dot(s, qnorm[q], xnorm[row]);
+    outk[q * R + r] = make_key(s, row);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+static int sort_labels(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
+                       DevBuf &blk, DevBuf &counts, int64_t *d_offsets, uint32_t *d_members,
+                       cudaStream_t s) {
+  int64_t nb = ceil_div(n, kSortBlock);
+  HORA_TRY(blk.reserve(sizeof(uint32_t) * nb * C));
+  HORA_TRY(counts.reserve(sizeof(int64_t) * C));
+  int smem = C * 4;
+  if (smem > 48 * 1024) {
+    HORA_CUDA_TRY(cudaFuncSetAttribute(label_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    HORA_CUDA_TRY(cudaFuncSetAttribute(label_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  }
+  {
+    ProfScope ps("ivf_sort", s);
+    label_hist_kernel<<<(unsigned)nb, 256, smem, s>>>(keys, labels, n, C, blk.as<uint32_t>());
+    HORA_LAUNCHED();
+    label_block_scan_kernel<<<ceil_div(C, 256), 256, 0, s>>>(blk.as<uint32_t>(), nb, C, counts.as<int64_t>());
+    HORA_LAUNCHED();
+    offsets_scan_kernel<<<1, 1024, 0, s>>>(counts.as<int64_t>(), C, d_offsets);
+    HORA_LAUNCHED();
+    label_scatter_kernel<<<(unsigned)nb, 256, smem, s>>>(keys, labels, n, C, blk.as<uint32_t>(),
+                                                        d_offsets, d_members);
+    HORA_LAUNCHED();
+  }
+  return HORA_OK;
+}
+
+static int pq_dmax_of(int64_t dim, int64_t n_sub) {
+  int64_t sd = dim / n_sub;
+  return (int)(sd + ((dim % sd) ? 1 : 0));
+}
+
+static int dm_bucket(int dmax) { return dmax <= 1 ? 1 : dmax <= 2 ? 2 : dmax <= 4 ? 4 : dmax <= 8 ? 8 : 16; }
+
+template <int DM>
+static int launch_pq_kmeans(IvfState &v, const float *Z, int64_t npos, const int64_t *toff,
+                            int epochs, uint64_t seed, int accum, uint8_t *asg, int *status,
+                            cudaStream_t s) {
+  int smem = (int)(v.K * DM * 4 + 8 + v.K * 8 + 16);
+  HORA_CUDA_TRY(cudaFuncSetAttribute(pq_kmeans_kernel<DM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  ProfScope ps("pq_kmeans", s);
+  pq_kmeans_kernel<DM><<<(unsigned)(v.n_list * v.n_sub), 256, smem, s>>>(
+      Z, npos, toff, (int)v.n_sub, (int)v.K, v.sub_len_d.as<int>(), epochs, seed, accum, asg,
+      v.books.as<float>(), v.trained.as<uint8_t>(), status);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+template <int DM>
+static int launch_pq_encode(IvfState &v, const float *X, int64_t ld, cudaStream_t s) {
+  int smem = (int)(v.K * DM * 4);
+  dim3 grid((unsigned)v.n_list, (unsigned)v.n_sub);
+  ProfScope ps("pq_encode", s);
+  pq_encode_kernel<DM><<<grid, 256, smem, s>>>(X, ld, v.centers.as<float>(), v.items.as<uint32_t>(),
+                                               v.offsets.as<int64_t>(), v.books.as<float>(),
+                                               (int)v.n_sub, (int)v.K, v.sub_begin_d.as<int>(),
+                                               v.sub_len_d.as<int>(), v.codes.as<uint8_t>());
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+static int encode_all(hora_index *h, IvfState &v, cudaStream_t s) {
+  const float *X = h->base.as<float>();
+  switch (dm_bucket((int)v.dmax)) {
+    case 1: return launch_pq_encode<1>(v, X, h->ld, s);
+    case 2: return launch_pq_encode<2>(v, X, h->ld, s);
+    case 4: return launch_pq_encode<4>(v, X, h->ld, s);
+    case 8: return launch_pq_encode<8>(v, X, h->ld, s);
+    default: return launch_pq_encode<16>(v, X, h->ld, s);
+  }
+}
+
+static void init_layout(hora_index *h, IvfState &v) {
+  v.n_list = (int64_t)h->ivf.n_kmeans_center;
+  v.n_sub = (int64_t)h->ivf.n_sub;
+  v.sub_bits = (int64_t)h->ivf.sub_bits;
+  v.K = (int64_t)1 << v.sub_bits;
+  v.dmax = dm_bucket(pq_dmax_of((int64_t)h->dim, v.n_sub));
+  // PQIndex::new subspace ranges (pq_idx.rs:75-88), dimension % sub_dimension as written
+  int64_t sd = (int64_t)h->dim / v.n_sub, r = (int64_t)h->dim % sd;
+  v.sub_begin.resize(v.n_sub);
+  v.sub_len.resize(v.n_sub);
+  for (int64_t i = 0; i < v.n_sub; ++i) {
+    int64_t b, e;
+    if (i < r) {
+      b = i * (sd + 1);
+      e = (i + 1) * (sd + 1);
+    } else {
+      b = r * (sd + 1) + (i - r) * sd;
+      e = r * (sd + 1) + (i + 1 - r) * sd;
+    }
+    v.sub_begin[i] = (int)b;
+    v.sub_len[i] = (int)(e - b);
+  }
+}
+
+static int upload_layout(IvfState &v, cudaStream_t s) {
+  HORA_TRY(v.sub_begin_d.reserve(sizeof(int) * v.n_sub));
+  HORA_TRY(v.sub_len_d.reserve(sizeof(int) * v.n_sub));
+  HORA_CUDA_TRY(cudaMemcpyAsync(v.sub_begin_d.ptr, v.sub_begin.data(), sizeof(int) * v.n_sub,
+                                cudaMemcpyHostToDevice, s));
+  HORA_CUDA_TRY(cudaMemcpyAsync(v.sub_len_d.ptr, v.sub_len.data(), sizeof(int) * v.n_sub,
+                                cudaMemcpyHostToDevice, s));
+  return HORA_OK;
+}
+
+// Assigns every item to its nearest centre (index metric) and builds the
+// inverted lists in item order.
+static int assign_lists(hora_index *h, IvfState &v, DevBuf &keys, DevBuf &blk, DevBuf &cnt,
+                        cudaStream_t s) {
+  const int64_t n = h->n;
+  HORA_TRY(keys.reserve(sizeof(uint64_t) * n));
+  if (h->metric == M_COS) {
+    HORA_TRY(v.cnorm.reserve(sizeof(float) * v.n_list));
+    HORA_TRY(launch_row_norms(v.centers.as<float>(), v.n_list, h->ld, h->dim, v.cnorm.as<float>(), nullptr, s));
+    HORA_TRY(ensure_norms(h, s));
+  }
+  TileParams p;
+  p.Q = h->base.as<float>();
+  p.ldq = h->ld;
+  p.nq = n;
+  p.X = v.centers.as<float>();
+  p.ldx = h->ld;
+  p.r_begin = 0;
+  p.r_end = v.n_list;
+  p.ld = h->ld;
+  p.qnorm = h->xnorm.as<float>();
+  p.xnorm = v.cnorm.as<float>();
+  p.out_key = keys.as<uint64_t>();
+  HORA_TRY(launch_dist_tile(h->metric, TILE_ARGMIN, p, s));
+  HORA_TRY(v.offsets.reserve(sizeof(int64_t) * (v.n_list + 1)));
+  HORA_TRY(v.items.reserve(sizeof(uint32_t) * std::max<int64_t>(n, 1)));
+  HORA_TRY(sort_labels(keys.as<uint64_t>(), nullptr, n, (int)v.n_list, blk, cnt,
+                       v.offsets.as<int64_t>(), v.items.as<uint32_t>(), s));
+  return HORA_OK;
+}
+
+static int fetch_offsets(IvfState &v, cudaStream_t s) {
+  v.h_offsets.resize(v.n_list + 1);
+  HORA_CUDA_TRY(cudaMemcpyAsync(v.h_offsets.data(), v.offsets.ptr, sizeof(int64_t) * (v.n_list + 1),
+                                cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  v.max_list = 0;
+  for (int64_t c = 0; c < v.n_list; ++c) v.max_list = std::max(v.max_list, v.h_offsets[c + 1] - v.h_offsets[c]);
+  return HORA_OK;
+}
+
+int ivf_build(hora_index *h) {
+  cudaStream_t s = h->stream;
+  if (h->n == 0) return fail(HORA_EINVAL, "None to assigned impossible split center");
+  std::unique_ptr<IvfState, IvfDeleter> vp(new IvfState());
+  IvfState &v = *vp;
+  init_layout(h, v);
+  if (v.n_list > h->n) {
+    // more centres than items is legal in the reference; lists simply stay empty
+  }
+  HORA_TRY(upload_layout(v, s));
+  const int64_t n = h->n;
+  const int64_t T = (h->train_size > 0 && (int64_t)h->train_size < n) ? (int64_t)h->train_size : n;
+  const int C = (int)v.n_list;
+  const int epochs = (int)h->ivf.train_epoch;
+  const float *X = h->base.as<float>();
+  HORA_TRY(v.centers.reserve(sizeof(float) * C * h->ld));
+  HORA_CUDA_TRY(cudaMemsetAsync(v.centers.ptr, 0, sizeof(float) * C * h->ld, s));
+  DevBuf keys, blk, cnt, members, moff, state;
+  HORA_TRY(state.reserve(64));
+  HORA_CUDA_TRY(cudaMemsetAsync(state.ptr, 0, 64, s));
+  uint64_t seed0 = instance_seed(h->seed, 0);
+  HORA_CUDA_TRY(cudaMemcpyAsync(state.ptr, &seed0, 8, cudaMemcpyHostToDevice, s));
+  uint64_t *d_rng = state.as<uint64_t>();
+  int *d_status = reinterpret_cast<int *>(state.as<char>() + 8);
+
+  // ---- coarse k-means on the first T items ----
+  {
+    ProfScope ps("coarse_init", s);
+    coarse_init_kernel<<<ceil_div(h->dim, 128), 128, 0, s>>>(X, h->ld, T, h->dim, C, h->accum_f64,
+                                                             v.centers.as<float>());
+    HORA_LAUNCHED();
+  }
+  HORA_TRY(keys.reserve(sizeof(uint64_t) * T));
+  HORA_TRY(members.reserve(sizeof(uint32_t) * T));
+  HORA_TRY(moff.reserve(sizeof(int64_t) * (C + 1)));
+  if (h->metric == M_COS) {
+    HORA_TRY(ensure_norms(h, s));
+    HORA_TRY(v.cnorm.reserve(sizeof(float) * C));
+  }
+  for (int ep = 0; ep < epochs; ++ep) {
+    if (h->metric == M_COS)
+      HORA_TRY(launch_row_norms(v.centers.as<float>(), C, h->ld, h->dim, v.cnorm.as<float>(), nullptr, s));
+    TileParams p;
+    p.Q = X;
+    p.ldq = h->ld;
+    p.nq = T;
+    p.X = v.centers.as<float>();
+    p.ldx = h->ld;
+    p.r_begin = 0;
+    p.r_end = C;
+    p.ld = h->ld;
+    p.qnorm = h->xnorm.as<float>();
+    p.xnorm = v.cnorm.as<float>();
+    p.out_key = keys.as<uint64_t>();
+    HORA_TRY(launch_dist_tile(h->metric, TILE_ARGMIN, p, s));
+    HORA_TRY(sort_labels(keys.as<uint64_t>(), nullptr, T, C, blk, cnt, moff.as<int64_t>(),
+                         members.as<uint32_t>(), s));
+    {
+      ProfScope ps("coarse_update", s);
+      center_sum_kernel<<<ceil_div((int64_t)C * h->dim, 256), 256, 0, s>>>(
+          X, h->ld, members.as<uint32_t>(), moff.as<int64_t>(), C, h->dim, h->accum_f64,
+          v.centers.as<float>());
+      HORA_LAUNCHED();
+    }
+    if (ep < epochs - 1) {
+      ProfScope ps("coarse_split", s);
+      split_kernel<<<1, 1, 0, s>>>(v.centers.as<float>(), h->ld, h->dim, cnt.as<int64_t>(), C, T,
+                                   d_rng, d_status);
+      HORA_LAUNCHED();
+    }
+  }
+  // ---- inverted lists over every item ----
+  HORA_TRY(assign_lists(h, v, keys, blk, cnt, s));
+  HORA_TRY(fetch_offsets(v, s));
+  v.n_items = n;
+
+  // ---- training rows per list: members among the first T items (all
+  //      members when a list has none of them) ----
+  std::vector<uint32_t> h_items(n);
+  HORA_CUDA_TRY(cudaMemcpyAsync(h_items.data(), v.items.ptr, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  std::vector<int64_t> toff(C + 1, 0);
+  std::vector<uint32_t> trows, tlist;
+  trows.reserve(T);
+  tlist.reserve(T);
+  for (int c = 0; c < C; ++c) {
+    int64_t lo = v.h_offsets[c], hi = v.h_offsets[c + 1];
+    int64_t nt = 0;
+    for (int64_t p = lo; p < hi; ++p) nt += h_items[p] < (uint64_t)T;
+    for (int64_t p = lo; p < hi; ++p)
+      if (nt == 0 || h_items[p] < (uint64_t)T) {
+        trows.push_back(h_items[p]);
+        tlist.push_back((uint32_t)c);
+      }
+    toff[c + 1] = (int64_t)trows.size();
+  }
+  const int64_t npos = (int64_t)trows.size();
+  DevBuf d_toff, d_trows, d_tlist, Z, asg;
+  HORA_TRY(d_toff.reserve(sizeof(int64_t) * (C + 1)));
+  HORA_TRY(d_trows.reserve(sizeof(uint32_t) * std::max<int64_t>(npos, 1)));
+  HORA_TRY(d_tlist.reserve(sizeof(uint32_t) * std::max<int64_t>(npos, 1)));
+  HORA_TRY(Z.reserve(sizeof(float) * std::max<int64_t>(npos, 1) * v.n_sub * v.dmax));
+  HORA_TRY(asg.reserve(std::max<int64_t>(npos, 1) * v.n_sub));
+  HORA_CUDA_TRY(cudaMemcpyAsync(d_toff.ptr, toff.data(), sizeof(int64_t) * (C + 1), cudaMemcpyHostToDevice, s));
+  if (npos) {
+    HORA_CUDA_TRY(cudaMemcpyAsync(d_trows.ptr, trows.data(), sizeof(uint32_t) * npos, cudaMemcpyHostToDevice, s));
+    HORA_CUDA_TRY(cudaMemcpyAsync(d_tlist.ptr, tlist.data(), sizeof(uint32_t) * npos, cudaMemcpyHostToDevice, s));
+    ProfScope ps("pq_residuals", s);
+    residual_gather_kernel<<<ceil_div(npos * v.n_sub, 256), 256, 0, s>>>(
+        X, h->ld, v.centers.as<float>(), d_trows.as<uint32_t>(), d_tlist.as<uint32_t>(), npos,
+        (int)v.n_sub, (int)v.dmax, v.sub_begin_d.as<int>(), v.sub_len_d.as<int>(), Z.as<float>());
+    HORA_LAUNCHED();
+  }
+  HORA_TRY(v.books.reserve(sizeof(float) * C * v.n_sub * v.K * v.dmax));
+  HORA_TRY(v.trained.reserve(C));
+  HORA_CUDA_TRY(cudaMemsetAsync(v.trained.ptr, 0, C, s));
+  switch (v.dmax) {
+    case 1: HORA_TRY(launch_pq_kmeans<1>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
+    case 2: HORA_TRY(launch_pq_kmeans<2>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
+    case 4: HORA_TRY(launch_pq_kmeans<4>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
+    case 8: HORA_TRY(launch_pq_kmeans<8>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
+    default: HORA_TRY(launch_pq_kmeans<16>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
+  }
+  // ---- codes of every member ----
+  HORA_TRY(v.codes.reserve(std::max<int64_t>(n, 1) * v.n_sub));
+  HORA_TRY(encode_all(h, v, s));
+  int status = 0;
+  HORA_CUDA_TRY(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  v.h_trained.resize(C);
+  HORA_CUDA_TRY(cudaMemcpyAsync(v.h_trained.data(), v.trained.ptr, C, cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (status) return fail(HORA_ETIMEDOUT, "k-means split walk did not terminate");
+  if (h->metric == M_COS) {
+    HORA_TRY(v.cnorm.reserve(sizeof(float) * C));
+    HORA_TRY(launch_row_norms(v.centers.as<float>(), C, h->ld, h->dim, v.cnorm.as<float>(), nullptr, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  h->ivfs = std::move(vp);
+  return HORA_OK;
+}
+
+int ivf_set_codebooks(hora_index *h, const float *centers, const float *codebooks) {
+  cudaStream_t s = h->stream;
+  if (h->n == 0) return fail(HORA_EINVAL, "no items");
+  if (h->metric == M_UNKNOWN) return fail(HORA_EMETRIC, "unknown method: build first or set a metric");
+  std::unique_ptr<IvfState, IvfDeleter> vp(new IvfState());
+  IvfState &v = *vp;
+  init_layout(h, v);
+  HORA_TRY(upload_layout(v, s));
+  const int C = (int)v.n_list;
+  HORA_TRY(v.centers.reserve(sizeof(float) * C * h->ld));
+  HORA_CUDA_TRY(cudaMemsetAsync(v.centers.ptr, 0, sizeof(float) * C * h->ld, s));
+  HORA_CUDA_TRY(cudaMemcpy2DAsync(v.centers.ptr, h->ld * 4, centers, h->dim * 4, h->dim * 4, C,
+                                  cudaMemcpyDefault, s));
+  // host codebooks are [C][M][K][dmax_exact]; device keeps dmax bucket
+  const int dexact = pq_dmax_of((int64_t)h->dim, v.n_sub);
+  HORA_TRY(v.books.reserve(sizeof(float) * C * v.n_sub * v.K * v.dmax));
+  HORA_CUDA_TRY(cudaMemsetAsync(v.books.ptr, 0, sizeof(float) * C * v.n_sub * v.K * v.dmax, s));
+  HORA_CUDA_TRY(cudaMemcpy2DAsync(v.books.ptr, v.dmax * 4, codebooks, dexact * 4, dexact * 4,
+                                  (size_t)C * v.n_sub * v.K, cudaMemcpyDefault, s));
+  DevBuf keys, blk, cnt;
+  HORA_TRY(assign_lists(h, v, keys, blk, cnt, s));
+  HORA_TRY(fetch_offsets(v, s));
+  v.n_items = h->n;
+  HORA_TRY(v.trained.reserve(C));
+  v.h_trained.assign(C, 0);
+  for (int c = 0; c < C; ++c) v.h_trained[c] = v.h_offsets[c + 1] > v.h_offsets[c];
+  HORA_CUDA_TRY(cudaMemcpyAsync(v.trained.ptr, v.h_trained.data(), C, cudaMemcpyHostToDevice, s));
+  HORA_TRY(v.codes.reserve(std::max<int64_t>(h->n, 1) * v.n_sub));
+  HORA_TRY(encode_all(h, v, s));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  h->ivfs = std::move(vp);
+  h->built = true;
+  return HORA_OK;
+}
+
+template <int DM>
+static int launch_adc(IvfState &v, const float *Q, int64_t ldq, int64_t ldc, int64_t npairs,
+                      int per, int kk, int pmax, uint64_t *cand, cudaStream_t s) {
+  size_t smem = sizeof(float) * v.n_sub * v.K + sizeof(uint32_t) * (kAdcChunk + 1024) +
+                sizeof(int) * 1024 + 256 * 4 + 40 * 4 + sizeof(uint32_t) * (kAdcChunk + 1024);
+  if (smem > 200 * 1024) return fail(HORA_ECAP, "IVF-PQ: LUT too large for shared memory");
+  HORA_CUDA_TRY(cudaFuncSetAttribute(adc_scan_kernel<DM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  unsigned grid = (unsigned)ceil_div(npairs, per);
+  if (grid == 0) return HORA_OK;
+  ProfScope ps("adc_scan", s);
+  adc_scan_kernel<DM><<<grid, kAdcThreads, smem, s>>>(
+      Q, ldq, v.centers.as<float>(), ldc, v.books.as<float>(), v.codes.as<uint8_t>(),
+      v.items.as<uint32_t>(), v.offsets.as<int64_t>(), v.trained.as<uint8_t>(), v.pair_q.as<uint32_t>(),
+      v.pair_c.as<uint32_t>(), v.pair_slot.as<uint32_t>(), npairs, per, (int)v.n_sub, (int)v.K,
+      v.sub_begin_d.as<int>(), v.sub_len_d.as<int>(), kk, pmax, cand);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+int ivf_search_keys(hora_index *h, int64_t nq, int k, int64_t nprobe, const uint32_t *d_nprobe,
+                    SearchWorkspace &ws, uint64_t *d_best, cudaStream_t s) {
+  if (!h->ivfs) return fail(HORA_ENOTBUILT, "index not built");
+  IvfState &v = *h->ivfs;
+  const int C = (int)v.n_list;
+  int64_t pmax = nprobe > 0 ? nprobe : (int64_t)h->ivf.search_n_center;
+  if (pmax > C) pmax = C;  // the reference pops an empty heap (panics) here
+  if (pmax < 1) pmax = 1;
+  const int R = h->ivf_rerank > k ? h->ivf_rerank : k;  // ADC candidates kept per query
+  if (R > 1024) return fail(HORA_ECAP, "IVF-PQ: k (or rerank width) must be <= 1024");
+  const float *Q = ws.q.as<float>();
+  // 1) coarse distances and probes (pq_idx.rs:416-425)
+  HORA_TRY(v.coarse.reserve(sizeof(float) * nq * C));
+  TileParams p;
+  p.Q = Q;
+  p.ldq = h->ld;
+  p.nq = nq;
+  p.X = v.centers.as<float>();
+  p.ldx = h->ld;
+  p.r_begin = 0;
+  p.r_end = C;
+  p.ld = h->ld;
+  p.qnorm = ws.qnorm.as<float>();
+  p.xnorm = v.cnorm.as<float>();
+  p.out_dist = v.coarse.as<float>();
+  p.ldo = C;
+  HORA_TRY(launch_dist_tile(h->metric, TILE_DIST, p, s));
+  HORA_TRY(v.probes.reserve(sizeof(uint64_t) * nq * pmax));
+  HORA_TRY(launch_rows_topk(v.coarse.as<float>(), nq, C, C, (int)pmax, v.probes.as<uint64_t>(), s));
+  // 2) (query, list) pairs grouped by list
+  HORA_TRY(v.pair_cnt.reserve(sizeof(int64_t) * (C + 1) * 2));
+  HORA_TRY(v.pair_off.reserve(sizeof(int64_t) * (C + 1)));
+  int64_t *cnt = v.pair_cnt.as<int64_t>();
+  int64_t *cursor = cnt + (C + 1);
+  HORA_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (C + 1) * 2, s));
+  int64_t tot = nq * pmax;
+  {
+    ProfScope ps("ivf_pairs", s);
+    pair_hist_kernel<<<ceil_div(tot, 256), 256, 0, s>>>(v.probes.as<uint64_t>(), nq, (int)pmax,
+                                                       d_nprobe, C, cnt);
+    HORA_LAUNCHED();
+    offsets_scan_kernel<<<1, 1024, 0, s>>>(cnt, C, v.pair_off.as<int64_t>());
+    HORA_LAUNCHED();
+  }
+  int64_t npairs = tot;
+  if (d_nprobe) {
+    HORA_CUDA_TRY(cudaMemcpyAsync(&npairs, v.pair_off.as<int64_t>() + C, sizeof(int64_t),
+                                  cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  HORA_TRY(v.pair_q.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
+  HORA_TRY(v.pair_c.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
+  HORA_TRY(v.pair_slot.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
+  {
+    ProfScope ps("ivf_pairs", s);
+    pair_scatter_kernel<<<ceil_div(tot, 256), 256, 0, s>>>(
+        v.probes.as<uint64_t>(), nq, (int)pmax, d_nprobe, C, v.pair_off.as<int64_t>(), cursor,
+        v.pair_q.as<uint32_t>(), v.pair_c.as<uint32_t>(), v.pair_slot.as<uint32_t>());
+    HORA_LAUNCHED();
+  }
+  // 3) LUT + ADC scan + per-pair R best
+  HORA_TRY(v.cand.reserve(sizeof(uint64_t) * nq * pmax * R));
+  HORA_CUDA_TRY(cudaMemsetAsync(v.cand.ptr, 0xff, sizeof(uint64_t) * nq * pmax * R, s));
+  const int per = 4;
+  switch (v.dmax) {
+    case 1: HORA_TRY(launch_adc<1>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
+    case 2: HORA_TRY(launch_adc<2>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
+    case 4: HORA_TRY(launch_adc<4>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
+    case 8: HORA_TRY(launch_adc<8>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
+    default: HORA_TRY(launch_adc<16>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
+  }
+  // 4) per-query merge of the pmax x R candidates (pq_idx.rs:429-436)
+  const int width = (int)(pmax * R);
+  uint64_t *merged = d_best;
+  if (R > k) {
+    HORA_TRY(v.best_r.reserve(sizeof(uint64_t) * nq * R));
+    merged = v.best_r.as<uint64_t>();
+  }
+  HORA_CUDA_TRY(cudaMemsetAsync(merged, 0xff, sizeof(uint64_t) * nq * R, s));
+  HORA_TRY(ws.ovf_flag.reserve(nq));
+  HORA_TRY(ws.ovf_counter.reserve(4));
+  if (merge_smem_bytes(R, width) <= 200 * 1024) {
+    HORA_TRY(launch_merge_topk(merged, R, v.cand.as<uint64_t>(), nullptr, width, width, nullptr, nq,
+                               ws.ovf_flag.as<uint8_t>(), ws.ovf_counter.as<uint32_t>(), s));
+  } else {
+    // merge probe slots in groups that fit one shared-memory sort
+    int grp = std::max(1, (16384 - R) / R);
+    for (int64_t j0 = 0; j0 < pmax; j0 += grp) {
+      int gw = (int)(std::min<int64_t>(grp, pmax - j0) * R);
+      // candidates of slots [j0, j0+g) are contiguous per query at offset j0*R
+      HORA_TRY(v.tmp_keys.reserve(sizeof(uint64_t) * nq * gw));
+      HORA_CUDA_TRY(cudaMemcpy2DAsync(v.tmp_keys.ptr, gw * 8, v.cand.as<uint64_t>() + j0 * R, width * 8,
+                                      gw * 8, nq, cudaMemcpyDeviceToDevice, s));
+      HORA_TRY(launch_merge_topk(merged, R, v.tmp_keys.as<uint64_t>(), nullptr, gw, gw, nullptr, nq,
+                                 ws.ovf_flag.as<uint8_t>(), ws.ovf_counter.as<uint32_t>(), s));
+    }
+  }
+  // 5) optional exact rerank
+  if (R > k) {
+    HORA_TRY(v.tmp_keys.reserve(sizeof(uint64_t) * nq * R));
+    if (h->metric == M_COS) HORA_TRY(ensure_norms(h, s));
+    {
+      ProfScope ps("ivf_rerank", s);
+      switch (h->metric) {
+        case M_L2: rerank_kernel<M_L2><<<(unsigned)nq, 128, 0, s>>>(Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(), h->xnorm.as<float>(), merged, R, v.tmp_keys.as<uint64_t>()); break;
+        case M_L1: rerank_kernel<M_L1><<<(unsigned)nq, 128, 0, s>>>(Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(), h->xnorm.as<float>(), merged, R, v.tmp_keys.as<uint64_t>()); break;
+        case M_IP: rerank_kernel<M_IP><<<(unsigned)nq, 128, 0, s>>>(Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(), h->xnorm.as<float>(), merged, R, v.tmp_keys.as<uint64_t>()); break;
+        default: rerank_kernel<M_COS><<<(unsigned)nq, 128, 0, s>>>(Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(), h->xnorm.as<float>(), merged, R, v.tmp_keys.as<uint64_t>()); break;
+      }
+      HORA_LAUNCHED();
+    }
+    HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
+    HORA_TRY(launch_merge_topk(d_best, k, v.tmp_keys.as<uint64_t>(), nullptr, R, R, nullptr, nq,
+                               ws.ovf_flag.as<uint8_t>(), ws.ovf_counter.as<uint32_t>(), s));
+  }
+  return HORA_OK;
+}
+
+int ivf_layout(const hora_index *h, uint64_t *n_list, uint64_t *n_sub, uint64_t *sub_bits,
+               uint64_t *dmax) {
+  if (h->kind != HORA_INDEX_IVFPQ) return fail(HORA_EINVAL, "not an IVF-PQ index");
+  int64_t sd = (int64_t)h->dim / (int64_t)h->ivf.n_sub;
+  if (n_list) *n_list = h->ivf.n_kmeans_center;
+  if (n_sub) *n_sub = h->ivf.n_sub;
+  if (sub_bits) *sub_bits = h->ivf.sub_bits;
+  if (dmax) *dmax = (uint64_t)(sd + (((int64_t)h->dim % sd) ? 1 : 0));
+  return HORA_OK;
+}
+
+int ivf_export(const hora_index *h, float *centers, int64_t *offsets, int64_t *items,
+               float *codebooks, uint8_t *codes, uint8_t *trained) {
+  if (h->kind != HORA_INDEX_IVFPQ) return fail(HORA_EINVAL, "not an IVF-PQ index");
+  if (!h->ivfs) return fail(HORA_ENOTBUILT, "index not built");
+  const IvfState &v = *h->ivfs;
+  const int64_t C = v.n_list, n = v.n_items;
+  const int dexact = pq_dmax_of((int64_t)h->dim, v.n_sub);
+  if (centers)
+    HORA_CUDA_TRY(cudaMemcpy2D(centers, h->dim * 4, v.centers.ptr, h->ld * 4, h->dim * 4, C, cudaMemcpyDeviceToHost));
+  if (offsets) std::copy(v.h_offsets.begin(), v.h_offsets.end(), offsets);
+  if (items && n) {
+    std::vector<uint32_t> t(n);
+    HORA_CUDA_TRY(cudaMemcpy(t.data(), v.items.ptr, 4 * n, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < n; ++i) items[i] = t[i];
+  }
+  if (codebooks)
+    HORA_CUDA_TRY(cudaMemcpy2D(codebooks, dexact * 4, v.books.ptr, v.dmax * 4, dexact * 4,
+                               (size_t)C * v.n_sub * v.K, cudaMemcpyDeviceToHost));
+  if (codes && n) HORA_CUDA_TRY(cudaMemcpy(codes, v.codes.ptr, n * v.n_sub, cudaMemcpyDeviceToHost));
+  if (trained) std::copy(v.h_trained.begin(), v.h_trained.end(), trained);
+  return HORA_OK;
+}
+
+// IVF-PQ block of the index file: layout sizes then the trained arrays.
+int ivf_dump(const hora_index *h, FILE *f) {
+  if (!h->ivfs) return HORA_OK;
+  const IvfState &v = *h->ivfs;
+  const int64_t C = v.n_list, n = v.n_items;
+  const int dexact = pq_dmax_of((int64_t)h->dim, v.n_sub);
+  std::vector<float> centers(C * h->dim), books(C * v.n_sub * v.K * dexact);
+  std::vector<int64_t> offs(C + 1), items(n);
+  std::vector<uint8_t> codes(n * v.n_sub), tr(C);
+  HORA_TRY(ivf_export(h, centers.data(), offs.data(), items.data(), books.data(), codes.data(), tr.data()));
+  int64_t hdr[3] = {C, n, v.n_sub};
+  bool ok = std::fwrite(hdr, sizeof(hdr), 1, f) == 1 &&
+            std::fwrite(centers.data(), 4, centers.size(), f) == centers.size() &&
+            std::fwrite(books.data(), 4, books.size(), f) == books.size() &&
+            std::fwrite(tr.data(), 1, tr.size(), f) == tr.size();
+  return ok ? HORA_OK : fail(HORA_EIO, "write failed");
+}
+
+int ivf_load(hora_index *h, FILE *f) {
+  int64_t hdr[3];
+  if (std::fread(hdr, sizeof(hdr), 1, f) != 1) return fail(HORA_EIO, "corrupt index file");
+  const int64_t C = hdr[0];
+  if (C != (int64_t)h->ivf.n_kmeans_center || hdr[1] != h->n || hdr[2] != (int64_t)h->ivf.n_sub)
+    return fail(HORA_EIO, "corrupt index file (IVF-PQ header)");
+  const int dexact = pq_dmax_of((int64_t)h->dim, (int64_t)h->ivf.n_sub);
+  const int64_t K = (int64_t)1 << h->ivf.sub_bits;
+  std::vector<float> centers(C * h->dim), books(C * h->ivf.n_sub * K * dexact);
+  std::vector<uint8_t> tr(C);
+  bool ok = std::fread(centers.data(), 4, centers.size(), f) == centers.size() &&
+            std::fread(books.data(), 4, books.size(), f) == books.size() &&
+            std::fread(tr.data(), 1, tr.size(), f) == tr.size();
+  if (!ok) return fail(HORA_EIO, "corrupt index file (IVF-PQ arrays)");
+  HORA_TRY(ivf_set_codebooks(h, centers.data(), books.data()));
+  // lists that were untrained stay untrained
+  IvfState &v = *h->ivfs;
+  for (int64_t c = 0; c < C; ++c) v.h_trained[c] = v.h_trained[c] && tr[c];
+  HORA_CUDA_TRY(cudaMemcpy(v.trained.ptr, v.h_trained.data(), C, cudaMemcpyHostToDevice));
+  return HORA_OK;
+}
+
+size_t ivf_device_bytes(const hora_index *h) {
+  if (!h->ivfs) return 0;
+  const IvfState &v = *h->ivfs;
+  return v.centers.bytes + v.offsets.bytes + v.items.bytes + v.codes.bytes + v.books.bytes +
+         v.trained.bytes + v.cnorm.bytes;
+}
+
+int ivf_info(const hora_index *h, std::string &out) {
+  if (!h->ivfs) {
+    out = "{\"trained\":false}";
+    return HORA_OK;
+  }
+  const IvfState &v = *h->ivfs;
+  int64_t empty = 0;
+  for (int64_t c = 0; c < v.n_list; ++c) empty += v.h_offsets[c + 1] == v.h_offsets[c];
+  out = "{\"n_list\":" + std::to_string(v.n_list) + ",\"n_sub\":" + std::to_string(v.n_sub) +
+        ",\"sub_bits\":" + std::to_string(v.sub_bits) + ",\"max_list\":" + std::to_string(v.max_list) +
+        ",\"empty_lists\":" + std::to_string(empty) + ",\"search_n_center\":" +
+        std::to_string(h->ivf.search_n_center) + ",\"rerank\":" + std::to_string(h->ivf_rerank) + "}";
+  return HORA_OK;
+}
+
+}  // namespace hora
