@@ -215,6 +215,23 @@ int hora_server_wait(hora_server *s, uint64_t ticket, int64_t timeout_ms, double
  * p99 ms, max in-flight requests, max admitted bytes, rejected]. */
 int hora_server_stats(hora_server *s, double *out7);
 
+/* ---- brute force without device allocation ------------------------------- */
+/* No counterpart in the reference.  Exact brute-force k-NN for callers that
+ * cannot call cudaMalloc (a host engine that owns all device memory through
+ * its own pool and budget, or a latency-critical path where cudaMalloc /
+ * cudaFree would synchronise the device).  base (n x dim), queries (nq x dim),
+ * ids_out and dist_out (nq x k, row numbers and distances as hora_search
+ * returns them) are all device memory; dim must be a multiple of 4 and the
+ * rows 16-byte aligned.  Scratch comes from one fixed 2.1 MiB device array
+ * that every GPU loading the library holds until the process exits: at most
+ * 256 queries and k <= 64 per call (HORA_ECAP beyond), metrics Euclidean,
+ * Manhattan and DotProduct.  Calls share that array: calls that overlap on
+ * the GPU race.  The first call on each device resolves the array's device
+ * address; make it before any stream capture.  stream may be NULL. */
+int hora_bf_search_noalloc(const float *base, uint64_t n, uint64_t dim, const float *queries,
+                           uint64_t nq, uint64_t k, int metric, uint64_t *ids_out,
+                           float *dist_out, void *stream);
+
 /* ---- diagnostics -------------------------------------------------------- */
 const char *hora_last_error(void);
 const char *hora_version(void);
