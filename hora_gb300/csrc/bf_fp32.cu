@@ -185,4 +185,54 @@ int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint
   return HORA_OK;
 }
 
+// Exact FP32 rerank: one thread per candidate walks the dimensions in order
+// (bit-identical to the scan kernel and the reference's scalar loops).
+template <int MT>
+__global__ void rerank_exact_kernel(const float *Q, int64_t ld, const float *X, int64_t dim,
+                                    const float *qnorm, const float *xnorm, const uint64_t *in,
+                                    int R, uint64_t *outk) {
+  const int64_t q = blockIdx.x;
+  const float *qq = Q + q * ld;
+  for (int r = threadIdx.x; r < R; r += blockDim.x) {
+    uint64_t key = in[q * R + r];
+    if (key == kEmptyKey) {
+      outk[q * R + r] = kEmptyKey;
+      continue;
+    }
+    uint32_t row = key_row(key);
+    const float4 *x4 = reinterpret_cast<const float4 *>(X + (int64_t)row * ld);
+    const float4 *q4 = reinterpret_cast<const float4 *>(qq);
+    float s = 0.0f;
+    const int64_t n4 = (dim + 3) / 4;
+    for (int64_t t = 0; t < n4; ++t) {
+      float4 a = q4[t], b = x4[t];
+      constexpr int OP = MT == M_COS ? M_IP : MT;
+      s = dist_op<OP>(s, a.x, b.x);
+      s = dist_op<OP>(s, a.y, b.y);
+      s = dist_op<OP>(s, a.z, b.z);
+      s = dist_op<OP>(s, a.w, b.w);
+    }
+    if (MT == M_COS) s = cosine_from_dot(s, qnorm[q], xnorm[row]);
+    outk[q * R + r] = make_key(s, row);
+  }
+}
+
+int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, int64_t dim,
+                        const float *qnorm, const float *xnorm, const uint64_t *in, int64_t nq,
+                        int R, uint64_t *out, cudaStream_t s) {
+  if (nq <= 0) return HORA_OK;
+  if (ld % 4) return fail(HORA_EINVAL, "rerank: pitch not a multiple of 4");
+  ProfScope ps("rerank_exact", s);
+  unsigned g = (unsigned)nq;
+  switch (metric) {
+    case M_L2: rerank_exact_kernel<M_L2><<<g, 128, 0, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
+    case M_L1: rerank_exact_kernel<M_L1><<<g, 128, 0, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
+    case M_IP: rerank_exact_kernel<M_IP><<<g, 128, 0, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
+    case M_COS: rerank_exact_kernel<M_COS><<<g, 128, 0, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
+    default: return fail(HORA_EMETRIC, "unknown method");
+  }
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
 }  // namespace hora

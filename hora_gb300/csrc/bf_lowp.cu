@@ -1,7 +1,535 @@
-// bf_lowp.cu — placeholder for the low-precision scoring path.
+// bf_lowp.cu — brute-force scoring on the 5th-generation tensor cores
+// (tcgen05.mma, TMA, TMEM) in BF16 or FP8 e4m3 with FP32 accumulation,
+// followed by an exact FP32 rerank of a widened candidate list.
+//
+// Scoring (not in the reference; it replaces the per-row metric calls of
+// BruteForceIndex::node_search_k, src/index/bruteforce_idx.rs:49-61, for the
+// approximate first pass):
+//   Euclidean         d~ = |q|^2 + |x|^2 - 2 <q~, x~>   (norms exact, from FP64)
+//   DotProduct        d~ = <q~, x~>
+//   CosineSimilarity  d~ = -<q~, x~> / (|q| |x|)
+// with q~, x~ the BF16 (or scaled e4m3) copies.  Each query keeps its R best
+// approximate keys through the same chunked candidate scan as the exact path;
+// the R rows are then rescored exactly in FP32 in the reference's op order
+// and the k best returned, so every returned distance is exact.  Manhattan
+// has no tensor-core form and always runs exactly on the CUDA cores.
+//
+// Kernel layout: CTA = 10 warps.  Warp 0 issues TMA loads (query tile once,
+// then a ring of base-row tiles), warp 1 owns TMEM (2 x 256 accumulator
+// columns) and issues tcgen05.mma for each 128 x 256 tile, warps 2-9 drain the
+// accumulators with tcgen05.ld (one query row per TMEM lane, half of the 256
+// columns per warp), form distances and append candidates that beat the
+// query's current R-th key.  Every mbarrier wait is bounded; a CTA that gives
+// up raises an error flag read by the host, waits for its MMAs and frees TMEM.
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "dist_tile.cuh"
 #include "index.h"
+#include "tc_ptx.cuh"
+
 namespace hora {
-struct LowpState {};
+
+constexpr int kLpBM = 128;           // queries per CTA (TMEM lanes)
+constexpr int kLpBN = 256;           // base rows per tile (accumulator columns)
+constexpr int kLpThreads = 320;      // 10 warps
+constexpr int kLpEpiThreads = 256;   // warps 2..9
+constexpr int kLpTilesPerCta = 8;
+
+struct LowpState {
+  int prec = 0;
+  int64_t n = 0, Dp = 0;
+  DevBuf base;    // n x Dp (bf16 or e4m3)
+  DevBuf xsq;     // n f32 exact squared norms
+  DevBuf xscale;  // n f32 (e4m3 per-row scale)
+  CUtensorMap tmap_b;
+  DevBuf q, qsq, qscale, qgather, err;
+};
+
 void lowp_state_free(LowpState *p) { delete p; }
-int lowp_search_keys(hora_index *, int64_t, int, SearchWorkspace &, uint64_t *, cudaStream_t) { return fail(HORA_ENOTIMPL, "low precision: not built yet"); }
+
+struct LpParams {
+  int64_t nq;
+  const int *qmap;
+  int64_t r_begin, r_end;
+  int nkb;        // 128-byte K blocks per row (1 or 2)
+  int stages;     // base-tile ring depth
+  const float *xsq, *xscale, *xnorm;
+  const float *qsq, *qscale, *qnorm;
+  uint64_t *best;
+  int k;
+  uint64_t *cand;
+  int cap;
+  uint32_t *count;
+  int *err;
+};
+
+template <int PREC, int MT, int MODE>
+__global__ void __launch_bounds__(kLpThreads, 1)
+    lowp_tile_kernel(const __grid_constant__ CUtensorMap tmap_a,
+                     const __grid_constant__ CUtensorMap tmap_b, LpParams p) {
+  extern __shared__ __align__(1024) uint8_t smraw[];
+  uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  const int nkb = p.nkb, S = p.stages;
+  const uint32_t a_kb_bytes = kLpBM * 128, b_kb_bytes = kLpBN * 128;
+  uint8_t *sA = sm;
+  uint8_t *sB = sm + nkb * a_kb_bytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sB + S * nkb * b_kb_bytes);
+  uint64_t *full = bars, *empty = bars + 4, *a_full = bars + 8, *acc_full = bars + 9,
+           *acc_empty = bars + 11, *done = bars + 13;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 14);
+  volatile int *abort = reinterpret_cast<volatile int *>(bars + 15);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t q0 = (int64_t)blockIdx.x * kLpBM;
+  const int64_t row0 = p.r_begin + (int64_t)blockIdx.y * kLpBN * kLpTilesPerCta;
+  int64_t rows_here = p.r_end - row0;
+  const int T = (int)std::min<int64_t>(kLpTilesPerCta, (rows_here + kLpBN - 1) / kLpBN);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      tc::mbar_init(full + s, 1);
+      tc::mbar_init(empty + s, 1);
+    }
+    tc::mbar_init(a_full, 1);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(acc_full + b, 1);
+      tc::mbar_init(acc_empty + b, kLpEpiThreads);
+    }
+    tc::mbar_init(done, 1);
+    *abort = 0;
+    tc::fence_barrier_init();
+  }
+  if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (tc::elect_one()) {
+      tc::prefetch_tmap(&tmap_a);
+      tc::prefetch_tmap(&tmap_b);
+      const int kb_elems = PREC == HORA_PREC_BF16 ? 64 : 128;
+      tc::mbar_arrive_expect_tx(a_full, nkb * a_kb_bytes);
+      for (int kb = 0; kb < nkb; ++kb) tc::tma_load_2d(sA + kb * a_kb_bytes, &tmap_a, a_full, kb * kb_elems, (int)q0);
+      for (int t = 0; t < T; ++t) {
+        const int s = t % S, j = t / S;
+        if (j > 0 && !tc::mbar_wait(empty + s, (j - 1) & 1, abort)) break;
+        tc::mbar_arrive_expect_tx(full + s, nkb * b_kb_bytes);
+        const int y = (int)(row0 + (int64_t)t * kLpBN);
+        for (int kb = 0; kb < nkb; ++kb)
+          tc::tma_load_2d(sB + (s * nkb + kb) * b_kb_bytes, &tmap_b, full + s, kb * kb_elems, y);
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (tc::elect_one()) {
+      constexpr uint32_t idesc = tc::idesc_f32acc(PREC == HORA_PREC_BF16 ? 1u : 0u, kLpBM, kLpBN);
+      bool ok = tc::mbar_wait(a_full, 0, abort);
+      for (int t = 0; ok && t < T; ++t) {
+        const int s = t % S, j = t / S, b = t & 1, jb = t >> 1;
+        if (!tc::mbar_wait(full + s, j & 1, abort)) break;
+        if (jb > 0 && !tc::mbar_wait(acc_empty + b, (jb - 1) & 1, abort)) break;
+        tc::fence_after_sync();
+        const uint32_t d = tmem + (uint32_t)(b * kLpBN);
+        for (int kb = 0; kb < nkb; ++kb) {
+          const uint32_t a0 = tc::smem_u32(sA + kb * a_kb_bytes);
+          const uint32_t b0 = tc::smem_u32(sB + (s * nkb + kb) * b_kb_bytes);
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t ad = tc::sdesc_kmajor_sw128(a0 + kk * 32);
+            const uint64_t bd = tc::sdesc_kmajor_sw128(b0 + kk * 32);
+            const uint32_t acc = (kb | kk) ? 1u : 0u;
+            if (PREC == HORA_PREC_BF16)
+              tc::mma_bf16(d, ad, bd, idesc, acc);
+            else
+              tc::mma_e4m3(d, ad, bd, idesc, acc);
+          }
+        }
+        tc::mma_commit(empty + s);
+        tc::mma_commit(acc_full + b);
+      }
+      // all MMAs of this thread complete before TMEM is released
+      tc::mma_commit(done);
+      tc::mbar_wait(done, 0, abort, 1u << 20);
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int g = warp & 3;           // TMEM lane group this warp may access
+    const int h = (warp - 2) >> 2;    // column half
+    const int m = g * 32 + lane;      // query row in the tile
+    const int64_t qrow = q0 + m;
+    const int64_t qid = qrow < p.nq ? (p.qmap ? p.qmap[qrow] : qrow) : -1;
+    float qa = 0.0f, qs = 1.0f;
+    if (qid >= 0) {
+      if (MT == M_L2) qa = p.qsq[qid];
+      if (MT == M_COS) qa = p.qnorm[qid];
+      if (PREC == HORA_PREC_FP8) qs = p.qscale[qid];
+    }
+    float tau_d = -__int_as_float(0x7f800000);
+    uint32_t tau_r = 0;
+    if (MODE == TILE_FILTER && qid >= 0) {
+      uint64_t tk = p.best[qid * p.k + (p.k - 1)];
+      tau_d = key_dist(tk);
+      tau_r = key_row(tk);
+      if (tk == kEmptyKey) {  // fewer than R keys yet: every finite distance passes
+        tau_d = __int_as_float(0x7f800000);
+        tau_r = 0xffffffffu;
+      }
+    }
+    for (int t = 0; t < T; ++t) {
+      const int b = t & 1, jb = t >> 1;
+      if (!tc::mbar_wait(acc_full + b, jb & 1, abort)) break;
+      tc::fence_after_sync();
+      const int64_t rt = row0 + (int64_t)t * kLpBN + h * 128;
+#pragma unroll 1
+      for (int c = 0; c < 4; ++c) {
+        uint32_t v[32];
+        tc::tmem_ld32(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + h * 128 + c * 32), v);
+        tc::tmem_ld_wait();
+        if (qid < 0) continue;
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) {
+          const int64_t row = rt + c * 32 + jj;
+          if (row >= p.r_end) break;
+          float dot = __uint_as_float(v[jj]);
+          if (PREC == HORA_PREC_FP8) dot *= qs * __ldg(p.xscale + row);
+          float d;
+          if (MT == M_L2) {
+            d = fmaf(-2.0f, dot, qa + __ldg(p.xsq + row));
+          } else if (MT == M_IP) {
+            d = dot;
+          } else {
+            float den = qa * __ldg(p.xnorm + row);
+            d = den == 0.0f ? 0.0f : -dot / den;
+          }
+          if (MODE == TILE_DENSE) {
+            p.cand[qid * p.cap + (row - p.r_begin)] = make_key(d, (uint32_t)row);
+          } else if (d < tau_d || (d == tau_d && (uint32_t)row < tau_r)) {
+            uint32_t slot = atomicAdd(p.count + qid, 1u);
+            if (slot < (uint32_t)p.cap) p.cand[qid * p.cap + slot] = make_key(d, (uint32_t)row);
+          }
+        }
+      }
+      tc::fence_before_sync();
+      tc::mbar_arrive(acc_empty + b);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 512);
+  }
+  if (threadIdx.x == 0 && *abort) atomicExch(p.err, 1);
 }
+
+// ---- conversions -------------------------------------------------------------------
+__global__ void to_bf16_kernel(const float *X, int64_t n, int64_t ld, int64_t dim, int64_t Dp,
+                               __nv_bfloat16 *out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * Dp) return;
+  int64_t r = i / Dp, t = i % Dp;
+  out[i] = __float2bfloat16_rn(t < dim ? X[r * ld + t] : 0.0f);
+}
+
+// one warp per row: per-row absmax scale so the row's largest entry maps to 448
+__global__ void to_e4m3_kernel(const float *X, int64_t n, int64_t ld, int64_t dim, int64_t Dp,
+                               uint8_t *out, float *scale) {
+  int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  float mx = 0.0f;
+  for (int64_t t = lane; t < dim; t += 32) mx = fmaxf(mx, fabsf(X[r * ld + t]));
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  float s = mx > 0.0f ? mx / 448.0f : 1.0f;
+  float inv = 1.0f / s;
+  for (int64_t t = lane; t < Dp; t += 32) {
+    float v = t < dim ? X[r * ld + t] * inv : 0.0f;
+    out[r * Dp + t] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+  }
+  if (lane == 0) scale[r] = s;
+}
+
+__global__ void f64_to_f32_kernel(const double *a, int64_t n, float *out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)a[i];
+}
+
+__global__ void gather_rows_u8_kernel(const uint8_t *src, int64_t row_bytes, const int *rows,
+                                      int64_t n, uint8_t *dst) {
+  int64_t r = blockIdx.x;
+  if (r >= n) return;
+  const uint8_t *s = src + (int64_t)rows[r] * row_bytes;
+  for (int64_t t = threadIdx.x; t < row_bytes; t += blockDim.x) dst[r * row_bytes + t] = s[t];
+}
+
+// ---- host ------------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int encode_fn(EncodeTiledFn *out) {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+      return fail(HORA_ECUDA, "cuTensorMapEncodeTiled unavailable");
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  *out = fn;
+  return HORA_OK;
+}
+
+// 2-D K-major map: rows x row_bytes, box = 128 bytes x box_rows, 128B swizzle.
+static int make_tmap(CUtensorMap *m, const void *ptr, int prec, int64_t Dp, int64_t rows,
+                     uint32_t box_rows) {
+  EncodeTiledFn enc;
+  HORA_TRY(encode_fn(&enc));
+  const bool bf = prec == HORA_PREC_BF16;
+  const uint64_t esz = bf ? 2 : 1;
+  cuuint64_t dims[2] = {(cuuint64_t)Dp, (cuuint64_t)std::max<int64_t>(rows, 1)};
+  cuuint64_t strides[1] = {(cuuint64_t)(Dp * esz)};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / esz), box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(m, bf ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 2,
+                   const_cast<void *>(ptr), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(HORA_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return HORA_OK;
+}
+
+static int lp_smem_bytes(int nkb, int stages) {
+  return 1024 + nkb * kLpBM * 128 + stages * nkb * kLpBN * 128 + 16 * 8 + 64;
+}
+
+template <int PREC, int MT, int MODE>
+static int launch_lp3(const CUtensorMap &ta, const CUtensorMap &tb, const LpParams &p,
+                      cudaStream_t s) {
+  const int smem = lp_smem_bytes(p.nkb, p.stages);
+  static int attr = 0;
+  if (attr < smem) {
+    HORA_CUDA_TRY(cudaFuncSetAttribute(lowp_tile_kernel<PREC, MT, MODE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr = smem;
+  }
+  const int64_t rows = p.r_end - p.r_begin;
+  dim3 grid((unsigned)ceil_div(p.nq, kLpBM), (unsigned)ceil_div(rows, (int64_t)kLpBN * kLpTilesPerCta));
+  if (grid.x == 0 || grid.y == 0) return HORA_OK;
+  ProfScope ps(PREC == HORA_PREC_BF16 ? "bf16_tc_scan" : "fp8_tc_scan", s);
+  lowp_tile_kernel<PREC, MT, MODE><<<grid, kLpThreads, smem, s>>>(ta, tb, p);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+template <int PREC>
+static int launch_lp2(int metric, int mode, const CUtensorMap &ta, const CUtensorMap &tb,
+                      const LpParams &p, cudaStream_t s) {
+  const bool dense = mode == TILE_DENSE;
+  switch (metric) {
+    case M_L2: return dense ? launch_lp3<PREC, M_L2, TILE_DENSE>(ta, tb, p, s) : launch_lp3<PREC, M_L2, TILE_FILTER>(ta, tb, p, s);
+    case M_IP: return dense ? launch_lp3<PREC, M_IP, TILE_DENSE>(ta, tb, p, s) : launch_lp3<PREC, M_IP, TILE_FILTER>(ta, tb, p, s);
+    case M_COS: return dense ? launch_lp3<PREC, M_COS, TILE_DENSE>(ta, tb, p, s) : launch_lp3<PREC, M_COS, TILE_FILTER>(ta, tb, p, s);
+  }
+  return fail(HORA_EMETRIC, "no tensor-core form for this metric");
+}
+
+static int launch_lp(int prec, int metric, int mode, const CUtensorMap &ta, const CUtensorMap &tb,
+                     const LpParams &p, cudaStream_t s) {
+  return prec == HORA_PREC_BF16 ? launch_lp2<HORA_PREC_BF16>(metric, mode, ta, tb, p, s)
+                                : launch_lp2<HORA_PREC_FP8>(metric, mode, ta, tb, p, s);
+}
+
+// Low-precision copy of the base (and its exact squared norms / scales),
+// rebuilt when the precision or the item count changes.
+static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
+  const int64_t kbe = prec == HORA_PREC_BF16 ? 64 : 128;
+  const int64_t Dp = round_up((int64_t)h->dim, kbe);
+  if (h->lowp && h->lowp->prec == prec && h->lowp->n == h->n) return HORA_OK;
+  std::unique_ptr<LowpState, LowpDeleter> st(new LowpState());
+  st->prec = prec;
+  st->n = h->n;
+  st->Dp = Dp;
+  const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
+  HORA_TRY(st->base.reserve(std::max<int64_t>(h->n, 1) * Dp * esz));
+  HORA_TRY(st->xsq.reserve(sizeof(float) * std::max<int64_t>(h->n, 1)));
+  HORA_TRY(st->err.reserve(16));
+  {
+    ProfScope ps("lowp_convert", s);
+    if (prec == HORA_PREC_BF16) {
+      to_bf16_kernel<<<ceil_div(h->n * Dp, 256), 256, 0, s>>>(h->base.as<float>(), h->n, h->ld, h->dim,
+                                                              Dp, st->base.as<__nv_bfloat16>());
+    } else {
+      HORA_TRY(st->xscale.reserve(sizeof(float) * std::max<int64_t>(h->n, 1)));
+      to_e4m3_kernel<<<ceil_div(h->n, 8), 256, 0, s>>>(h->base.as<float>(), h->n, h->ld, h->dim, Dp,
+                                                       st->base.as<uint8_t>(), st->xscale.as<float>());
+    }
+    HORA_LAUNCHED();
+    f64_to_f32_kernel<<<ceil_div(h->n, 256), 256, 0, s>>>(h->xsq64.as<double>(), h->n, st->xsq.as<float>());
+    HORA_LAUNCHED();
+  }
+  HORA_TRY(make_tmap(&st->tmap_b, st->base.ptr, prec, Dp, h->n, kLpBN));
+  h->lowp = std::move(st);
+  return HORA_OK;
+}
+
+int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
+                     cudaStream_t s) {
+  const int prec = h->precision;
+  const int64_t kbe = prec == HORA_PREC_BF16 ? 64 : 128;
+  const int64_t Dp = round_up((int64_t)h->dim, kbe);
+  const int nkb = (int)(Dp / kbe);
+  if (h->metric == M_L1 || nkb > 2) {
+    // no tensor-core form (Manhattan) or dimension beyond the resident tile:
+    // the exact FP32 path answers
+    int retries = 0;
+    HORA_TRY(bf_topk_exact(base_view(h), h->metric, ws.q.as<float>(), ws.qnorm.as<float>(), nq, k,
+                           h->cand_cap, ws, d_best, s, &retries));
+    h->last_retries = retries;
+    return HORA_OK;
+  }
+  HORA_TRY(ensure_lowp(h, prec, s));
+  LowpState &L = *h->lowp;
+  int R = h->rerank > 0 ? h->rerank : (prec == HORA_PREC_BF16 ? std::max(2 * k, k + 64) : std::max(4 * k, k + 128));
+  R = std::max(R, k);
+  R = (int)std::min<int64_t>(R, std::max<int64_t>(h->n, k));
+  if (R > 4096) return fail(HORA_ECAP, "rerank width must be <= 4096");
+  int cap = std::max(h->cand_cap, 2 * R);
+  cap = (int)round_up(cap, 128);
+  const int stages = nkb == 1 ? 4 : 2;
+  const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
+
+  // query copies
+  HORA_TRY(L.q.reserve(std::max<int64_t>(nq, 1) * Dp * esz));
+  HORA_TRY(L.qsq.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
+  const double *qsq64 = reinterpret_cast<const double *>(ws.qnorm.as<char>() + round_up(sizeof(float) * nq, 16));
+  {
+    ProfScope ps("lowp_convert", s);
+    if (prec == HORA_PREC_BF16) {
+      to_bf16_kernel<<<ceil_div(nq * Dp, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp,
+                                                            L.q.as<__nv_bfloat16>());
+    } else {
+      HORA_TRY(L.qscale.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
+      to_e4m3_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp,
+                                                     L.q.as<uint8_t>(), L.qscale.as<float>());
+    }
+    HORA_LAUNCHED();
+    f64_to_f32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(qsq64, nq, L.qsq.as<float>());
+    HORA_LAUNCHED();
+  }
+  CUtensorMap ta;
+  HORA_TRY(make_tmap(&ta, L.q.ptr, prec, Dp, nq, kLpBM));
+
+  // approximate R-best lists
+  HORA_TRY(ws.best.reserve(sizeof(uint64_t) * nq * R));
+  HORA_TRY(ws.cand.reserve(sizeof(uint64_t) * nq * cap));
+  HORA_TRY(ws.count.reserve(sizeof(uint32_t) * nq));
+  HORA_TRY(ws.ovf_flag.reserve(nq));
+  HORA_TRY(ws.ovf_counter.reserve(sizeof(uint32_t)));
+  HORA_TRY(ws.qlist.reserve(sizeof(int) * nq));
+  uint64_t *bestR = ws.best.as<uint64_t>();
+  uint32_t *count = ws.count.as<uint32_t>();
+  uint8_t *flags = ws.ovf_flag.as<uint8_t>();
+  uint32_t *ovc = ws.ovf_counter.as<uint32_t>();
+  HORA_CUDA_TRY(cudaMemsetAsync(bestR, 0xff, sizeof(uint64_t) * nq * R, s));
+  HORA_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t) * nq, s));
+  HORA_CUDA_TRY(cudaMemsetAsync(flags, 0, nq, s));
+  HORA_CUDA_TRY(cudaMemsetAsync(ovc, 0, sizeof(uint32_t), s));
+  HORA_CUDA_TRY(cudaMemsetAsync(L.err.ptr, 0, 16, s));
+
+  LpParams p{};
+  p.nq = nq;
+  p.qmap = nullptr;
+  p.nkb = nkb;
+  p.stages = stages;
+  p.xsq = L.xsq.as<float>();
+  p.xscale = L.xscale.as<float>();
+  p.xnorm = h->xnorm.as<float>();
+  p.qsq = L.qsq.as<float>();
+  p.qscale = L.qscale.as<float>();
+  p.qnorm = ws.qnorm.as<float>();
+  p.best = bestR;
+  p.k = R;
+  p.cand = ws.cand.as<uint64_t>();
+  p.cap = cap;
+  p.count = count;
+  p.err = L.err.as<int>();
+  const int64_t n = h->n;
+  int64_t c0 = std::min<int64_t>(n, std::min<int64_t>(cap, round_up(std::max(2 * R, 1024), kLpBN)));
+  p.r_begin = 0;
+  p.r_end = c0;
+  HORA_TRY(launch_lp(prec, h->metric, TILE_DENSE, ta, L.tmap_b, p, s));
+  HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, (int)c0, nullptr, nq, flags, ovc, s));
+  int64_t done = c0;
+  const int64_t max_chunk = (int64_t)60000 * kLpBN * kLpTilesPerCta;
+  while (done < n) {
+    double grow = (double)cap / (4.0 * R);
+    int64_t c = (int64_t)((double)done * std::max(grow, 1.0));
+    c = std::max<int64_t>(c, (int64_t)kLpBN * 64);
+    c = std::min<int64_t>(round_up(c, kLpBN), std::min<int64_t>(n - done, max_chunk));
+    p.r_begin = done;
+    p.r_end = done + c;
+    HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, ta, L.tmap_b, p, s));
+    HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s));
+    done += c;
+  }
+  // overflow rescans over gathered query rows
+  uint32_t h_ovc = 0;
+  int errflag = 0;
+  HORA_CUDA_TRY(cudaMemcpyAsync(&h_ovc, ovc, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaMemcpyAsync(&errflag, L.err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (errflag) return fail(HORA_ETIMEDOUT, "tensor-core scan: a pipeline wait timed out");
+  int rounds = 0;
+  while (h_ovc > 0) {
+    if (++rounds > 64) return fail(HORA_ECUDA, "candidate overflow did not converge");
+    ws.h_flags.resize(nq);
+    HORA_CUDA_TRY(cudaMemcpyAsync(ws.h_flags.data(), flags, nq, cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<int> list;
+    for (int64_t q = 0; q < nq; ++q)
+      if (ws.h_flags[q]) list.push_back((int)q);
+    const int64_t nl = (int64_t)list.size();
+    HORA_CUDA_TRY(cudaMemcpyAsync(ws.qlist.ptr, list.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, s));
+    HORA_CUDA_TRY(cudaMemsetAsync(flags, 0, nq, s));
+    HORA_CUDA_TRY(cudaMemsetAsync(ovc, 0, sizeof(uint32_t), s));
+    HORA_TRY(L.qgather.reserve(nl * Dp * esz));
+    gather_rows_u8_kernel<<<(unsigned)nl, 128, 0, s>>>(L.q.as<uint8_t>(), Dp * esz, ws.qlist.as<int>(), nl,
+                                                       L.qgather.as<uint8_t>());
+    HORA_LAUNCHED();
+    CUtensorMap tg;
+    HORA_TRY(make_tmap(&tg, L.qgather.ptr, prec, Dp, nl, kLpBM));
+    LpParams r = p;
+    r.nq = nl;
+    r.qmap = ws.qlist.as<int>();
+    for (int64_t lo = 0; lo < n; lo += max_chunk) {
+      r.r_begin = lo;
+      r.r_end = std::min<int64_t>(n, lo + max_chunk);
+      HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, tg, L.tmap_b, r, s));
+      HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, ws.qlist.as<int>(), nl, flags, ovc, s));
+    }
+    HORA_CUDA_TRY(cudaMemcpyAsync(&h_ovc, ovc, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  h->last_retries = rounds;
+  // exact FP32 rerank of the R candidates, then the k best
+  HORA_TRY(ws.tmp.reserve(sizeof(uint64_t) * nq * R));
+  HORA_TRY(launch_rerank_exact(h->metric, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim,
+                               ws.qnorm.as<float>(), h->xnorm.as<float>(), bestR, nq, R,
+                               ws.tmp.as<uint64_t>(), s));
+  HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
+  HORA_TRY(launch_merge_topk(d_best, k, ws.tmp.as<uint64_t>(), nullptr, R, R, nullptr, nq, flags, ovc, s));
+  return HORA_OK;
+}
+
+}  // namespace hora

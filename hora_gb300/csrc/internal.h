@@ -44,6 +44,12 @@ int launch_row_norms(const float *X, int64_t n, int64_t ld, int64_t dim, float *
 int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint32_t *flag,
                         cudaStream_t s);
 
+// Exact FP32 distances (reference op order) for R candidate rows per query:
+// in = approximate keys (row in the low word), out = exact keys.
+int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, int64_t dim,
+                        const float *qnorm, const float *xnorm, const uint64_t *in, int64_t nq,
+                        int R, uint64_t *out, cudaStream_t s);
+
 // ---- selection (topk.cu) ------------------------------------------------------
 // Merges each query's candidates into its sorted k-best key list (dedup by
 // key).  dense_n > 0: candidates are the first dense_n slots, count ignored.

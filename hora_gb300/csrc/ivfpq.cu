@@ -642,28 +642,6 @@ __global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
   }
 }
 
-// Exact FP32 rerank of each query's R best ADC rows with the index metric.
-template <int MT>
-__global__ void rerank_kernel(const float *Q, int64_t ld, const float *X, int64_t dim,
-                              const float *qnorm, const float *xnorm, const uint64_t *in, int R,
-                              uint64_t *outk) {
-  const int64_t q = blockIdx.x;
-  for (int r = threadIdx.x; r < R; r += blockDim.x) {
-    uint64_t key = in[q * R + r];
-    if (key == kEmptyKey) {
-      outk[q * R + r] = kEmptyKey;
-      continue;
-    }
-    uint32_t row = key_row(key);
-    const float *x = X + (int64_t)row * ld;
-    const float *qq = Q + q * ld;
-    float s = 0.0f;
-    for (int64_t t = 0; t < dim; ++t) s = dist_op<MT == M_COS ? M_IP : MT>(s, qq[t], x[t]);
-    if (MT == M_COS) s = cosine_from_dot(s, qnorm[q], xnorm[row]);
-    outk[q * R + r] = make_key(s, row);
-  }
-}
-
 // ---------------------------------------------------------------------------
 // host side
 
@@ -1109,16 +1087,8 @@ int ivf_search_keys(hora_index *h, int64_t nq, int k, int64_t nprobe, const uint
   if (R > k) {
     HORA_TRY(v.tmp_keys.reserve(sizeof(uint64_t) * nq * R));
     if (h->metric == M_COS) HORA_TRY(ensure_norms(h, s));
-    {
-      ProfScope ps("ivf_rerank", s);
-      switch (h->metric) {
-        case M_L2: rerank_kernel<M_L2><<<(unsigned)nq, 128, 0, s>>>(Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(), h->xnorm.as<float>(), merged, R, v.tmp_keys.as<uint64_t>()); break;
-        case M_L1: rerank_kernel<M_L1><<<(unsigned)nq, 128, 0, s>>>(Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(), h->xnorm.as<float>(), merged, R, v.tmp_keys.as<uint64_t>()); break;
-        case M_IP: rerank_kernel<M_IP><<<(unsigned)nq, 128, 0, s>>>(Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(), h->xnorm.as<float>(), merged, R, v.tmp_keys.as<uint64_t>()); break;
-        default: rerank_kernel<M_COS><<<(unsigned)nq, 128, 0, s>>>(Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(), h->xnorm.as<float>(), merged, R, v.tmp_keys.as<uint64_t>()); break;
-      }
-      HORA_LAUNCHED();
-    }
+    HORA_TRY(launch_rerank_exact(h->metric, Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(),
+                                 h->xnorm.as<float>(), merged, nq, R, v.tmp_keys.as<uint64_t>(), s));
     HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
     HORA_TRY(launch_merge_topk(d_best, k, v.tmp_keys.as<uint64_t>(), nullptr, R, R, nullptr, nq,
                                ws.ovf_flag.as<uint8_t>(), ws.ovf_counter.as<uint32_t>(), s));
