@@ -46,7 +46,6 @@ struct LowpState {
   DevBuf xsq;     // n f32 exact squared norms
   DevBuf xscale;  // n f32 (e4m3 per-row scale)
   CUtensorMap tmap_b;
-  DevBuf q, qsq, qscale, qgather, err;
 };
 
 void lowp_state_free(LowpState *p) { delete p; }
@@ -363,7 +362,6 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
   const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
   HORA_TRY(st->base.reserve(std::max<int64_t>(h->n, 1) * Dp * esz));
   HORA_TRY(st->xsq.reserve(sizeof(float) * std::max<int64_t>(h->n, 1)));
-  HORA_TRY(st->err.reserve(16));
   {
     ProfScope ps("lowp_convert", s);
     if (prec == HORA_PREC_BF16) {
@@ -410,25 +408,26 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
 
   // query copies
-  HORA_TRY(L.q.reserve(std::max<int64_t>(nq, 1) * Dp * esz));
-  HORA_TRY(L.qsq.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
+  HORA_TRY(ws.lq.reserve(std::max<int64_t>(nq, 1) * Dp * esz));
+  HORA_TRY(ws.lerr.reserve(16));
+  HORA_TRY(ws.lqsq.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
   const double *qsq64 = reinterpret_cast<const double *>(ws.qnorm.as<char>() + round_up(sizeof(float) * nq, 16));
   {
     ProfScope ps("lowp_convert", s);
     if (prec == HORA_PREC_BF16) {
       to_bf16_kernel<<<ceil_div(nq * Dp, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp,
-                                                            L.q.as<__nv_bfloat16>());
+                                                            ws.lq.as<__nv_bfloat16>());
     } else {
-      HORA_TRY(L.qscale.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
+      HORA_TRY(ws.lqscale.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
       to_e4m3_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp,
-                                                     L.q.as<uint8_t>(), L.qscale.as<float>());
+                                                     ws.lq.as<uint8_t>(), ws.lqscale.as<float>());
     }
     HORA_LAUNCHED();
-    f64_to_f32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(qsq64, nq, L.qsq.as<float>());
+    f64_to_f32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(qsq64, nq, ws.lqsq.as<float>());
     HORA_LAUNCHED();
   }
   CUtensorMap ta;
-  HORA_TRY(make_tmap(&ta, L.q.ptr, prec, Dp, nq, kLpBM));
+  HORA_TRY(make_tmap(&ta, ws.lq.ptr, prec, Dp, nq, kLpBM));
 
   // approximate R-best lists
   HORA_TRY(ws.best.reserve(sizeof(uint64_t) * nq * R));
@@ -445,7 +444,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   HORA_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t) * nq, s));
   HORA_CUDA_TRY(cudaMemsetAsync(flags, 0, nq, s));
   HORA_CUDA_TRY(cudaMemsetAsync(ovc, 0, sizeof(uint32_t), s));
-  HORA_CUDA_TRY(cudaMemsetAsync(L.err.ptr, 0, 16, s));
+  HORA_CUDA_TRY(cudaMemsetAsync(ws.lerr.ptr, 0, 16, s));
 
   LpParams p{};
   p.nq = nq;
@@ -455,15 +454,15 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   p.xsq = L.xsq.as<float>();
   p.xscale = L.xscale.as<float>();
   p.xnorm = h->xnorm.as<float>();
-  p.qsq = L.qsq.as<float>();
-  p.qscale = L.qscale.as<float>();
+  p.qsq = ws.lqsq.as<float>();
+  p.qscale = ws.lqscale.as<float>();
   p.qnorm = ws.qnorm.as<float>();
   p.best = bestR;
   p.k = R;
   p.cand = ws.cand.as<uint64_t>();
   p.cap = cap;
   p.count = count;
-  p.err = L.err.as<int>();
+  p.err = ws.lerr.as<int>();
   const int64_t n = h->n;
   int64_t c0 = std::min<int64_t>(n, std::min<int64_t>(cap, round_up(std::max(2 * R, 1024), kLpBN)));
   p.r_begin = 0;
@@ -487,7 +486,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   uint32_t h_ovc = 0;
   int errflag = 0;
   HORA_CUDA_TRY(cudaMemcpyAsync(&h_ovc, ovc, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  HORA_CUDA_TRY(cudaMemcpyAsync(&errflag, L.err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaMemcpyAsync(&errflag, ws.lerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
   HORA_CUDA_TRY(cudaStreamSynchronize(s));
   if (errflag) return fail(HORA_ETIMEDOUT, "tensor-core scan: a pipeline wait timed out");
   int rounds = 0;
@@ -503,12 +502,12 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     HORA_CUDA_TRY(cudaMemcpyAsync(ws.qlist.ptr, list.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, s));
     HORA_CUDA_TRY(cudaMemsetAsync(flags, 0, nq, s));
     HORA_CUDA_TRY(cudaMemsetAsync(ovc, 0, sizeof(uint32_t), s));
-    HORA_TRY(L.qgather.reserve(nl * Dp * esz));
-    gather_rows_u8_kernel<<<(unsigned)nl, 128, 0, s>>>(L.q.as<uint8_t>(), Dp * esz, ws.qlist.as<int>(), nl,
-                                                       L.qgather.as<uint8_t>());
+    HORA_TRY(ws.lqgather.reserve(nl * Dp * esz));
+    gather_rows_u8_kernel<<<(unsigned)nl, 128, 0, s>>>(ws.lq.as<uint8_t>(), Dp * esz, ws.qlist.as<int>(), nl,
+                                                       ws.lqgather.as<uint8_t>());
     HORA_LAUNCHED();
     CUtensorMap tg;
-    HORA_TRY(make_tmap(&tg, L.qgather.ptr, prec, Dp, nl, kLpBM));
+    HORA_TRY(make_tmap(&tg, ws.lqgather.ptr, prec, Dp, nl, kLpBM));
     LpParams r = p;
     r.nq = nl;
     r.qmap = ws.qlist.as<int>();

@@ -78,6 +78,18 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
 int ivf_build(hora_index *h);
 int ivf_search_keys(hora_index *h, int64_t nq, int k, int64_t nprobe, const uint32_t *d_nprobe,
                     SearchWorkspace &ws, uint64_t *d_best, cudaStream_t s);
+int ivf_pmax(const hora_index *h, int64_t nprobe);
+int ivf_probe(hora_index *h, int64_t nq, int pmax, SearchWorkspace &ws, cudaStream_t s);
+const uint64_t *ivf_probe_keys(const SearchWorkspace &ws);
+int ivf_adc_merge(hora_index *h, int64_t nq, int pmax, int jbegin, const uint32_t *d_nprobe,
+                  int R, uint64_t *M, SearchWorkspace &ws, cudaStream_t s);
+int ivf_finalize(hora_index *h, int64_t nq, int k, int R, const uint64_t *M, SearchWorkspace &ws,
+                 uint64_t *d_best, cudaStream_t s);
+int ivf_rerank_width(const hora_index *h, int k);
+uint64_t *ivf_merge_buffer(SearchWorkspace &ws, int64_t nq, int R, uint64_t *d_best, int k);
+// learned nprobe (nprobe_mlp.cu)
+int ivf_search_learned(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
+                       cudaStream_t s);
 int ivf_layout(const hora_index *h, uint64_t *n_list, uint64_t *n_sub, uint64_t *sub_bits,
                uint64_t *dmax);
 int ivf_export(const hora_index *h, float *centers, int64_t *offsets, int64_t *items,

@@ -68,9 +68,18 @@ int launch_rows_topk(const float *D, int64_t rows, int64_t cols, int64_t ldd, in
                      uint64_t *out_keys, cudaStream_t s);
 
 // ---- brute force (bf_search.cu) ---------------------------------------------------
+// Per-search scratch.  One workspace per concurrent search context (the
+// handle owns one; every serving slot owns another), so searches on
+// different contexts can run on different streams over the same index.
 struct SearchWorkspace {
   DevBuf q, qnorm, best, cand, count, ovf_flag, ovf_counter, qlist, out_ids, out_dist, rows,
       keys2, tmp;
+  // IVF-PQ
+  DevBuf coarse, probes, pair_cnt, pair_off, pair_q, pair_c, pair_slot, ivf_cand, best_r, tmp_keys;
+  // low-precision scoring
+  DevBuf lq, lqsq, lqscale, lqgather, lerr;
+  // learned nprobe
+  DevBuf feats, pred, npq;
   std::vector<uint8_t> h_flags;
 };
 

@@ -42,9 +42,6 @@ struct IvfState {
   std::vector<int64_t> h_offsets;
   std::vector<uint8_t> h_trained;
   int64_t max_list = 0;
-  // search scratch
-  DevBuf coarse, probes, pair_q, pair_c, pair_slot, pair_cnt, pair_off, cand, best_r, nprobe_q;
-  DevBuf tmp_keys;
 };
 
 void ivf_state_free(IvfState *p) { delete p; }
@@ -442,7 +439,7 @@ __global__ void __launch_bounds__(256) pq_encode_kernel(
 // search
 
 // Pairs (query, probe slot) grouped by list: histogram / scan / scatter.
-__global__ void pair_hist_kernel(const uint64_t *probes, int64_t nq, int pmax,
+__global__ void pair_hist_kernel(const uint64_t *probes, int64_t nq, int pmax, int jbegin,
                                  const uint32_t *nprobe_q, int C, int64_t *cnt) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nq * pmax) return;
@@ -450,11 +447,11 @@ __global__ void pair_hist_kernel(const uint64_t *probes, int64_t nq, int pmax,
   int j = (int)(t % pmax);
   int p = nprobe_q ? (int)nprobe_q[q] : pmax;
   uint64_t k = probes[t];
-  if (j >= p || k == kEmptyKey) return;
+  if (j < jbegin || j >= p || k == kEmptyKey) return;
   atomicAdd(reinterpret_cast<unsigned long long *>(cnt + key_row(k)), 1ull);
 }
 
-__global__ void pair_scatter_kernel(const uint64_t *probes, int64_t nq, int pmax,
+__global__ void pair_scatter_kernel(const uint64_t *probes, int64_t nq, int pmax, int jbegin,
                                     const uint32_t *nprobe_q, int C, const int64_t *off,
                                     int64_t *cursor, uint32_t *pq, uint32_t *pc, uint32_t *pslot) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -463,7 +460,7 @@ __global__ void pair_scatter_kernel(const uint64_t *probes, int64_t nq, int pmax
   int j = (int)(t % pmax);
   int p = nprobe_q ? (int)nprobe_q[q] : pmax;
   uint64_t k = probes[t];
-  if (j >= p || k == kEmptyKey) return;
+  if (j < jbegin || j >= p || k == kEmptyKey) return;
   uint32_t c = key_row(k);
   int64_t pos = off[c] + (int64_t)atomicAdd(reinterpret_cast<unsigned long long *>(cursor + c), 1ull);
   pq[pos] = (uint32_t)q;
@@ -968,8 +965,8 @@ int ivf_set_codebooks(hora_index *h, const float *centers, const float *codebook
 }
 
 template <int DM>
-static int launch_adc(IvfState &v, const float *Q, int64_t ldq, int64_t ldc, int64_t npairs,
-                      int per, int kk, int pmax, uint64_t *cand, cudaStream_t s) {
+static int launch_adc(IvfState &v, SearchWorkspace &ws, const float *Q, int64_t ldq, int64_t ldc,
+                      int64_t npairs, int per, int kk, int pmax, uint64_t *cand, cudaStream_t s) {
   size_t smem = sizeof(float) * v.n_sub * v.K + sizeof(uint32_t) * (kAdcChunk + 1024) +
                 sizeof(int) * 1024 + 256 * 4 + 40 * 4 + sizeof(uint32_t) * (kAdcChunk + 1024);
   if (smem > 200 * 1024) return fail(HORA_ECAP, "IVF-PQ: LUT too large for shared memory");
@@ -979,28 +976,29 @@ static int launch_adc(IvfState &v, const float *Q, int64_t ldq, int64_t ldc, int
   ProfScope ps("adc_scan", s);
   adc_scan_kernel<DM><<<grid, kAdcThreads, smem, s>>>(
       Q, ldq, v.centers.as<float>(), ldc, v.books.as<float>(), v.codes.as<uint8_t>(),
-      v.items.as<uint32_t>(), v.offsets.as<int64_t>(), v.trained.as<uint8_t>(), v.pair_q.as<uint32_t>(),
-      v.pair_c.as<uint32_t>(), v.pair_slot.as<uint32_t>(), npairs, per, (int)v.n_sub, (int)v.K,
+      v.items.as<uint32_t>(), v.offsets.as<int64_t>(), v.trained.as<uint8_t>(), ws.pair_q.as<uint32_t>(),
+      ws.pair_c.as<uint32_t>(), ws.pair_slot.as<uint32_t>(), npairs, per, (int)v.n_sub, (int)v.K,
       v.sub_begin_d.as<int>(), v.sub_len_d.as<int>(), kk, pmax, cand);
   HORA_LAUNCHED();
   return HORA_OK;
 }
 
-int ivf_search_keys(hora_index *h, int64_t nq, int k, int64_t nprobe, const uint32_t *d_nprobe,
-                    SearchWorkspace &ws, uint64_t *d_best, cudaStream_t s) {
-  if (!h->ivfs) return fail(HORA_ENOTBUILT, "index not built");
-  IvfState &v = *h->ivfs;
-  const int C = (int)v.n_list;
+int ivf_pmax(const hora_index *h, int64_t nprobe) {
+  const int64_t C = (int64_t)h->ivf.n_kmeans_center;
   int64_t pmax = nprobe > 0 ? nprobe : (int64_t)h->ivf.search_n_center;
   if (pmax > C) pmax = C;  // the reference pops an empty heap (panics) here
   if (pmax < 1) pmax = 1;
-  const int R = h->ivf_rerank > k ? h->ivf_rerank : k;  // ADC candidates kept per query
-  if (R > 1024) return fail(HORA_ECAP, "IVF-PQ: k (or rerank width) must be <= 1024");
-  const float *Q = ws.q.as<float>();
-  // 1) coarse distances and probes (pq_idx.rs:416-425)
-  HORA_TRY(v.coarse.reserve(sizeof(float) * nq * C));
+  return (int)pmax;
+}
+
+// Coarse distances of the staged queries to every centre and each query's
+// pmax nearest lists, ascending (pq_idx.rs:416-425).
+int ivf_probe(hora_index *h, int64_t nq, int pmax, SearchWorkspace &ws, cudaStream_t s) {
+  IvfState &v = *h->ivfs;
+  const int C = (int)v.n_list;
+  HORA_TRY(ws.coarse.reserve(sizeof(float) * nq * C));
   TileParams p;
-  p.Q = Q;
+  p.Q = ws.q.as<float>();
   p.ldq = h->ld;
   p.nq = nq;
   p.X = v.centers.as<float>();
@@ -1010,90 +1008,130 @@ int ivf_search_keys(hora_index *h, int64_t nq, int k, int64_t nprobe, const uint
   p.ld = h->ld;
   p.qnorm = ws.qnorm.as<float>();
   p.xnorm = v.cnorm.as<float>();
-  p.out_dist = v.coarse.as<float>();
+  p.out_dist = ws.coarse.as<float>();
   p.ldo = C;
   HORA_TRY(launch_dist_tile(h->metric, TILE_DIST, p, s));
-  HORA_TRY(v.probes.reserve(sizeof(uint64_t) * nq * pmax));
-  HORA_TRY(launch_rows_topk(v.coarse.as<float>(), nq, C, C, (int)pmax, v.probes.as<uint64_t>(), s));
-  // 2) (query, list) pairs grouped by list
-  HORA_TRY(v.pair_cnt.reserve(sizeof(int64_t) * (C + 1) * 2));
-  HORA_TRY(v.pair_off.reserve(sizeof(int64_t) * (C + 1)));
-  int64_t *cnt = v.pair_cnt.as<int64_t>();
+  HORA_TRY(ws.probes.reserve(sizeof(uint64_t) * nq * pmax));
+  HORA_TRY(launch_rows_topk(ws.coarse.as<float>(), nq, C, C, pmax, ws.probes.as<uint64_t>(), s));
+  return HORA_OK;
+}
+
+const uint64_t *ivf_probe_keys(const SearchWorkspace &ws) { return ws.probes.as<uint64_t>(); }
+
+// ADC over the probe slots [jbegin, min(nprobe_q, pmax)) of every query,
+// merged into M (nq x R keys, kept sorted; the caller initialises it).
+int ivf_adc_merge(hora_index *h, int64_t nq, int pmax, int jbegin, const uint32_t *d_nprobe,
+                  int R, uint64_t *M, SearchWorkspace &ws, cudaStream_t s) {
+  IvfState &v = *h->ivfs;
+  const int C = (int)v.n_list;
+  const float *Q = ws.q.as<float>();
+  HORA_TRY(ws.pair_cnt.reserve(sizeof(int64_t) * (C + 1) * 2));
+  HORA_TRY(ws.pair_off.reserve(sizeof(int64_t) * (C + 1)));
+  int64_t *cnt = ws.pair_cnt.as<int64_t>();
   int64_t *cursor = cnt + (C + 1);
   HORA_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (C + 1) * 2, s));
-  int64_t tot = nq * pmax;
+  const int64_t tot = nq * pmax;
   {
     ProfScope ps("ivf_pairs", s);
-    pair_hist_kernel<<<ceil_div(tot, 256), 256, 0, s>>>(v.probes.as<uint64_t>(), nq, (int)pmax,
+    pair_hist_kernel<<<ceil_div(tot, 256), 256, 0, s>>>(ws.probes.as<uint64_t>(), nq, pmax, jbegin,
                                                        d_nprobe, C, cnt);
     HORA_LAUNCHED();
-    offsets_scan_kernel<<<1, 1024, 0, s>>>(cnt, C, v.pair_off.as<int64_t>());
+    offsets_scan_kernel<<<1, 1024, 0, s>>>(cnt, C, ws.pair_off.as<int64_t>());
     HORA_LAUNCHED();
   }
-  int64_t npairs = tot;
+  int64_t npairs = nq * (pmax - jbegin);
   if (d_nprobe) {
-    HORA_CUDA_TRY(cudaMemcpyAsync(&npairs, v.pair_off.as<int64_t>() + C, sizeof(int64_t),
+    HORA_CUDA_TRY(cudaMemcpyAsync(&npairs, ws.pair_off.as<int64_t>() + C, sizeof(int64_t),
                                   cudaMemcpyDeviceToHost, s));
     HORA_CUDA_TRY(cudaStreamSynchronize(s));
   }
-  HORA_TRY(v.pair_q.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
-  HORA_TRY(v.pair_c.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
-  HORA_TRY(v.pair_slot.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
+  if (npairs <= 0) return HORA_OK;
+  HORA_TRY(ws.pair_q.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
+  HORA_TRY(ws.pair_c.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
+  HORA_TRY(ws.pair_slot.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
   {
     ProfScope ps("ivf_pairs", s);
     pair_scatter_kernel<<<ceil_div(tot, 256), 256, 0, s>>>(
-        v.probes.as<uint64_t>(), nq, (int)pmax, d_nprobe, C, v.pair_off.as<int64_t>(), cursor,
-        v.pair_q.as<uint32_t>(), v.pair_c.as<uint32_t>(), v.pair_slot.as<uint32_t>());
+        ws.probes.as<uint64_t>(), nq, pmax, jbegin, d_nprobe, C, ws.pair_off.as<int64_t>(), cursor,
+        ws.pair_q.as<uint32_t>(), ws.pair_c.as<uint32_t>(), ws.pair_slot.as<uint32_t>());
     HORA_LAUNCHED();
   }
-  // 3) LUT + ADC scan + per-pair R best
-  HORA_TRY(v.cand.reserve(sizeof(uint64_t) * nq * pmax * R));
-  HORA_CUDA_TRY(cudaMemsetAsync(v.cand.ptr, 0xff, sizeof(uint64_t) * nq * pmax * R, s));
+  // LUT + ADC scan + per-pair R best
+  HORA_TRY(ws.ivf_cand.reserve(sizeof(uint64_t) * nq * pmax * R));
+  HORA_CUDA_TRY(cudaMemsetAsync(ws.ivf_cand.ptr, 0xff, sizeof(uint64_t) * nq * pmax * R, s));
   const int per = 4;
   switch (v.dmax) {
-    case 1: HORA_TRY(launch_adc<1>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
-    case 2: HORA_TRY(launch_adc<2>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
-    case 4: HORA_TRY(launch_adc<4>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
-    case 8: HORA_TRY(launch_adc<8>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
-    default: HORA_TRY(launch_adc<16>(v, Q, h->ld, h->ld, npairs, per, R, (int)pmax, v.cand.as<uint64_t>(), s)); break;
+    case 1: HORA_TRY(launch_adc<1>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
+    case 2: HORA_TRY(launch_adc<2>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
+    case 4: HORA_TRY(launch_adc<4>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
+    case 8: HORA_TRY(launch_adc<8>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
+    default: HORA_TRY(launch_adc<16>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
   }
-  // 4) per-query merge of the pmax x R candidates (pq_idx.rs:429-436)
-  const int width = (int)(pmax * R);
-  uint64_t *merged = d_best;
-  if (R > k) {
-    HORA_TRY(v.best_r.reserve(sizeof(uint64_t) * nq * R));
-    merged = v.best_r.as<uint64_t>();
-  }
-  HORA_CUDA_TRY(cudaMemsetAsync(merged, 0xff, sizeof(uint64_t) * nq * R, s));
+  // per-query merge of the candidates (pq_idx.rs:429-436)
+  const int width = pmax * R;
   HORA_TRY(ws.ovf_flag.reserve(nq));
   HORA_TRY(ws.ovf_counter.reserve(4));
   if (merge_smem_bytes(R, width) <= 200 * 1024) {
-    HORA_TRY(launch_merge_topk(merged, R, v.cand.as<uint64_t>(), nullptr, width, width, nullptr, nq,
+    HORA_TRY(launch_merge_topk(M, R, ws.ivf_cand.as<uint64_t>(), nullptr, width, width, nullptr, nq,
                                ws.ovf_flag.as<uint8_t>(), ws.ovf_counter.as<uint32_t>(), s));
   } else {
     // merge probe slots in groups that fit one shared-memory sort
     int grp = std::max(1, (16384 - R) / R);
-    for (int64_t j0 = 0; j0 < pmax; j0 += grp) {
+    for (int64_t j0 = jbegin; j0 < pmax; j0 += grp) {
       int gw = (int)(std::min<int64_t>(grp, pmax - j0) * R);
-      // candidates of slots [j0, j0+g) are contiguous per query at offset j0*R
-      HORA_TRY(v.tmp_keys.reserve(sizeof(uint64_t) * nq * gw));
-      HORA_CUDA_TRY(cudaMemcpy2DAsync(v.tmp_keys.ptr, gw * 8, v.cand.as<uint64_t>() + j0 * R, width * 8,
+      HORA_TRY(ws.tmp_keys.reserve(sizeof(uint64_t) * nq * gw));
+      HORA_CUDA_TRY(cudaMemcpy2DAsync(ws.tmp_keys.ptr, gw * 8, ws.ivf_cand.as<uint64_t>() + j0 * R, width * 8,
                                       gw * 8, nq, cudaMemcpyDeviceToDevice, s));
-      HORA_TRY(launch_merge_topk(merged, R, v.tmp_keys.as<uint64_t>(), nullptr, gw, gw, nullptr, nq,
+      HORA_TRY(launch_merge_topk(M, R, ws.tmp_keys.as<uint64_t>(), nullptr, gw, gw, nullptr, nq,
                                  ws.ovf_flag.as<uint8_t>(), ws.ovf_counter.as<uint32_t>(), s));
     }
   }
-  // 5) optional exact rerank
-  if (R > k) {
-    HORA_TRY(v.tmp_keys.reserve(sizeof(uint64_t) * nq * R));
-    if (h->metric == M_COS) HORA_TRY(ensure_norms(h, s));
-    HORA_TRY(launch_rerank_exact(h->metric, Q, h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(),
-                                 h->xnorm.as<float>(), merged, nq, R, v.tmp_keys.as<uint64_t>(), s));
-    HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
-    HORA_TRY(launch_merge_topk(d_best, k, v.tmp_keys.as<uint64_t>(), nullptr, R, R, nullptr, nq,
-                               ws.ovf_flag.as<uint8_t>(), ws.ovf_counter.as<uint32_t>(), s));
-  }
   return HORA_OK;
+}
+
+// k best of M (nq x R ADC keys): an exact FP32 rerank when R > k.
+int ivf_finalize(hora_index *h, int64_t nq, int k, int R, const uint64_t *M, SearchWorkspace &ws,
+                 uint64_t *d_best, cudaStream_t s) {
+  if (R == k) {
+    if (M != d_best)
+      HORA_CUDA_TRY(cudaMemcpyAsync(d_best, M, sizeof(uint64_t) * nq * k, cudaMemcpyDeviceToDevice, s));
+    return HORA_OK;
+  }
+  HORA_TRY(ws.tmp_keys.reserve(sizeof(uint64_t) * nq * R));
+  if (h->metric == M_COS) HORA_TRY(ensure_norms(h, s));
+  HORA_TRY(launch_rerank_exact(h->metric, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim,
+                               ws.qnorm.as<float>(), h->xnorm.as<float>(), M, nq, R,
+                               ws.tmp_keys.as<uint64_t>(), s));
+  HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
+  HORA_TRY(ws.ovf_flag.reserve(nq));
+  HORA_TRY(ws.ovf_counter.reserve(4));
+  HORA_TRY(launch_merge_topk(d_best, k, ws.tmp_keys.as<uint64_t>(), nullptr, R, R, nullptr, nq,
+                             ws.ovf_flag.as<uint8_t>(), ws.ovf_counter.as<uint32_t>(), s));
+  return HORA_OK;
+}
+
+int ivf_rerank_width(const hora_index *h, int k) { return h->ivf_rerank > k ? h->ivf_rerank : k; }
+
+uint64_t *ivf_merge_buffer(SearchWorkspace &ws, int64_t nq, int R, uint64_t *d_best, int k) {
+  if (R == k) return d_best;
+  if (ws.best_r.reserve(sizeof(uint64_t) * nq * R) != HORA_OK) return nullptr;
+  return ws.best_r.as<uint64_t>();
+}
+
+int ivf_search_keys(hora_index *h, int64_t nq, int k, int64_t nprobe, const uint32_t *d_nprobe,
+                    SearchWorkspace &ws, uint64_t *d_best, cudaStream_t s) {
+  if (!h->ivfs) return fail(HORA_ENOTBUILT, "index not built");
+  const int pmax = ivf_pmax(h, nprobe);
+  const int R = ivf_rerank_width(h, k);  // ADC candidates kept per query
+  if (R > 1024) return fail(HORA_ECAP, "IVF-PQ: k (or rerank width) must be <= 1024");
+  if (h->learned_nprobe && h->nprobe && !d_nprobe && nprobe == 0)
+    return ivf_search_learned(h, nq, k, ws, d_best, s);
+  HORA_TRY(ivf_probe(h, nq, pmax, ws, s));
+  uint64_t *M = ivf_merge_buffer(ws, nq, R, d_best, k);
+  if (!M) return fail(HORA_EOOM, "IVF-PQ: merge buffer");
+  HORA_CUDA_TRY(cudaMemsetAsync(M, 0xff, sizeof(uint64_t) * nq * R, s));
+  HORA_TRY(ivf_adc_merge(h, nq, pmax, 0, d_nprobe, R, M, ws, s));
+  return ivf_finalize(h, nq, k, R, M, ws, d_best, s);
 }
 
 int ivf_layout(const hora_index *h, uint64_t *n_list, uint64_t *n_sub, uint64_t *sub_bits,
