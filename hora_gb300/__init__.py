@@ -8,7 +8,7 @@ errors when the library is missing; there is no CPU fallback.
 """
 from ._lib import HoraError, launches, lib  # noqa: F401
 from .index import (NO_ID, BruteForceIndex, BruteForceParams, IVFPQIndex,  # noqa: F401
-                    IVFPQParams, Metric, Node, Option, PQIVFIndex, Precision)
+                    IVFPQParams, Metric, Node, Option, PQIVFIndex, Precision, Server)
 
 __all__ = ["BruteForceIndex", "BruteForceParams", "IVFPQIndex", "PQIVFIndex", "IVFPQParams",
-           "Metric", "Node", "Option", "Precision", "HoraError", "NO_ID", "lib", "launches"]
+           "Metric", "Node", "Option", "Precision", "Server", "HoraError", "NO_ID", "lib", "launches"]

@@ -128,6 +128,17 @@ int bf_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64
   return HORA_OK;
 }
 
+int prepare_for_concurrent_search(hora_index *h) {
+  std::lock_guard<std::mutex> g(h->mu);
+  if (!h->built) return fail(HORA_ENOTBUILT, "index not built");
+  cudaStream_t s = h->stream;
+  if (h->metric == M_COS || h->precision != HORA_PREC_FP32) HORA_TRY(ensure_norms(h, s));
+  if (h->kind == HORA_INDEX_BRUTE_FORCE && h->precision != HORA_PREC_FP32 && h->metric != M_L1)
+    HORA_TRY(lowp_prepare(h, s));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  return HORA_OK;
+}
+
 }  // namespace hora
 
 using namespace hora;
@@ -314,17 +325,14 @@ int hora_rebuild(hora_index *h, int metric) {
   return fail(HORA_ENOTIMPL, "not implement");  // ann_index.rs:69-71
 }
 
-static int search_common(hora_index *h, const float *queries, uint64_t nq, uint64_t k,
-                         uint64_t nprobe, uint64_t *ids_out, float *dist_out, float *vecs_out) {
-  if (!h) return fail(HORA_EINVAL, "null index");
-  if (nq == 0) return HORA_OK;
-  if (!queries || (!ids_out && !dist_out && !vecs_out)) return fail(HORA_EINVAL, "null buffer");
-  if (k == 0) return fail(HORA_EINVAL, "k must be positive");
-  if (k > 4096) return fail(HORA_ECAP, "k must be <= 4096");
-  std::lock_guard<std::mutex> g(h->mu);
-  if (!h->built || h->metric == M_UNKNOWN) return fail(HORA_ENOTBUILT, "unknown method");
-  cudaStream_t s = h->stream;
-  SearchWorkspace &ws = h->ws;
+}  // extern "C"
+
+namespace hora {
+// One search on a given workspace and stream (no handle lock: the index is
+// read-only during searches; the serving slots call this concurrently).
+int search_core(hora_index *h, SearchWorkspace &ws, cudaStream_t s, const float *queries,
+                uint64_t nq, uint64_t k, uint64_t nprobe, uint64_t *ids_out, float *dist_out,
+                float *vecs_out) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -380,6 +388,21 @@ static int search_common(hora_index *h, const float *queries, uint64_t nq, uint6
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return rc;
+}
+}  // namespace hora
+
+extern "C" {
+
+static int search_common(hora_index *h, const float *queries, uint64_t nq, uint64_t k,
+                         uint64_t nprobe, uint64_t *ids_out, float *dist_out, float *vecs_out) {
+  if (!h) return fail(HORA_EINVAL, "null index");
+  if (nq == 0) return HORA_OK;
+  if (!queries || (!ids_out && !dist_out && !vecs_out)) return fail(HORA_EINVAL, "null buffer");
+  if (k == 0) return fail(HORA_EINVAL, "k must be positive");
+  if (k > 4096) return fail(HORA_ECAP, "k must be <= 4096");
+  std::lock_guard<std::mutex> g(h->mu);
+  if (!h->built || h->metric == M_UNKNOWN) return fail(HORA_ENOTBUILT, "unknown method");
+  return search_core(h, h->ws, h->stream, queries, nq, k, nprobe, ids_out, dist_out, vecs_out);
 }
 
 int hora_search(hora_index *h, const float *queries, uint64_t nq, uint64_t k, uint64_t *ids_out,
@@ -442,8 +465,8 @@ int hora_idx_info(const hora_index *h, char *buf, uint64_t cap) {
        "\"CosineSimilarity\":\"-cos(x,q) ascending, 0 for a zero norm\"}";
   s += ",\"device_bytes\":" + std::to_string(h->base.bytes + h->ids.bytes + h->xnorm.bytes +
                                              h->xsq64.bytes + ivf_device_bytes(h));
-  s += ",\"last_search_ms\":" + std::to_string(h->last_ms);
-  s += ",\"last_overflow_rescans\":" + std::to_string(h->last_retries);
+  s += ",\"last_search_ms\":" + std::to_string(h->last_ms.load());
+  s += ",\"last_overflow_rescans\":" + std::to_string(h->last_retries.load());
   if (h->kind == HORA_INDEX_IVFPQ) {
     std::string iv;
     ivf_info(h, iv);

@@ -14,11 +14,12 @@
 // and the k best returned, so every returned distance is exact.  Manhattan
 // has no tensor-core form and always runs exactly on the CUDA cores.
 //
-// Kernel layout: CTA = 10 warps.  Warp 0 issues TMA loads (query tile once,
+// Kernel layout: CTA = 18 warps.  Warp 0 issues TMA loads (query tile once,
 // then a ring of base-row tiles), warp 1 owns TMEM (2 x 256 accumulator
-// columns) and issues tcgen05.mma for each 128 x 256 tile, warps 2-9 drain the
-// accumulators with tcgen05.ld (one query row per TMEM lane, half of the 256
-// columns per warp), form distances and append candidates that beat the
+// columns) and issues tcgen05.mma for each 128 x 256 tile, warps 2-17 drain
+// the accumulators with tcgen05.ld (one query row per TMEM lane, a quarter of
+// the 256 columns per warp; the TMEM buffer is released as soon as it is in
+// registers), form distances and append candidates that beat the
 // query's current R-th key.  Every mbarrier wait is bounded; a CTA that gives
 // up raises an error flag read by the host, waits for its MMAs and frees TMEM.
 #include <cuda_bf16.h>
@@ -35,9 +36,9 @@ namespace hora {
 
 constexpr int kLpBM = 128;           // queries per CTA (TMEM lanes)
 constexpr int kLpBN = 256;           // base rows per tile (accumulator columns)
-constexpr int kLpThreads = 320;      // 10 warps
-constexpr int kLpEpiThreads = 256;   // warps 2..9
-constexpr int kLpTilesPerCta = 8;
+constexpr int kLpThreads = 576;      // 18 warps
+constexpr int kLpEpiThreads = 512;   // warps 2..17
+constexpr int kLpTilesPerCta = 16;
 
 struct LowpState {
   int prec = 0;
@@ -160,7 +161,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
   } else {
     // ---------------- epilogue ----------------
     const int g = warp & 3;           // TMEM lane group this warp may access
-    const int h = (warp - 2) >> 2;    // column half
+    const int h = (warp - 2) >> 2;    // column quarter (64 columns)
     const int m = g * 32 + lane;      // query row in the tile
     const int64_t qrow = q0 + m;
     const int64_t qid = qrow < p.nq ? (p.qmap ? p.qmap[qrow] : qrow) : -1;
@@ -183,40 +184,61 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     }
     for (int t = 0; t < T; ++t) {
       const int b = t & 1, jb = t >> 1;
-      if (!tc::mbar_wait(acc_full + b, jb & 1, abort)) break;
+      const int64_t rt = row0 + (int64_t)t * kLpBN + h * 64;
+      // per-row factors of this warp's 64 columns: one coalesced load per
+      // lane (rows rt+lane, rt+32+lane) before the wait, broadcast by shuffle
+      float xa0 = 0.0f, xa1 = 0.0f, xs0 = 1.0f, xs1 = 1.0f;
+      {
+        const int64_t r0 = rt + lane, r1 = rt + 32 + lane;
+        const float *va = MT == M_L2 ? p.xsq : (MT == M_COS ? p.xnorm : nullptr);
+        if (va) {
+          xa0 = r0 < p.r_end ? __ldg(va + r0) : 0.0f;
+          xa1 = r1 < p.r_end ? __ldg(va + r1) : 0.0f;
+        }
+        if (PREC == HORA_PREC_FP8) {
+          xs0 = r0 < p.r_end ? __ldg(p.xscale + r0) : 0.0f;
+          xs1 = r1 < p.r_end ? __ldg(p.xscale + r1) : 0.0f;
+        }
+      }
+      const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full + b, jb & 1, abort));
+      if (!ok) break;
       tc::fence_after_sync();
-      const int64_t rt = row0 + (int64_t)t * kLpBN + h * 128;
-#pragma unroll 1
-      for (int c = 0; c < 4; ++c) {
-        uint32_t v[32];
-        tc::tmem_ld32(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + h * 128 + c * 32), v);
-        tc::tmem_ld_wait();
-        if (qid < 0) continue;
+      uint32_t v0[32], v1[32];
+      const uint32_t ta = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + h * 64);
+      tc::tmem_ld32(ta, v0);
+      tc::tmem_ld32(ta + 32, v1);
+      tc::tmem_ld_wait();
+      // the accumulator is in registers: hand the TMEM buffer back at once
+      tc::fence_before_sync();
+      tc::mbar_arrive(acc_empty + b);
+      const bool live = qid >= 0;
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
 #pragma unroll
         for (int jj = 0; jj < 32; ++jj) {
-          const int64_t row = rt + c * 32 + jj;
-          if (row >= p.r_end) break;
-          float dot = __uint_as_float(v[jj]);
-          if (PREC == HORA_PREC_FP8) dot *= qs * __ldg(p.xscale + row);
+          const int64_t row = rt + half * 32 + jj;
+          const bool valid = live && row < p.r_end;
+          float dot = __uint_as_float(half ? v1[jj] : v0[jj]);
+          if (PREC == HORA_PREC_FP8) dot *= qs * __shfl_sync(0xffffffffu, half ? xs1 : xs0, jj);
           float d;
           if (MT == M_L2) {
-            d = fmaf(-2.0f, dot, qa + __ldg(p.xsq + row));
+            d = fmaf(-2.0f, dot, qa + __shfl_sync(0xffffffffu, half ? xa1 : xa0, jj));
           } else if (MT == M_IP) {
             d = dot;
           } else {
-            float den = qa * __ldg(p.xnorm + row);
+            float den = qa * __shfl_sync(0xffffffffu, half ? xa1 : xa0, jj);
             d = den == 0.0f ? 0.0f : -dot / den;
           }
           if (MODE == TILE_DENSE) {
-            p.cand[qid * p.cap + (row - p.r_begin)] = make_key(d, (uint32_t)row);
-          } else if (d < tau_d || (d == tau_d && (uint32_t)row < tau_r)) {
-            uint32_t slot = atomicAdd(p.count + qid, 1u);
-            if (slot < (uint32_t)p.cap) p.cand[qid * p.cap + slot] = make_key(d, (uint32_t)row);
+            if (valid) p.cand[qid * p.cap + (row - p.r_begin)] = make_key(d, (uint32_t)row);
+          } else if (valid && d <= tau_d) {
+            if (d < tau_d || (uint32_t)row < tau_r) {
+              uint32_t slot = atomicAdd(p.count + qid, 1u);
+              if (slot < (uint32_t)p.cap) p.cand[qid * p.cap + slot] = make_key(d, (uint32_t)row);
+            }
           }
         }
       }
-      tc::fence_before_sync();
-      tc::mbar_arrive(acc_empty + b);
     }
   }
   tc::fence_before_sync();
@@ -379,6 +401,12 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
   HORA_TRY(make_tmap(&st->tmap_b, st->base.ptr, prec, Dp, h->n, kLpBN));
   h->lowp = std::move(st);
   return HORA_OK;
+}
+
+int lowp_prepare(hora_index *h, cudaStream_t s) {
+  const int64_t kbe = h->precision == HORA_PREC_BF16 ? 64 : 128;
+  if (round_up((int64_t)h->dim, kbe) / kbe > 2) return HORA_OK;  // exact path answers
+  return ensure_lowp(h, h->precision, s);
 }
 
 int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,

@@ -1,6 +1,7 @@
 // index.h — the handle behind hora_index* (shared by the translation units).
 #pragma once
 
+#include <atomic>
 #include <memory>
 #include <mutex>
 
@@ -52,14 +53,20 @@ struct hora_index {
   std::unique_ptr<hora::IvfState, hora::IvfDeleter> ivfs;
   std::unique_ptr<hora::LowpState, hora::LowpDeleter> lowp;
   std::unique_ptr<hora::NprobeModel, hora::NprobeDeleter> nprobe;
-  // last search diagnostics
-  int last_retries = 0;
-  double last_ms = 0.0;
+  // last search diagnostics (written by whichever search finished last)
+  std::atomic<int> last_retries{0};
+  std::atomic<double> last_ms{0.0};
 };
 
 namespace hora {
 
 BaseView base_view(hora_index *h);
+int search_core(hora_index *h, SearchWorkspace &ws, cudaStream_t s, const float *queries,
+                uint64_t nq, uint64_t k, uint64_t nprobe, uint64_t *ids_out, float *dist_out,
+                float *vecs_out);
+// Builds the lazily derived state a search may need (norms, low-precision
+// copy) so that concurrent searches only read the index.
+int prepare_for_concurrent_search(hora_index *h);
 int ensure_norms(hora_index *h, cudaStream_t s);
 // Copies nq x dim queries (host or device) into ws.q with pitch h->ld, checks
 // finiteness and computes f32 norms when the metric needs them.
@@ -73,6 +80,7 @@ int bf_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64
 // Low-precision scoring + FP32 rerank (bf_lowp.cu).
 int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
                      cudaStream_t s);
+int lowp_prepare(hora_index *h, cudaStream_t s);
 
 // IVF-PQ (ivfpq.cu)
 int ivf_build(hora_index *h);

@@ -317,3 +317,55 @@ class IVFPQIndex(_Index):
 
 
 PQIVFIndex = IVFPQIndex
+
+
+class Server:
+    """Continuous-batching request loop over built indexes (hora_server_*).
+
+    submit() queues a request (host buffers; they must stay alive until
+    wait() returns) and returns a ticket; wait() blocks until it finished and
+    returns its latency in ms.  stats() gives completed requests / queries,
+    p50 / p99 latency (ms), peak in-flight requests, peak admitted bytes and
+    rejected requests."""
+
+    def __init__(self, indexes, n_slots: int = 4, hbm_budget_bytes: int = 120 << 30):
+        self._idx = list(indexes)
+        arr = (C.c_void_p * len(self._idx))(*[ix._h for ix in self._idx])
+        self._h = C.c_void_p()
+        check(lib().hora_server_create(arr, len(self._idx), n_slots, hbm_budget_bytes,
+                                       C.byref(self._h)))
+        self._keep = {}
+
+    def submit(self, index_no: int, queries, k: int):
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        ids = np.empty((q.shape[0], k), np.uint64)
+        dist = np.empty((q.shape[0], k), np.float32)
+        t = C.c_uint64()
+        check(lib().hora_server_submit(self._h, index_no, C.c_void_p(q.ctypes.data), q.shape[0], k,
+                                       C.c_void_p(ids.ctypes.data), C.c_void_p(dist.ctypes.data),
+                                       C.byref(t)))
+        self._keep[t.value] = (q, ids, dist)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        lat = C.c_double()
+        rc = lib().hora_server_wait(self._h, ticket, timeout_ms, C.byref(lat))
+        q, ids, dist = self._keep.pop(ticket) if rc != -11 else self._keep[ticket]
+        check(rc)
+        return ids, dist, lat.value
+
+    def stats(self) -> dict:
+        o = (C.c_double * 7)()
+        check(lib().hora_server_stats(self._h, o))
+        keys = ("completed", "queries", "p50_ms", "p99_ms", "max_inflight", "max_admitted_bytes",
+                "rejected")
+        return dict(zip(keys, list(o)))
+
+    def close(self):
+        if self._h:
+            lib().hora_server_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            self.close()

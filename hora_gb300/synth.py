@@ -24,14 +24,15 @@ def normal(n: int, d: int, sigma: float = 10.0, stream: int = 0, seed: int = SEE
     return (rng(stream, seed).standard_normal((n, d), dtype=np.float32) * np.float32(sigma))
 
 
-def mixture_centers(n_centers: int, d: int, seed: int = SEED) -> np.ndarray:
-    return rng(1000, seed).standard_normal((n_centers, d), dtype=np.float32) * np.float32(3.0)
+def mixture_centers(n_centers: int, d: int, seed: int = SEED, spread: float = 3.0) -> np.ndarray:
+    return rng(1000, seed).standard_normal((n_centers, d), dtype=np.float32) * np.float32(spread)
 
 
 def mixture(n: int, d: int, n_centers: int = 1024, stream: int = 1, seed: int = SEED,
-            chunk: int = 1 << 18) -> np.ndarray:
-    """n points of the Gaussian mixture, generated in chunks to bound memory."""
-    c = mixture_centers(n_centers, d, seed)
+            chunk: int = 1 << 18, spread: float = 3.0) -> np.ndarray:
+    """n points of the Gaussian mixture (centres ~ spread * N(0, I)),
+    generated in chunks to bound memory."""
+    c = mixture_centers(n_centers, d, seed, spread)
     g = rng(stream, seed)
     out = np.empty((n, d), np.float32)
     for lo in range(0, n, chunk):
