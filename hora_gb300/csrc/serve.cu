@@ -60,7 +60,7 @@ struct hora_server {
   std::condition_variable cv_work, cv_done;
   std::deque<hora::Request *> queue;
   std::unordered_map<uint64_t, hora::Request *> all;
-  std::vector<hora::Slot> slots;
+  std::vector<std::unique_ptr<hora::Slot>> slots;
   bool stop = false;
   uint64_t next_ticket = 1;
   int device = 0;
@@ -109,7 +109,7 @@ static int ensure_pinned(Slot &sl, size_t nq, size_t dim, size_t kk) {
 
 static void worker(hora_server *sv, int slot_no) {
   cudaSetDevice(sv->device);
-  Slot &sl = sv->slots[slot_no];
+  Slot &sl = *sv->slots[slot_no];
   std::vector<Request *> batch;
   for (;;) {
     batch.clear();
@@ -208,15 +208,15 @@ int hora_server_create(hora_index *const *indexes, uint32_t n_indexes, uint32_t 
   sv->idx.assign(indexes, indexes + n_indexes);
   sv->budget = hbm_budget_bytes ? hbm_budget_bytes : UINT64_MAX;
   cudaGetDevice(&sv->device);
-  sv->slots.resize(n_slots);
+  for (uint32_t i = 0; i < n_slots; ++i) sv->slots.emplace_back(new Slot());
   for (uint32_t i = 0; i < n_slots; ++i) {
-    if (cudaStreamCreateWithFlags(&sv->slots[i].stream, cudaStreamNonBlocking) != cudaSuccess) {
-      for (uint32_t j = 0; j < i; ++j) cudaStreamDestroy(sv->slots[j].stream);
+    if (cudaStreamCreateWithFlags(&sv->slots[i]->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      for (uint32_t j = 0; j < i; ++j) cudaStreamDestroy(sv->slots[j]->stream);
       delete sv;
       return fail(HORA_ECUDA, "cudaStreamCreate failed");
     }
   }
-  for (uint32_t i = 0; i < n_slots; ++i) sv->slots[i].th = std::thread(worker, sv, (int)i);
+  for (uint32_t i = 0; i < n_slots; ++i) sv->slots[i]->th = std::thread(worker, sv, (int)i);
   *out = sv;
   return HORA_OK;
 }
@@ -228,9 +228,10 @@ int hora_server_free(hora_server *sv) {
     sv->stop = true;
   }
   sv->cv_work.notify_all();
-  for (auto &sl : sv->slots)
-    if (sl.th.joinable()) sl.th.join();
-  for (auto &sl : sv->slots) {
+  for (auto &slp : sv->slots)
+    if (slp->th.joinable()) slp->th.join();
+  for (auto &slp : sv->slots) {
+    hora::Slot &sl = *slp;
     cudaStreamSynchronize(sl.stream);
     cudaStreamDestroy(sl.stream);
     if (sl.h_q) cudaFreeHost(sl.h_q);
