@@ -41,12 +41,13 @@ constexpr int kLpEpiThreads = 512;   // warps 2..17
 constexpr int kLpTilesPerCta = 16;
 
 struct LowpState {
-  int prec = 0;
+  int prec = 0, metric = 0;
   int64_t n = 0, Dp = 0;
-  DevBuf base;    // n x Dp (bf16 or e4m3)
-  DevBuf xsq;     // n f32 exact squared norms
-  DevBuf xscale;  // n f32 (e4m3 per-row scale)
-  CUtensorMap tmap_b;
+  DevBuf base;     // n x Dp (bf16 or e4m3); unit rows for BF16 cosine
+  DevBuf xsq;      // n f32 exact squared norms
+  DevBuf xscale;   // n f32 (e4m3 per-row scale)
+  DevBuf normblk;  // BF16 Euclidean: n x 16 bf16, -|x|^2/2 in three parts
+  CUtensorMap tmap_b, tmap_n;
 };
 
 void lowp_state_free(LowpState *p) { delete p; }
@@ -67,17 +68,30 @@ struct LpParams {
   int *err;
 };
 
+// BF16 Euclidean folds the row norm into the MMA: one extra K = 16 step
+// whose A columns are (1, 1, 1, 0...) and whose B columns hold -|x|^2 / 2
+// split into three BF16 parts, so the accumulator is <q,x> - |x|^2/2 and the
+// drain needs one compare per column.  Those 16-column blocks use the
+// unswizzled K-major layout: 8-row x 16-byte core matrices, 128 bytes apart
+// along M/N, the two 8-column halves kNormHalfA / kNormHalfB bytes apart.
+constexpr uint32_t kNormHalfA = kLpBM * 16, kNormHalfB = kLpBN * 16;
+constexpr uint32_t kNormBytesA = 2 * kNormHalfA, kNormBytesB = 2 * kNormHalfB;
+
 template <int PREC, int MT, int MODE>
 __global__ void __launch_bounds__(kLpThreads, 1)
     lowp_tile_kernel(const __grid_constant__ CUtensorMap tmap_a,
-                     const __grid_constant__ CUtensorMap tmap_b, LpParams p) {
+                     const __grid_constant__ CUtensorMap tmap_b,
+                     const __grid_constant__ CUtensorMap tmap_n, LpParams p) {
+  constexpr bool FOLD = PREC == HORA_PREC_BF16 && MT == M_L2;
   extern __shared__ __align__(1024) uint8_t smraw[];
   uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   const int nkb = p.nkb, S = p.stages;
   const uint32_t a_kb_bytes = kLpBM * 128, b_kb_bytes = kLpBN * 128;
+  const uint32_t stage_bytes = nkb * b_kb_bytes + (FOLD ? kNormBytesB : 0);
   uint8_t *sA = sm;
-  uint8_t *sB = sm + nkb * a_kb_bytes;
-  uint64_t *bars = reinterpret_cast<uint64_t *>(sB + S * nkb * b_kb_bytes);
+  uint8_t *sAn = sm + nkb * a_kb_bytes;  // FOLD: the (1,1,1,0...) block
+  uint8_t *sB = sAn + (FOLD ? 4096 : 0);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sB + S * stage_bytes);
   uint64_t *full = bars, *empty = bars + 4, *a_full = bars + 8, *acc_full = bars + 9,
            *acc_empty = bars + 11, *done = bars + 13;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 14);
@@ -103,6 +117,16 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     *abort = 0;
     tc::fence_barrier_init();
   }
+  if (FOLD) {
+    // A-side norm block: row r = (1, 1, 1, 0, 0, 0, 0, 0 | 0 ... 0)
+    uint32_t *w = reinterpret_cast<uint32_t *>(sAn);
+    for (int i = threadIdx.x; i < (int)(kNormBytesA / 4); i += blockDim.x) {
+      const int word = i & 3;  // 4 words per 16-byte row of the first half
+      const bool first_half = i < (int)(kNormHalfA / 4);
+      w[i] = !first_half ? 0u : word == 0 ? 0x3F803F80u : word == 1 ? 0x00003F80u : 0u;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
   if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
   tc::fence_before_sync();
   __syncthreads();
@@ -114,16 +138,23 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     if (tc::elect_one()) {
       tc::prefetch_tmap(&tmap_a);
       tc::prefetch_tmap(&tmap_b);
+      if (FOLD) tc::prefetch_tmap(&tmap_n);
       const int kb_elems = PREC == HORA_PREC_BF16 ? 64 : 128;
       tc::mbar_arrive_expect_tx(a_full, nkb * a_kb_bytes);
       for (int kb = 0; kb < nkb; ++kb) tc::tma_load_2d(sA + kb * a_kb_bytes, &tmap_a, a_full, kb * kb_elems, (int)q0);
       for (int t = 0; t < T; ++t) {
         const int s = t % S, j = t / S;
         if (j > 0 && !tc::mbar_wait(empty + s, (j - 1) & 1, abort)) break;
-        tc::mbar_arrive_expect_tx(full + s, nkb * b_kb_bytes);
+        tc::mbar_arrive_expect_tx(full + s, stage_bytes);
         const int y = (int)(row0 + (int64_t)t * kLpBN);
+        uint8_t *st = sB + (size_t)s * stage_bytes;
         for (int kb = 0; kb < nkb; ++kb)
-          tc::tma_load_2d(sB + (s * nkb + kb) * b_kb_bytes, &tmap_b, full + s, kb * kb_elems, y);
+          tc::tma_load_2d(st + kb * b_kb_bytes, &tmap_b, full + s, kb * kb_elems, y);
+        if (FOLD) {
+          uint8_t *sn = st + nkb * b_kb_bytes;
+          tc::tma_load_2d(sn, &tmap_n, full + s, 0, y);
+          tc::tma_load_2d(sn + kNormHalfB, &tmap_n, full + s, 8, y);
+        }
       }
     }
   } else if (warp == 1) {
@@ -137,9 +168,10 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         if (jb > 0 && !tc::mbar_wait(acc_empty + b, (jb - 1) & 1, abort)) break;
         tc::fence_after_sync();
         const uint32_t d = tmem + (uint32_t)(b * kLpBN);
+        uint8_t *st = sB + (size_t)s * stage_bytes;
         for (int kb = 0; kb < nkb; ++kb) {
           const uint32_t a0 = tc::smem_u32(sA + kb * a_kb_bytes);
-          const uint32_t b0 = tc::smem_u32(sB + (s * nkb + kb) * b_kb_bytes);
+          const uint32_t b0 = tc::smem_u32(st + kb * b_kb_bytes);
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
             const uint64_t ad = tc::sdesc_kmajor_sw128(a0 + kk * 32);
@@ -150,6 +182,11 @@ __global__ void __launch_bounds__(kLpThreads, 1)
             else
               tc::mma_e4m3(d, ad, bd, idesc, acc);
           }
+        }
+        if (FOLD) {
+          const uint64_t ad = tc::sdesc_kmajor_none(tc::smem_u32(sAn), kNormHalfA, 128);
+          const uint64_t bd = tc::sdesc_kmajor_none(tc::smem_u32(st + nkb * b_kb_bytes), kNormHalfB, 128);
+          tc::mma_bf16(d, ad, bd, idesc, 1u);
         }
         tc::mma_commit(empty + s);
         tc::mma_commit(acc_full + b);
@@ -182,9 +219,51 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         tau_r = 0xffffffffu;
       }
     }
+    // BF16: the accumulator already is the distance up to a per-query affine
+    // map (Euclidean: qsq - 2 acc with the norm folded in; DotProduct: acc;
+    // CosineSimilarity on unit rows: -acc), so a column is a candidate only
+    // if sgn*acc >= thr; thr is loosened by a relative 1e-6 so no candidate
+    // is lost to rounding, and the exact key test runs on the rare hits.
+    constexpr bool FAST = PREC == HORA_PREC_BF16;
+    const float sgn = MT == M_IP ? -1.0f : 1.0f;
+    float thr = -__int_as_float(0x7f800000);
+    if (FAST && MODE == TILE_FILTER) {
+      const float slack = 1e-6f * (fabsf(qa) + fabsf(tau_d)) + 1e-30f;
+      thr = MT == M_L2 ? 0.5f * (qa - tau_d) - slack : (MT == M_IP ? -(tau_d + slack) : -tau_d - slack);
+    }
     for (int t = 0; t < T; ++t) {
       const int b = t & 1, jb = t >> 1;
       const int64_t rt = row0 + (int64_t)t * kLpBN + h * 64;
+      if constexpr (FAST) {
+        const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full + b, jb & 1, abort));
+        if (!ok) break;
+        tc::fence_after_sync();
+        uint32_t v[64];
+        const uint32_t ta = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + h * 64);
+        tc::tmem_ld32(ta, *reinterpret_cast<uint32_t(*)[32]>(v));
+        tc::tmem_ld32(ta + 32, *reinterpret_cast<uint32_t(*)[32]>(v + 32));
+        tc::tmem_ld_wait();
+        tc::fence_before_sync();
+        tc::mbar_arrive(acc_empty + b);
+        if (qid < 0) continue;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+          const float acc = __uint_as_float(v[j]);
+          if (MODE == TILE_DENSE || sgn * acc >= thr) {
+            const int64_t row = rt + j;
+            if (row < p.r_end) {
+              const float d = MT == M_L2 ? fmaf(-2.0f, acc, qa) : (MT == M_IP ? acc : -acc);
+              if (MODE == TILE_DENSE) {
+                p.cand[qid * p.cap + (row - p.r_begin)] = make_key(d, (uint32_t)row);
+              } else if (d < tau_d || (d == tau_d && (uint32_t)row < tau_r)) {
+                uint32_t slot = atomicAdd(p.count + qid, 1u);
+                if (slot < (uint32_t)p.cap) p.cand[qid * p.cap + slot] = make_key(d, (uint32_t)row);
+              }
+            }
+          }
+        }
+        continue;
+      }
       // per-row factors of this warp's 64 columns: one coalesced load per
       // lane (rows rt+lane, rt+32+lane) before the wait, broadcast by shuffle
       float xa0 = 0.0f, xa1 = 0.0f, xs0 = 1.0f, xs1 = 1.0f;
@@ -251,12 +330,32 @@ __global__ void __launch_bounds__(kLpThreads, 1)
 }
 
 // ---- conversions -------------------------------------------------------------------
+// sq != nullptr scales row r by 1/sqrt(sq[r]) (unit rows; zero rows stay 0)
 __global__ void to_bf16_kernel(const float *X, int64_t n, int64_t ld, int64_t dim, int64_t Dp,
-                               __nv_bfloat16 *out) {
+                               const double *sq, __nv_bfloat16 *out) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n * Dp) return;
   int64_t r = i / Dp, t = i % Dp;
-  out[i] = __float2bfloat16_rn(t < dim ? X[r * ld + t] : 0.0f);
+  float v = t < dim ? X[r * ld + t] : 0.0f;
+  if (sq) v = sq[r] > 0.0 ? (float)((double)v / sqrt(sq[r])) : 0.0f;
+  out[i] = __float2bfloat16_rn(v);
+}
+
+// -|x|^2 / 2 as h1 + h2 + h3 in BF16 (24 bits, the f32 value), columns 3..15 zero
+__global__ void norm_block_kernel(const double *sq, int64_t n, __nv_bfloat16 *out) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  float v = (float)(-0.5 * sq[r]);
+  __nv_bfloat16 h1 = __float2bfloat16_rn(v);
+  float r1 = v - __bfloat162float(h1);
+  __nv_bfloat16 h2 = __float2bfloat16_rn(r1);
+  float r2 = r1 - __bfloat162float(h2);
+  __nv_bfloat16 h3 = __float2bfloat16_rn(r2);
+  __nv_bfloat16 *o = out + r * 16;
+  o[0] = h1;
+  o[1] = h2;
+  o[2] = h3;
+  for (int i = 3; i < 16; ++i) o[i] = __float2bfloat16_rn(0.0f);
 }
 
 // one warp per row: per-row absmax scale so the row's largest entry maps to 448
@@ -330,14 +429,31 @@ static int make_tmap(CUtensorMap *m, const void *ptr, int prec, int64_t Dp, int6
   return HORA_OK;
 }
 
-static int lp_smem_bytes(int nkb, int stages) {
-  return 1024 + nkb * kLpBM * 128 + stages * nkb * kLpBN * 128 + 16 * 8 + 64;
+// The norm block: rows x 16 bf16 (32-byte rows), box 8 columns x 256 rows,
+// no swizzle (lands as the unswizzled K-major core-matrix layout).
+static int make_tmap_norm(CUtensorMap *m, const void *ptr, int64_t rows) {
+  EncodeTiledFn enc;
+  HORA_TRY(encode_fn(&enc));
+  cuuint64_t dims[2] = {16, (cuuint64_t)std::max<int64_t>(rows, 1)};
+  cuuint64_t strides[1] = {32};
+  cuuint32_t box[2] = {8, (cuuint32_t)kLpBN};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides,
+                   box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(HORA_ECUDA, "cuTensorMapEncodeTiled (norm) failed: " + std::to_string((int)r));
+  return HORA_OK;
+}
+
+static int lp_smem_bytes(int nkb, int stages, bool fold) {
+  return 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) +
+         stages * (nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0)) + 16 * 8 + 64;
 }
 
 template <int PREC, int MT, int MODE>
-static int launch_lp3(const CUtensorMap &ta, const CUtensorMap &tb, const LpParams &p,
-                      cudaStream_t s) {
-  const int smem = lp_smem_bytes(p.nkb, p.stages);
+static int launch_lp3(const CUtensorMap &ta, const CUtensorMap &tb, const CUtensorMap &tn,
+                      const LpParams &p, cudaStream_t s) {
+  const int smem = lp_smem_bytes(p.nkb, p.stages, PREC == HORA_PREC_BF16 && MT == M_L2);
   static int attr = 0;
   if (attr < smem) {
     HORA_CUDA_TRY(cudaFuncSetAttribute(lowp_tile_kernel<PREC, MT, MODE>,
@@ -348,27 +464,28 @@ static int launch_lp3(const CUtensorMap &ta, const CUtensorMap &tb, const LpPara
   dim3 grid((unsigned)ceil_div(p.nq, kLpBM), (unsigned)ceil_div(rows, (int64_t)kLpBN * kLpTilesPerCta));
   if (grid.x == 0 || grid.y == 0) return HORA_OK;
   ProfScope ps(PREC == HORA_PREC_BF16 ? "bf16_tc_scan" : "fp8_tc_scan", s);
-  lowp_tile_kernel<PREC, MT, MODE><<<grid, kLpThreads, smem, s>>>(ta, tb, p);
+  lowp_tile_kernel<PREC, MT, MODE><<<grid, kLpThreads, smem, s>>>(ta, tb, tn, p);
   HORA_LAUNCHED();
   return HORA_OK;
 }
 
 template <int PREC>
 static int launch_lp2(int metric, int mode, const CUtensorMap &ta, const CUtensorMap &tb,
-                      const LpParams &p, cudaStream_t s) {
+                      const CUtensorMap &tn, const LpParams &p, cudaStream_t s) {
   const bool dense = mode == TILE_DENSE;
   switch (metric) {
-    case M_L2: return dense ? launch_lp3<PREC, M_L2, TILE_DENSE>(ta, tb, p, s) : launch_lp3<PREC, M_L2, TILE_FILTER>(ta, tb, p, s);
-    case M_IP: return dense ? launch_lp3<PREC, M_IP, TILE_DENSE>(ta, tb, p, s) : launch_lp3<PREC, M_IP, TILE_FILTER>(ta, tb, p, s);
-    case M_COS: return dense ? launch_lp3<PREC, M_COS, TILE_DENSE>(ta, tb, p, s) : launch_lp3<PREC, M_COS, TILE_FILTER>(ta, tb, p, s);
+    case M_L2: return dense ? launch_lp3<PREC, M_L2, TILE_DENSE>(ta, tb, tn, p, s) : launch_lp3<PREC, M_L2, TILE_FILTER>(ta, tb, tn, p, s);
+    case M_IP: return dense ? launch_lp3<PREC, M_IP, TILE_DENSE>(ta, tb, tn, p, s) : launch_lp3<PREC, M_IP, TILE_FILTER>(ta, tb, tn, p, s);
+    case M_COS: return dense ? launch_lp3<PREC, M_COS, TILE_DENSE>(ta, tb, tn, p, s) : launch_lp3<PREC, M_COS, TILE_FILTER>(ta, tb, tn, p, s);
   }
   return fail(HORA_EMETRIC, "no tensor-core form for this metric");
 }
 
-static int launch_lp(int prec, int metric, int mode, const CUtensorMap &ta, const CUtensorMap &tb,
+static int launch_lp(int prec, int metric, int mode, const CUtensorMap &ta, const LowpState &L,
                      const LpParams &p, cudaStream_t s) {
-  return prec == HORA_PREC_BF16 ? launch_lp2<HORA_PREC_BF16>(metric, mode, ta, tb, p, s)
-                                : launch_lp2<HORA_PREC_FP8>(metric, mode, ta, tb, p, s);
+  const CUtensorMap &tn = L.normblk.ptr ? L.tmap_n : L.tmap_b;  // unused unless BF16 Euclidean
+  return prec == HORA_PREC_BF16 ? launch_lp2<HORA_PREC_BF16>(metric, mode, ta, L.tmap_b, tn, p, s)
+                                : launch_lp2<HORA_PREC_FP8>(metric, mode, ta, L.tmap_b, tn, p, s);
 }
 
 // Low-precision copy of the base (and its exact squared norms / scales),
@@ -376,9 +493,11 @@ static int launch_lp(int prec, int metric, int mode, const CUtensorMap &ta, cons
 static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
   const int64_t kbe = prec == HORA_PREC_BF16 ? 64 : 128;
   const int64_t Dp = round_up((int64_t)h->dim, kbe);
-  if (h->lowp && h->lowp->prec == prec && h->lowp->n == h->n) return HORA_OK;
+  if (h->lowp && h->lowp->prec == prec && h->lowp->n == h->n && h->lowp->metric == h->metric)
+    return HORA_OK;
   std::unique_ptr<LowpState, LowpDeleter> st(new LowpState());
   st->prec = prec;
+  st->metric = h->metric;
   st->n = h->n;
   st->Dp = Dp;
   const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
@@ -387,8 +506,15 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
   {
     ProfScope ps("lowp_convert", s);
     if (prec == HORA_PREC_BF16) {
-      to_bf16_kernel<<<ceil_div(h->n * Dp, 256), 256, 0, s>>>(h->base.as<float>(), h->n, h->ld, h->dim,
-                                                              Dp, st->base.as<__nv_bfloat16>());
+      to_bf16_kernel<<<ceil_div(h->n * Dp, 256), 256, 0, s>>>(
+          h->base.as<float>(), h->n, h->ld, h->dim, Dp,
+          h->metric == M_COS ? h->xsq64.as<double>() : nullptr, st->base.as<__nv_bfloat16>());
+      if (h->metric == M_L2) {
+        HORA_LAUNCHED();
+        HORA_TRY(st->normblk.reserve(std::max<int64_t>(h->n, 1) * 16 * 2));
+        norm_block_kernel<<<ceil_div(h->n, 256), 256, 0, s>>>(h->xsq64.as<double>(), h->n,
+                                                              st->normblk.as<__nv_bfloat16>());
+      }
     } else {
       HORA_TRY(st->xscale.reserve(sizeof(float) * std::max<int64_t>(h->n, 1)));
       to_e4m3_kernel<<<ceil_div(h->n, 8), 256, 0, s>>>(h->base.as<float>(), h->n, h->ld, h->dim, Dp,
@@ -399,6 +525,7 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
     HORA_LAUNCHED();
   }
   HORA_TRY(make_tmap(&st->tmap_b, st->base.ptr, prec, Dp, h->n, kLpBN));
+  if (st->normblk.ptr) HORA_TRY(make_tmap_norm(&st->tmap_n, st->normblk.ptr, h->n));
   h->lowp = std::move(st);
   return HORA_OK;
 }
@@ -444,6 +571,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     ProfScope ps("lowp_convert", s);
     if (prec == HORA_PREC_BF16) {
       to_bf16_kernel<<<ceil_div(nq * Dp, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp,
+                                                            h->metric == M_COS ? qsq64 : nullptr,
                                                             ws.lq.as<__nv_bfloat16>());
     } else {
       HORA_TRY(ws.lqscale.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
@@ -495,7 +623,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   int64_t c0 = std::min<int64_t>(n, std::min<int64_t>(cap, round_up(std::max(2 * R, 1024), kLpBN)));
   p.r_begin = 0;
   p.r_end = c0;
-  HORA_TRY(launch_lp(prec, h->metric, TILE_DENSE, ta, L.tmap_b, p, s));
+  HORA_TRY(launch_lp(prec, h->metric, TILE_DENSE, ta, L, p, s));
   HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, (int)c0, nullptr, nq, flags, ovc, s));
   int64_t done = c0;
   const int64_t max_chunk = (int64_t)60000 * kLpBN * kLpTilesPerCta;
@@ -506,7 +634,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     c = std::min<int64_t>(round_up(c, kLpBN), std::min<int64_t>(n - done, max_chunk));
     p.r_begin = done;
     p.r_end = done + c;
-    HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, ta, L.tmap_b, p, s));
+    HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, ta, L, p, s));
     HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s));
     done += c;
   }
@@ -542,7 +670,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     for (int64_t lo = 0; lo < n; lo += max_chunk) {
       r.r_begin = lo;
       r.r_end = std::min<int64_t>(n, lo + max_chunk);
-      HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, tg, L.tmap_b, r, s));
+      HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, tg, L, r, s));
       HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, ws.qlist.as<int>(), nl, flags, ovc, s));
     }
     HORA_CUDA_TRY(cudaMemcpyAsync(&h_ovc, ovc, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));

@@ -25,6 +25,7 @@
 
 #include "dist_tile.cuh"
 #include "index.h"
+#include "select.cuh"
 
 namespace hora {
 
@@ -488,16 +489,11 @@ __device__ void cta_select_k(const uint32_t *keys, int L, int k, int *sel, uint3
       if ((v & mask) == prefix) atomicAdd(&hist[(v >> shift) & 255u], 1u);
     }
     __syncthreads();
+    if (threadIdx.x < 32) warp_find_digit(hist, (uint32_t)scratch[1], scratch + 2);
+    __syncthreads();
     if (threadIdx.x == 0) {
-      int rem = scratch[1];
-      uint32_t run = 0;
-      int d = 0;
-      for (; d < 256; ++d) {
-        if (run + hist[d] >= (uint32_t)rem) break;
-        run += hist[d];
-      }
-      scratch[1] = rem - (int)run;
-      scratch[3] = d;
+      scratch[1] -= scratch[3];  // keys below the chosen digit
+      scratch[3] = scratch[2];
     }
     __syncthreads();
     prefix |= ((uint32_t)scratch[3]) << shift;

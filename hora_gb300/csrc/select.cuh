@@ -1,0 +1,49 @@
+// select.cuh — CTA-wide radix selection helpers.
+#pragma once
+
+#include "common.cuh"
+
+namespace hora {
+
+// Warp 0 scans a 256-bin histogram: finds the digit d whose cumulative count
+// first reaches `rem` and writes d and the count of keys below d into
+// out[0], out[1].  Lane l owns bins 8l..8l+7.
+__device__ __forceinline__ void warp_find_digit(const uint32_t *hist, uint32_t rem, int *out) {
+  const int lane = threadIdx.x & 31;
+  uint32_t b[8], s = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    b[i] = hist[lane * 8 + i];
+    s += b[i];
+  }
+  uint32_t inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  const uint32_t exc = inc - s;
+  // the lane whose range contains the rem-th key
+  const bool mine = exc < rem && inc >= rem;
+  const unsigned who = __ballot_sync(0xffffffffu, mine);
+  if (mine) {
+    uint32_t run = exc;
+    int d = lane * 8;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (run + b[i] >= rem) {
+        d = lane * 8 + i;
+        break;
+      }
+      run += b[i];
+    }
+    out[0] = d;
+    out[1] = (int)run;
+  }
+  if (who == 0 && lane == 31) {  // rem above the total (callers avoid it): last digit
+    out[0] = 255;
+    out[1] = (int)(inc - b[7]);
+  }
+}
+
+}  // namespace hora

@@ -90,6 +90,17 @@ __device__ __forceinline__ uint64_t sdesc_kmajor_sw128(uint32_t saddr) {
   return d;
 }
 
+// Unswizzled K-major operand: 8-row x 16-byte core matrices; `lbo` bytes
+// between core matrices adjacent along K, `sbo` bytes along M/N.
+__device__ __forceinline__ uint64_t sdesc_kmajor_none(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version; layout 0 = no swizzle
+  return d;
+}
+
 // Instruction descriptor, dense, D = F32, A and B K-major.
 // ab_format: kind::f16 -> 1 = BF16; kind::f8f6f4 -> 0 = E4M3.
 __host__ __device__ constexpr uint32_t idesc_f32acc(uint32_t ab_format, uint32_t M, uint32_t N) {

@@ -10,6 +10,7 @@
 #include <algorithm>
 
 #include "internal.h"
+#include "select.cuh"
 
 namespace hora {
 
@@ -103,6 +104,80 @@ __global__ void __launch_bounds__(kMergeThreads) merge_topk_kernel(
   }
 }
 
+// Merge without duplicates (candidate rows are disjoint from the rows already
+// in the list: chunks and lists never overlap): radix-select the k-th
+// smallest of the c + k keys on 8-bit digits, gather the k winners and sort
+// only those.  Cheaper than sorting all c + k keys when c >> k.
+__global__ void __launch_bounds__(kMergeThreads) merge_select_kernel(
+    uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n,
+    uint8_t *ovf_flag, uint32_t *ovf_counter) {
+  extern __shared__ uint64_t sk[];
+  __shared__ uint32_t hist[256];
+  __shared__ int dig[2];
+  __shared__ int n_sel;
+  const int64_t q = blockIdx.x;
+  uint32_t c = dense_n > 0 ? (uint32_t)dense_n : count[q];
+  if (c == 0) return;
+  const bool ovf = c > (uint32_t)cap;
+  if (ovf) c = cap;
+  const uint64_t *cq = cand + q * cap;
+  uint64_t *bq = best + q * k;
+  // live keys: candidates, then the list's non-empty prefix
+  const int n = (int)c + k;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sk[i] = i < (int)c ? cq[i] : bq[i - c];
+  __syncthreads();
+  // count the non-empty keys (the list may be partially empty)
+  if (threadIdx.x == 0) n_sel = 0;
+  __syncthreads();
+  int live = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) live += sk[i] != kEmptyKey;
+  atomicAdd(&n_sel, live);
+  __syncthreads();
+  const int nl = n_sel;
+  const int want = nl < k ? nl : k;
+  uint64_t *sel = sk + n;  // want keys
+  if (want > 0) {
+    uint64_t prefix = 0, mask = 0;
+    uint32_t rem = (uint32_t)want;
+    for (int shift = 56; shift >= 0; shift -= 8) {
+      for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        uint64_t v = sk[i];
+        if (v != kEmptyKey && (v & mask) == prefix) atomicAdd(&hist[(v >> shift) & 255u], 1u);
+      }
+      __syncthreads();
+      if (threadIdx.x < 32) warp_find_digit(hist, rem, dig);
+      __syncthreads();
+      rem -= (uint32_t)dig[1];
+      prefix |= (uint64_t)dig[0] << shift;
+      mask |= (uint64_t)0xff << shift;
+      __syncthreads();
+    }
+    // keys are distinct, so exactly `want` keys are <= the k-th key
+    if (threadIdx.x == 0) n_sel = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      uint64_t v = sk[i];
+      if (v != kEmptyKey && v <= prefix) sel[atomicAdd(&n_sel, 1)] = v;
+    }
+    __syncthreads();
+    int P = 1;
+    while (P < want) P <<= 1;
+    for (int i = want + threadIdx.x; i < P; i += blockDim.x) sel[i] = kEmptyKey;
+    __syncthreads();
+    block_bitonic_sort(sel, P);
+  }
+  for (int i = threadIdx.x; i < k; i += blockDim.x) bq[i] = i < want ? sel[i] : kEmptyKey;
+  if (threadIdx.x == 0) {
+    if (dense_n <= 0) count[q] = 0;
+    if (ovf) {
+      ovf_flag[q] = 1;
+      atomicAdd(ovf_counter, 1u);
+    }
+  }
+}
+
 int merge_smem_bytes(int k, int cap) {
   int P = 1;
   while (P < k + cap) P <<= 1;
@@ -113,14 +188,29 @@ int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *cou
                       int dense_n, const int *qlist, int64_t nlist, uint8_t *ovf_flag,
                       uint32_t *ovf_counter, cudaStream_t s) {
   if (nlist <= 0) return HORA_OK;
-  int smem = merge_smem_bytes(k, dense_n > 0 ? dense_n : cap);
-  if (smem > 200 * 1024) return fail(HORA_ECAP, "merge: k + candidate capacity too large");
-  static int attr = 0;
-  if (smem > attr) {
+  static bool attr = false;
+  if (!attr) {
     HORA_CUDA_TRY(cudaFuncSetAttribute(merge_topk_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = 200 * 1024;
+    HORA_CUDA_TRY(cudaFuncSetAttribute(merge_select_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
   }
+  const int cmax = dense_n > 0 ? dense_n : cap;
+  if (!qlist) {
+    int P = 1;
+    while (P < k) P <<= 1;
+    const size_t smem = (size_t)(cmax + k + P) * 8;
+    if (smem <= 200 * 1024) {
+      ProfScope ps("topk_merge", s);
+      merge_select_kernel<<<(unsigned)nlist, kMergeThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
+                                                                       ovf_flag, ovf_counter);
+      HORA_LAUNCHED();
+      return HORA_OK;
+    }
+  }
+  int smem = merge_smem_bytes(k, cmax);
+  if (smem > 200 * 1024) return fail(HORA_ECAP, "merge: k + candidate capacity too large");
   ProfScope ps("topk_merge", s);
   merge_topk_kernel<<<(unsigned)nlist, kMergeThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
                                                                 qlist, ovf_flag, ovf_counter);

@@ -34,7 +34,7 @@ def test_mlp_forward_and_gradients_match_oracle(hora, oracle, gpu):
 def _ivf(hora, synth, n=200_000, d=64, lists=256):
     # overlapping clusters: neighbours spread over several lists, so the
     # nprobe a query needs varies (well-separated clusters need one list)
-    X = synth.mixture(n, d, 512, stream=51, spread=0.6)
+    X = synth.mixture(n, d, 512, stream=51, spread=1.2)
     p = hora.IVFPQParams(n_sub=16, sub_bits=8, n_kmeans_center=lists, search_n_center=8,
                          train_epoch=6)
     ix = hora.IVFPQIndex(d, p)
@@ -47,8 +47,8 @@ def _ivf(hora, synth, n=200_000, d=64, lists=256):
 def test_learned_nprobe_trains_and_gains(hora, oracle, gpu):
     from hora_gb300 import synth
     ix, X = _ivf(hora, synth)
-    train = synth.mixture(20_000, 64, 512, stream=52, spread=0.6)
-    held = synth.mixture(2_000, 64, 512, stream=53, spread=0.6)
+    train = synth.mixture(20_000, 64, 512, stream=52, spread=1.2)
+    held = synth.mixture(2_000, 64, 512, stream=53, spread=1.2)
     stats = ix.train_nprobe(train, max_nprobe=64, recall_target=0.9, epochs=20)
     assert np.isfinite(stats[0]) and stats[2] <= 6.0
     # exact neighbours of the held-out queries
@@ -65,7 +65,7 @@ def test_learned_nprobe_trains_and_gains(hora, oracle, gpu):
         ids, _ = ix.search_batch(held, 10, nprobe=npb)
         fixed[npb] = rec(ids)
     ix.set_option(hora.Option.LEARNED_NPROBE, 1)
-    ix.set_option(hora.Option.NPROBE_MARGIN, 0.5)
+    ix.set_option(hora.Option.NPROBE_MARGIN, 1.0)
     ids, d = ix.search_batch(held, 10)
     r_learned = rec(ids)
     pred = ix.predict_nprobe(held)
@@ -81,7 +81,7 @@ def test_learned_nprobe_trains_and_gains(hora, oracle, gpu):
     fixed_at_same_cost = fixed[lo] + w * (fixed[hi] - fixed[lo])
     print("fixed", fixed, "learned", r_learned, "mean probes", mean_probes, "fixed needs", need,
           "fixed at the same cost", fixed_at_same_cost)
-    assert r_learned >= 0.8
+    assert r_learned >= 0.95
     assert mean_probes < need or r_learned > fixed_at_same_cost + 0.002, \
         (mean_probes, need, fixed, r_learned)
     # features are finite and the model's nprobe respects the clamp
