@@ -46,6 +46,12 @@ def args_parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="queries in the CPU baseline sample")
     ap.add_argument("--small", action="store_true", help="tiny workload for a quick check")
     ap.add_argument("--nq", type=int, default=0, help="override the number of queries (profiling)")
+    ap.add_argument("--no-ivf", action="store_true", help="skip the IVF-PQ section")
+    ap.add_argument("--ivf-epochs", type=int, default=25)
+    ap.add_argument("--ivf-train-queries", type=int, default=200_000)
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[20_000.0, 200_000.0])
+    ap.add_argument("--serve-seconds", type=float, default=4.0)
     return ap.parse_args()
 
 
@@ -174,6 +180,126 @@ def cpu_sample_qps(base, q, k, n_sample, threads):
     return n_sample / dt, dt
 
 
+# ---- the reference's CPU-runnable case ---------------------------------------------
+def run_config1(H, rank0: bool):
+    """BruteForceIndex 10,000 x 64, entries Normal(0, 10), 1,000 queries, k = 10,
+    Euclidean, exact FP32 on the GPU; the oracle port on the host beside it,
+    single-threaded one query at a time (as the reference ships) and on all
+    cores."""
+    import torch
+    from hora_gb300 import synth
+    base = synth.normal(10_000, 64, 10.0, stream=11)
+    q = synth.normal(1_000, 64, 10.0, stream=12)
+    ix = H.BruteForceIndex(64)
+    ix.madd(base, None)
+    ix.build(H.Metric.Euclidean)
+    dq = torch.from_numpy(q).cuda()
+    ids = torch.empty((1000, 10), dtype=torch.int64, device="cuda")
+    dd = torch.empty((1000, 10), dtype=torch.float32, device="cuda")
+    ms = []
+    for i in range(13):
+        ix.search_batch(dq, 10, ids_out=ids, dist_out=dd)
+        if i >= 3:
+            ms.append(json.loads(ix.idx_info())["last_search_ms"])
+    out = {"workload": "BruteForceIndex 10kx64 Normal(0,10), 1k queries, k=10, Euclidean, exact FP32",
+           "gpu_qps": 1000 / (np.median(ms) / 1e3), "gpu_ms": float(np.median(ms))}
+    if rank0:
+        from oracle import oracle as O
+        O.build()
+        t0 = time.perf_counter()
+        O.bf_search(base, q[:200], 10, O.EUCLIDEAN, threads=1)
+        out["cpu_single_thread_qps"] = 200 / (time.perf_counter() - t0)
+        th = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        O.bf_search(base, q, 10, O.EUCLIDEAN, threads=th)
+        out["cpu_all_cores_qps"] = 1000 / (time.perf_counter() - t0)
+        out["cpu_cores"] = th
+    return out
+
+
+# ---- IVF-PQ (PQIVFIndex) on the same data ---------------------------------------------
+def run_ivf(a, H, base, q, exact):
+    """1M x 128 mixture, 1,024 lists, 32 x 8-bit PQ trained on the first 500k
+    items, k = 10 with an exact FP32 rerank of 100 ADC candidates; QPS and
+    recall@10 (against the exact brute-force top-10) for nprobe 1..128 and
+    for the learned per-query nprobe trained on separate synthetic queries."""
+    import torch
+    from hora_gb300 import synth
+    n = base.shape[0]
+    params = H.IVFPQParams(n_sub=32, sub_bits=8, n_kmeans_center=1024, search_n_center=16,
+                           train_epoch=a.ivf_epochs)
+    ix = H.IVFPQIndex(DIM, params)
+    ix.set_option(H.Option.TRAIN_SIZE, min(500_000, n))
+    ix.madd(torch.from_numpy(base).cuda(), None)
+    t0 = time.perf_counter()
+    ix.build(H.Metric.Euclidean)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    ix.set_option(H.Option.IVF_RERANK, 100)
+    dq = torch.from_numpy(q).cuda()
+    nq = q.shape[0]
+    ids_d = torch.empty((nq, 10), dtype=torch.int64, device="cuda")
+    dist_d = torch.empty((nq, 10), dtype=torch.float32, device="cuda")
+    ex10 = exact[:, :10] if exact is not None else None
+
+    def timed(nprobe=0, reps=3):
+        ix.search_batch(dq, 10, nprobe=nprobe, ids_out=ids_d, dist_out=dist_d)
+        ms = []
+        for _ in range(reps):
+            ix.search_batch(dq, 10, nprobe=nprobe, ids_out=ids_d, dist_out=dist_d)
+            ms.append(json.loads(ix.idx_info())["last_search_ms"])
+        torch.cuda.synchronize()
+        ids = ids_d.cpu().numpy()
+        rec = recall_at(ids, ex10, 10) if ex10 is not None else None
+        return {"qps": nq / (np.median(ms) / 1e3), "recall@10": rec, "ms": float(np.median(ms))}
+
+    sweep = {p: timed(p) for p in (1, 2, 4, 8, 16, 32, 64, 128)}
+    out = {"workload": "IVFPQIndex 1Mx128 mixture, 1024 lists, 32x8-bit PQ, train 500k, "
+                       f"{a.ivf_epochs} epochs, 10k queries, k=10, exact rerank of 100 ADC candidates",
+           "build_s": build_s, "sweep": {str(k): v for k, v in sweep.items()}}
+    # learned nprobe (trained on queries from the same distribution, disjoint from the bench's)
+    try:
+        tq = synth.mixture(a.ivf_train_queries, DIM, N_CENTERS, stream=7)
+        t0 = time.perf_counter()
+        st = ix.train_nprobe(tq, max_nprobe=128, recall_target=1.0, epochs=20)
+        train_s = time.perf_counter() - t0
+        ix.set_option(H.Option.LEARNED_NPROBE, 1)
+        best = None
+        for margin in (0.5, 1.0):
+            ix.set_option(H.Option.NPROBE_MARGIN, margin)
+            r = timed(0)
+            r["mean_nprobe"] = float(np.maximum(ix.predict_nprobe(q), 4).mean())
+            r["margin"] = margin
+            out.setdefault("learned", []).append(r)
+        ix.set_option(H.Option.LEARNED_NPROBE, 0)
+        out["learned_train"] = {"queries": a.ivf_train_queries, "seconds": train_s, "final_loss": st[0],
+                                "label_mean_log2": st[1]}
+        ok = [v for v in sweep.values() if (v["recall@10"] or 0) >= 0.95]
+        out["fixed_best_at_0.95"] = max(ok, key=lambda v: v["qps"]) if ok else None
+        okl = [v for v in out["learned"] if (v["recall@10"] or 0) >= 0.95]
+        out["learned_best_at_0.95"] = max(okl, key=lambda v: v["qps"]) if okl else None
+    except H.HoraError as e:
+        out["learned_error"] = str(e)
+    return out, ix
+
+
+def run_serving(a, H, indexes, pools):
+    """Open-loop Poisson load on the two built indexes (brute force in its
+    headline form, IVF-PQ with rerank): batch sizes log-uniform 1..256,
+    k in {1, 10, 100}, HBM admission budget 120 GB."""
+    from hora_gb300 import loadgen
+    srv = H.Server(indexes, n_slots=4, hbm_budget_bytes=120 << 30)
+    out = {"workload": "serving mix: Poisson arrivals, batch 1..256 log-uniform, k in {1,10,100}, "
+                       "50/50 brute force 1Mx128 / IVF-PQ 1Mx128, 4 slots, HBM budget 120 GB",
+           "rates": []}
+    try:
+        for rate in a.serve_rates:
+            out["rates"].append(loadgen.run(srv, pools, rate, a.serve_seconds, seed=int(rate)))
+    finally:
+        srv.close()
+    return out
+
+
 # ---- our implementation ------------------------------------------------------------
 def run_ours(a, dist: Dist):
     import torch
@@ -298,6 +424,13 @@ def run_ours(a, dist: Dist):
         roof["traffic"] = None
         roof["share_of_step"] = ms / (t_dev * 1e3)
 
+    config1 = run_config1(H, dist.rank == 0) if not a.small else None
+    ivf, serving = None, None
+    if not a.no_ivf:
+        ivf, ivx = run_ivf(a, H, base, q, exact)
+        if not a.no_serve:
+            serving = run_serving(a, H, [ix, ivx], [q, q])
+
     cpu = None
     if dist.rank == 0:
         ns = min(q.shape[0], a.cpu_sample or (32 if a.small else 2048))
@@ -319,7 +452,8 @@ def run_ours(a, dist: Dist):
                        "parallelism": f"replicas x{dist.world}"},
             "forms": forms, "p50_ms": float(np.percentile(step_ms, 50)),
             "p99_ms": float(np.percentile(step_ms, 99)), "wall_s": t_wall,
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "ivfpq": ivf,
+            "serving": serving, "config1": config1,
             "gpu_launches": launches, "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
         }
         print(json.dumps(line), flush=True)

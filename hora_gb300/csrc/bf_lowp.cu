@@ -14,14 +14,15 @@
 // and the k best returned, so every returned distance is exact.  Manhattan
 // has no tensor-core form and always runs exactly on the CUDA cores.
 //
-// Kernel layout: CTA = 18 warps.  Warp 0 issues TMA loads (query tile once,
-// then a ring of base-row tiles), warp 1 owns TMEM (2 x 256 accumulator
-// columns) and issues tcgen05.mma for each 128 x 256 tile, warps 2-17 drain
-// the accumulators with tcgen05.ld (one query row per TMEM lane, a quarter of
-// the 256 columns per warp; the TMEM buffer is released as soon as it is in
-// registers), form distances and append candidates that beat the
-// query's current R-th key.  Every mbarrier wait is bounded; a CTA that gives
-// up raises an error flag read by the host, waits for its MMAs and frees TMEM.
+// Kernel layout: CTA = 18 warps over 128 queries x 4,096 rows.  Warp 0
+// issues TMA loads (the query tile once, then a 4-8 deep ring of 128-row base
+// tiles), warp 1 owns TMEM (4 accumulator buffers of 128 columns) and issues
+// tcgen05.mma per tile, warps 2-17 drain the accumulators with tcgen05.ld (one
+// query row per TMEM lane, 32 columns per warp; the buffer is released as
+// soon as it is in registers), build a hit mask against the query's current
+// R-th key and hand the rare hits to an out-of-line append.  Every mbarrier
+// wait is bounded; a CTA that gives up raises an error flag read by the host,
+// waits for its MMAs and frees TMEM.
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
 
@@ -35,10 +36,12 @@
 namespace hora {
 
 constexpr int kLpBM = 128;           // queries per CTA (TMEM lanes)
-constexpr int kLpBN = 256;           // base rows per tile (accumulator columns)
+constexpr int kLpBN = 128;           // base rows per tile (accumulator columns)
+constexpr int kLpNB = 4;             // TMEM accumulator buffers (4 x 128 columns)
 constexpr int kLpThreads = 576;      // 18 warps
 constexpr int kLpEpiThreads = 512;   // warps 2..17
-constexpr int kLpTilesPerCta = 16;
+constexpr int kLpTilesPerCta = 32;   // 4,096 rows per CTA
+constexpr int kLpMaxStages = 8;
 
 struct LowpState {
   int prec = 0, metric = 0;
@@ -77,6 +80,36 @@ struct LpParams {
 constexpr uint32_t kNormHalfA = kLpBM * 16, kNormHalfB = kLpBN * 16;
 constexpr uint32_t kNormBytesA = 2 * kNormHalfA, kNormBytesB = 2 * kNormHalfB;
 
+// What the drain needs to test and append the columns that hit.
+struct DrainCtx {
+  uint64_t *cand;
+  uint32_t *count;
+  int64_t qid, rt, r_begin, r_end;
+  int cap;
+  float qa, tau_d;
+  uint32_t tau_r;
+};
+
+// Rare path, kept out of line so the hot loop stays small: vals are raw
+// accumulators (RAW, BF16 forms) or finished distances.
+template <int MT, int MODE, bool RAW>
+__device__ __noinline__ void drain_hits(const float *vals, uint32_t hits, DrainCtx c) {
+  while (hits) {
+    const int j = __ffs(hits) - 1;
+    hits &= hits - 1;
+    const int64_t row = c.rt + j;
+    if (row >= c.r_end) continue;
+    const float a = vals[j];
+    const float d = !RAW ? a : MT == M_L2 ? fmaf(-2.0f, a, c.qa) : (MT == M_IP ? a : -a);
+    if (MODE == TILE_DENSE) {
+      c.cand[c.qid * c.cap + (row - c.r_begin)] = make_key(d, (uint32_t)row);
+    } else if (d < c.tau_d || (d == c.tau_d && (uint32_t)row < c.tau_r)) {
+      uint32_t slot = atomicAdd(c.count + c.qid, 1u);
+      if (slot < (uint32_t)c.cap) c.cand[c.qid * c.cap + slot] = make_key(d, (uint32_t)row);
+    }
+  }
+}
+
 template <int PREC, int MT, int MODE>
 __global__ void __launch_bounds__(kLpThreads, 1)
     lowp_tile_kernel(const __grid_constant__ CUtensorMap tmap_a,
@@ -92,15 +125,15 @@ __global__ void __launch_bounds__(kLpThreads, 1)
   uint8_t *sAn = sm + nkb * a_kb_bytes;  // FOLD: the (1,1,1,0...) block
   uint8_t *sB = sAn + (FOLD ? 4096 : 0);
   uint64_t *bars = reinterpret_cast<uint64_t *>(sB + S * stage_bytes);
-  uint64_t *full = bars, *empty = bars + 4, *a_full = bars + 8, *acc_full = bars + 9,
-           *acc_empty = bars + 11, *done = bars + 13;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 14);
-  volatile int *abort = reinterpret_cast<volatile int *>(bars + 15);
+  uint64_t *full = bars, *empty = bars + kLpMaxStages, *a_full = bars + 2 * kLpMaxStages;
+  uint64_t *acc_full = a_full + 1, *acc_empty = acc_full + kLpNB, *done = acc_empty + kLpNB;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  volatile int *abort = reinterpret_cast<volatile int *>(done + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t q0 = (int64_t)blockIdx.x * kLpBM;
   const int64_t row0 = p.r_begin + (int64_t)blockIdx.y * kLpBN * kLpTilesPerCta;
-  int64_t rows_here = p.r_end - row0;
+  const int64_t rows_here = p.r_end - row0;
   const int T = (int)std::min<int64_t>(kLpTilesPerCta, (rows_here + kLpBN - 1) / kLpBN);
 
   if (threadIdx.x == 0) {
@@ -109,7 +142,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       tc::mbar_init(empty + s, 1);
     }
     tc::mbar_init(a_full, 1);
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kLpNB; ++b) {
       tc::mbar_init(acc_full + b, 1);
       tc::mbar_init(acc_empty + b, kLpEpiThreads);
     }
@@ -127,7 +160,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
+  if (warp == 1) tc::tmem_alloc(tmem_slot, kLpNB * kLpBN);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -163,7 +196,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       constexpr uint32_t idesc = tc::idesc_f32acc(PREC == HORA_PREC_BF16 ? 1u : 0u, kLpBM, kLpBN);
       bool ok = tc::mbar_wait(a_full, 0, abort);
       for (int t = 0; ok && t < T; ++t) {
-        const int s = t % S, j = t / S, b = t & 1, jb = t >> 1;
+        const int s = t % S, j = t / S, b = t % kLpNB, jb = t / kLpNB;
         if (!tc::mbar_wait(full + s, j & 1, abort)) break;
         if (jb > 0 && !tc::mbar_wait(acc_empty + b, (jb - 1) & 1, abort)) break;
         tc::fence_after_sync();
@@ -196,9 +229,9 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       tc::mbar_wait(done, 0, abort, 1u << 20);
     }
   } else {
-    // ---------------- epilogue ----------------
+    // ---------------- drain ----------------
     const int g = warp & 3;           // TMEM lane group this warp may access
-    const int h = (warp - 2) >> 2;    // column quarter (64 columns)
+    const int h = (warp - 2) >> 2;    // column quarter (32 columns)
     const int m = g * 32 + lane;      // query row in the tile
     const int64_t qrow = q0 + m;
     const int64_t qid = qrow < p.nq ? (p.qmap ? p.qmap[qrow] : qrow) : -1;
@@ -208,123 +241,91 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       if (MT == M_COS) qa = p.qnorm[qid];
       if (PREC == HORA_PREC_FP8) qs = p.qscale[qid];
     }
-    float tau_d = -__int_as_float(0x7f800000);
-    uint32_t tau_r = 0;
+    float tau_d = __int_as_float(0x7f800000);
+    uint32_t tau_r = 0xffffffffu;  // fewer than R keys yet: every finite distance passes
     if (MODE == TILE_FILTER && qid >= 0) {
       uint64_t tk = p.best[qid * p.k + (p.k - 1)];
-      tau_d = key_dist(tk);
-      tau_r = key_row(tk);
-      if (tk == kEmptyKey) {  // fewer than R keys yet: every finite distance passes
-        tau_d = __int_as_float(0x7f800000);
-        tau_r = 0xffffffffu;
+      if (tk != kEmptyKey) {
+        tau_d = key_dist(tk);
+        tau_r = key_row(tk);
       }
     }
-    // BF16: the accumulator already is the distance up to a per-query affine
-    // map (Euclidean: qsq - 2 acc with the norm folded in; DotProduct: acc;
-    // CosineSimilarity on unit rows: -acc), so a column is a candidate only
-    // if sgn*acc >= thr; thr is loosened by a relative 1e-6 so no candidate
-    // is lost to rounding, and the exact key test runs on the rare hits.
+    // BF16: the accumulator is the distance up to a per-query affine map
+    // (Euclidean: qsq - 2 acc with the norm folded in; DotProduct: acc;
+    // CosineSimilarity on unit rows: -acc), so a column can only be a
+    // candidate if acc clears thr; thr is loosened by a relative 1e-6 so no
+    // candidate is lost to rounding, and the exact key test runs in the drain.
     constexpr bool FAST = PREC == HORA_PREC_BF16;
-    const float sgn = MT == M_IP ? -1.0f : 1.0f;
-    float thr = -__int_as_float(0x7f800000);
+    float thr = 0.0f;
     if (FAST && MODE == TILE_FILTER) {
       const float slack = 1e-6f * (fabsf(qa) + fabsf(tau_d)) + 1e-30f;
-      thr = MT == M_L2 ? 0.5f * (qa - tau_d) - slack : (MT == M_IP ? -(tau_d + slack) : -tau_d - slack);
+      thr = MT == M_L2 ? 0.5f * (qa - tau_d) - slack : (MT == M_IP ? tau_d + slack : -tau_d - slack);
     }
+    DrainCtx c{p.cand, p.count, qid, 0, p.r_begin, p.r_end, p.cap, qa, tau_d, tau_r};
     for (int t = 0; t < T; ++t) {
-      const int b = t & 1, jb = t >> 1;
-      const int64_t rt = row0 + (int64_t)t * kLpBN + h * 64;
-      if constexpr (FAST) {
-        const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full + b, jb & 1, abort));
-        if (!ok) break;
-        tc::fence_after_sync();
-        uint32_t v[64];
-        const uint32_t ta = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + h * 64);
-        tc::tmem_ld32(ta, *reinterpret_cast<uint32_t(*)[32]>(v));
-        tc::tmem_ld32(ta + 32, *reinterpret_cast<uint32_t(*)[32]>(v + 32));
-        tc::tmem_ld_wait();
-        tc::fence_before_sync();
-        tc::mbar_arrive(acc_empty + b);
-        if (qid < 0) continue;
-#pragma unroll
-        for (int j = 0; j < 64; ++j) {
-          const float acc = __uint_as_float(v[j]);
-          if (MODE == TILE_DENSE || sgn * acc >= thr) {
-            const int64_t row = rt + j;
-            if (row < p.r_end) {
-              const float d = MT == M_L2 ? fmaf(-2.0f, acc, qa) : (MT == M_IP ? acc : -acc);
-              if (MODE == TILE_DENSE) {
-                p.cand[qid * p.cap + (row - p.r_begin)] = make_key(d, (uint32_t)row);
-              } else if (d < tau_d || (d == tau_d && (uint32_t)row < tau_r)) {
-                uint32_t slot = atomicAdd(p.count + qid, 1u);
-                if (slot < (uint32_t)p.cap) p.cand[qid * p.cap + slot] = make_key(d, (uint32_t)row);
-              }
-            }
-          }
-        }
-        continue;
-      }
-      // per-row factors of this warp's 64 columns: one coalesced load per
-      // lane (rows rt+lane, rt+32+lane) before the wait, broadcast by shuffle
-      float xa0 = 0.0f, xa1 = 0.0f, xs0 = 1.0f, xs1 = 1.0f;
-      {
-        const int64_t r0 = rt + lane, r1 = rt + 32 + lane;
+      const int b = t % kLpNB, jb = t / kLpNB;
+      c.rt = row0 + (int64_t)t * kLpBN + h * 32;
+      // generic forms: this lane's row factor, broadcast by shuffle below
+      float xa = 0.0f, xs = 1.0f;
+      if (!FAST) {
+        const int64_t r = c.rt + lane;
         const float *va = MT == M_L2 ? p.xsq : (MT == M_COS ? p.xnorm : nullptr);
-        if (va) {
-          xa0 = r0 < p.r_end ? __ldg(va + r0) : 0.0f;
-          xa1 = r1 < p.r_end ? __ldg(va + r1) : 0.0f;
-        }
-        if (PREC == HORA_PREC_FP8) {
-          xs0 = r0 < p.r_end ? __ldg(p.xscale + r0) : 0.0f;
-          xs1 = r1 < p.r_end ? __ldg(p.xscale + r1) : 0.0f;
-        }
+        if (va) xa = r < p.r_end ? __ldg(va + r) : 0.0f;
+        if (PREC == HORA_PREC_FP8) xs = r < p.r_end ? __ldg(p.xscale + r) : 0.0f;
       }
       const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full + b, jb & 1, abort));
       if (!ok) break;
       tc::fence_after_sync();
-      uint32_t v0[32], v1[32];
-      const uint32_t ta = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + h * 64);
-      tc::tmem_ld32(ta, v0);
-      tc::tmem_ld32(ta + 32, v1);
+      uint32_t v[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + h * 32), v);
       tc::tmem_ld_wait();
       // the accumulator is in registers: hand the TMEM buffer back at once
       tc::fence_before_sync();
       tc::mbar_arrive(acc_empty + b);
-      const bool live = qid >= 0;
+      if (FAST) {
+        uint32_t hits = 0;
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
+        for (int j = 0; j < 32; ++j) {
+          const float a = __uint_as_float(v[j]);
+          const bool hit = MT == M_IP ? a <= thr : a >= thr;
+          hits |= (uint32_t)hit << j;
+        }
+        if (MODE == TILE_DENSE) hits = 0xffffffffu;
+        if (qid >= 0 && hits) {
+          float f[32];  // only on the rare path
 #pragma unroll
-        for (int jj = 0; jj < 32; ++jj) {
-          const int64_t row = rt + half * 32 + jj;
-          const bool valid = live && row < p.r_end;
-          float dot = __uint_as_float(half ? v1[jj] : v0[jj]);
-          if (PREC == HORA_PREC_FP8) dot *= qs * __shfl_sync(0xffffffffu, half ? xs1 : xs0, jj);
-          float d;
+          for (int j = 0; j < 32; ++j) f[j] = __uint_as_float(v[j]);
+          drain_hits<MT, MODE, true>(f, hits, c);
+        }
+        continue;
+      }
+      float f[32];
+      uint32_t hits = 0;
+      {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          float dot = __uint_as_float(v[j]);
+          if (PREC == HORA_PREC_FP8) dot *= qs * __shfl_sync(0xffffffffu, xs, j);
           if (MT == M_L2) {
-            d = fmaf(-2.0f, dot, qa + __shfl_sync(0xffffffffu, half ? xa1 : xa0, jj));
+            f[j] = fmaf(-2.0f, dot, qa + __shfl_sync(0xffffffffu, xa, j));
           } else if (MT == M_IP) {
-            d = dot;
+            f[j] = dot;
           } else {
-            float den = qa * __shfl_sync(0xffffffffu, half ? xa1 : xa0, jj);
-            d = den == 0.0f ? 0.0f : -dot / den;
+            float den = qa * __shfl_sync(0xffffffffu, xa, j);
+            f[j] = den == 0.0f ? 0.0f : -dot / den;
           }
-          if (MODE == TILE_DENSE) {
-            if (valid) p.cand[qid * p.cap + (row - p.r_begin)] = make_key(d, (uint32_t)row);
-          } else if (valid && d <= tau_d) {
-            if (d < tau_d || (uint32_t)row < tau_r) {
-              uint32_t slot = atomicAdd(p.count + qid, 1u);
-              if (slot < (uint32_t)p.cap) p.cand[qid * p.cap + slot] = make_key(d, (uint32_t)row);
-            }
-          }
+          hits |= (uint32_t)(f[j] <= tau_d) << j;
         }
       }
+      if (MODE == TILE_DENSE) hits = 0xffffffffu;
+      if (qid >= 0 && hits) drain_hits<MT, MODE, false>(f, hits, c);
     }
   }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 1) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tmem, 512);
+    tc::tmem_dealloc(tmem, kLpNB * kLpBN);
   }
   if (threadIdx.x == 0 && *abort) atomicExch(p.err, 1);
 }
@@ -447,7 +448,14 @@ static int make_tmap_norm(CUtensorMap *m, const void *ptr, int64_t rows) {
 
 static int lp_smem_bytes(int nkb, int stages, bool fold) {
   return 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) +
-         stages * (nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0)) + 16 * 8 + 64;
+         stages * (nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0)) + 32 * 8;
+}
+
+// Ring depth: as many base tiles as fit in ~200 KB of shared memory.
+static int lp_stages(int nkb, bool fold) {
+  const int fixed = 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) + 32 * 8;
+  const int stage = nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0);
+  return std::max(2, std::min(kLpMaxStages, (200 * 1024 - fixed) / stage));
 }
 
 template <int PREC, int MT, int MODE>
@@ -559,7 +567,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   if (R > 4096) return fail(HORA_ECAP, "rerank width must be <= 4096");
   int cap = std::max(h->cand_cap, 2 * R);
   cap = (int)round_up(cap, 128);
-  const int stages = nkb == 1 ? 4 : 2;
+  const int stages = lp_stages(nkb, prec == HORA_PREC_BF16 && h->metric == M_L2);
   const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
 
   // query copies
