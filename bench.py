@@ -260,20 +260,24 @@ def run_ivf(a, H, base, q, exact):
     # learned nprobe (trained on queries from the same distribution, disjoint from the bench's)
     try:
         tq = synth.mixture(a.ivf_train_queries, DIM, N_CENTERS, stream=7)
-        t0 = time.perf_counter()
-        st = ix.train_nprobe(tq, max_nprobe=128, recall_target=1.0, epochs=20)
-        train_s = time.perf_counter() - t0
-        ix.set_option(H.Option.LEARNED_NPROBE, 1)
-        best = None
-        for margin in (0.5, 1.0):
-            ix.set_option(H.Option.NPROBE_MARGIN, margin)
-            r = timed(0)
-            r["mean_nprobe"] = float(np.maximum(ix.predict_nprobe(q), 4).mean())
-            r["margin"] = margin
-            out.setdefault("learned", []).append(r)
-        ix.set_option(H.Option.LEARNED_NPROBE, 0)
-        out["learned_train"] = {"queries": a.ivf_train_queries, "seconds": train_s, "final_loss": st[0],
-                                "label_mean_log2": st[1]}
+        out["learned_train"] = []
+        for p1 in (4, 1):  # lists probed before the model reads its features
+            ix.set_option(H.Option.NPROBE_PHASE1, p1)
+            t0 = time.perf_counter()
+            st = ix.train_nprobe(tq, max_nprobe=128, recall_target=1.0, epochs=20)
+            train_s = time.perf_counter() - t0
+            ix.set_option(H.Option.LEARNED_NPROBE, 1)
+            for margin in (0.5, 1.0):
+                ix.set_option(H.Option.NPROBE_MARGIN, margin)
+                r = timed(0)
+                r["mean_nprobe"] = float(np.maximum(ix.predict_nprobe(q), p1).mean())
+                r["margin"] = margin
+                r["phase1_probes"] = p1
+                out.setdefault("learned", []).append(r)
+            ix.set_option(H.Option.LEARNED_NPROBE, 0)
+            out["learned_train"].append({"phase1_probes": p1, "queries": a.ivf_train_queries,
+                                         "seconds": train_s, "final_loss": st[0],
+                                         "label_mean_log2": st[1]})
         ok = [v for v in sweep.values() if (v["recall@10"] or 0) >= 0.95]
         out["fixed_best_at_0.95"] = max(ok, key=lambda v: v["qps"]) if ok else None
         okl = [v for v in out["learned"] if (v["recall@10"] or 0) >= 0.95]

@@ -596,6 +596,10 @@ int hora_set_option(hora_index *h, int key, double v) {
     case HORA_OPT_LEARNED_NPROBE: h->learned_nprobe = v != 0; return HORA_OK;
     case HORA_OPT_NPROBE_MARGIN: h->nprobe_margin = v; return HORA_OK;
     case HORA_OPT_NPROBE_MAX: h->nprobe_max = (int)(v < 0 ? 0 : v); return HORA_OK;
+    case HORA_OPT_NPROBE_PHASE1:
+      if (v < 1 || v > 64) return fail(HORA_ECAP, "phase-1 probes must be in [1, 64]");
+      h->nprobe_phase1 = (int)v;
+      return HORA_OK;
     case HORA_OPT_IVF_RERANK:
       if (v < 0 || v > 4096) return fail(HORA_ECAP, "ivf rerank must be in [0, 4096]");
       h->ivf_rerank = (int)v;
@@ -617,6 +621,7 @@ int hora_get_option(const hora_index *h, int key, double *out) {
     case HORA_OPT_NPROBE_MARGIN: *out = h->nprobe_margin; return HORA_OK;
     case HORA_OPT_NPROBE_MAX: *out = h->nprobe_max; return HORA_OK;
     case HORA_OPT_IVF_RERANK: *out = h->ivf_rerank; return HORA_OK;
+    case HORA_OPT_NPROBE_PHASE1: *out = h->nprobe_phase1; return HORA_OK;
   }
   return fail(HORA_EINVAL, "unknown option");
 }

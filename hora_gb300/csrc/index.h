@@ -46,6 +46,7 @@ struct hora_index {
   double nprobe_margin = 0.0;
   int nprobe_max = 0;
   int ivf_rerank = 0;
+  int nprobe_phase1 = 4;
 
   cudaStream_t stream = nullptr;
   std::mutex mu;

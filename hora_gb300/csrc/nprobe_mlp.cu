@@ -37,6 +37,7 @@ struct NprobeModel {
   DevBuf params, mean, inv_std;
   int f = kF, h1 = kH1, h2 = kH2;
   int pmax = 128;
+  int p1 = 4;  // lists probed before the features are read
   double final_loss = 0;
 };
 
@@ -307,7 +308,7 @@ static int learned_nprobe_per_query(hora_index *h, int64_t nq, int R, uint64_t *
   NprobeModel &md = *h->nprobe;
   // phase 1: the 4 nearest lists
   HORA_TRY(np_q.reserve(sizeof(uint32_t) * std::max<int64_t>(nq, 1)));
-  const int p1 = std::min(4, pw);
+  const int p1 = std::min(md.p1, pw);
   fill_u32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(np_q.as<uint32_t>(), nq, (uint32_t)p1);
   HORA_LAUNCHED();
   HORA_CUDA_TRY(cudaMemsetAsync(M, 0xff, sizeof(uint64_t) * nq * R, s));
@@ -345,7 +346,7 @@ int ivf_search_learned(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, ui
   DevBuf &npq = ws.npq;
   HORA_TRY(learned_nprobe_per_query(h, nq, R, M, ws, pw, npq, s));
   // phase 2: the remaining lists of each query
-  HORA_TRY(ivf_adc_merge(h, nq, pw, 4, npq.as<uint32_t>(), R, M, ws, s));
+  HORA_TRY(ivf_adc_merge(h, nq, pw, h->nprobe->p1, npq.as<uint32_t>(), R, M, ws, s));
   return ivf_finalize(h, nq, k, R, M, ws, d_best, s);
 }
 
@@ -417,7 +418,8 @@ int hora_ivfpq_nprobe_features(hora_index *h, const float *queries, uint64_t nq,
   HORA_TRY(M.reserve(8 * nq * R));
   HORA_TRY(npq.reserve(4 * nq));
   HORA_TRY(F.reserve(4 * nq * kF));
-  fill_u32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(npq.as<uint32_t>(), nq, (uint32_t)std::min(4, pw));
+  fill_u32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(npq.as<uint32_t>(), nq,
+                                                    (uint32_t)std::min(h->nprobe ? h->nprobe->p1 : h->nprobe_phase1, pw));
   HORA_LAUNCHED();
   HORA_CUDA_TRY(cudaMemsetAsync(M.ptr, 0xff, 8 * nq * R, s));
   HORA_TRY(ivf_adc_merge(h, (int64_t)nq, pw, 0, npq.as<uint32_t>(), R, M.as<uint64_t>(), ws, s));
@@ -462,6 +464,7 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
   const int pm = (int)std::min<uint64_t>(std::max<uint64_t>(max_nprobe, 1), (uint64_t)C);
   const int pw = std::min(C, std::max(32, pm));
   const int kk = 10;
+  const int p1 = h->nprobe_phase1;
   const int R = ivf_rerank_width(h, kk);
   std::vector<int> grid;
   for (int p = 1; p < pm; p *= 2) grid.push_back(p);
@@ -505,7 +508,7 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
     }
     // features after the first 4 probes
     HORA_TRY(ivf_probe(h, nq, pw, ws, s));
-    fill_u32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(npq.as<uint32_t>(), nq, (uint32_t)std::min(4, pw));
+    fill_u32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(npq.as<uint32_t>(), nq, (uint32_t)std::min(p1, pw));
     HORA_LAUNCHED();
     HORA_CUDA_TRY(cudaMemsetAsync(M.ptr, 0xff, 8 * nq * R, s));
     HORA_TRY(ivf_adc_merge(h, nq, pw, 0, npq.as<uint32_t>(), R, M.as<uint64_t>(), ws, s));
@@ -594,6 +597,7 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
   for (float v : l) loss += v;
   loss /= N;
   md->pmax = pm;
+  md->p1 = p1;
   md->final_loss = loss;
   h->nprobe = std::move(md);
   if (stats_out) {

@@ -50,6 +50,7 @@ class Option(enum.IntEnum):
     NPROBE_MARGIN = 8
     NPROBE_MAX = 9
     IVF_RERANK = 10
+    NPROBE_PHASE1 = 11
 
 
 @dataclass

@@ -110,8 +110,10 @@ typedef enum {
   HORA_OPT_LEARNED_NPROBE = 7, /* IVF-PQ: use the trained nprobe model (0/1) */
   HORA_OPT_NPROBE_MARGIN = 8,  /* learned nprobe: additive margin in log2 units */
   HORA_OPT_NPROBE_MAX = 9,     /* learned nprobe: upper clamp */
-  HORA_OPT_IVF_RERANK = 10     /* IVF-PQ: exact FP32 rerank of this many ADC
+  HORA_OPT_IVF_RERANK = 10,    /* IVF-PQ: exact FP32 rerank of this many ADC
                                   candidates (0 = off, reference behaviour) */
+  HORA_OPT_NPROBE_PHASE1 = 11  /* learned nprobe: lists probed before the model
+                                  reads its features (default 4; fixed at training) */
 } hora_option;
 
 typedef struct hora_index hora_index;
