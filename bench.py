@@ -52,6 +52,8 @@ def args_parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[20_000.0, 200_000.0])
     ap.add_argument("--serve-seconds", type=float, default=4.0)
+    ap.add_argument("--serve-ivf-n", type=int, default=10_000_000,
+                    help="rows of the serving mix's PQIVF index (96 dims)")
     return ap.parse_args()
 
 
@@ -287,18 +289,47 @@ def run_ivf(a, H, base, q, exact):
     return out, ix
 
 
-def run_serving(a, H, indexes, pools):
-    """Open-loop Poisson load on the two built indexes (brute force in its
-    headline form, IVF-PQ with rerank): batch sizes log-uniform 1..256,
-    k in {1, 10, 100}, HBM admission budget 120 GB."""
+def build_serving_ivf(a, H):
+    """The serving mix's second index: PQIVFIndex over an N x 96 mixture
+    (N = 10M by default, drawn on the device), 4,096 lists, 24 x 8-bit PQ,
+    trained on the first 2M items; nprobe 16, exact rerank of 100."""
+    import torch
+    from hora_gb300 import synth
+    n = a.serve_ivf_n
+    X = synth.mixture_device(n, 96, 1024, stream=5)
+    pool = synth.mixture_device(8192, 96, 1024, stream=6).cpu().numpy()
+    params = H.IVFPQParams(n_sub=24, sub_bits=8, n_kmeans_center=4096, search_n_center=16,
+                           train_epoch=a.ivf_epochs)
+    ix = H.PQIVFIndex(96, params)
+    ix.set_option(H.Option.TRAIN_SIZE, min(2_000_000, n))
+    ix.madd(X, None)
+    del X
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ix.build(H.Metric.Euclidean)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    ix.set_option(H.Option.IVF_RERANK, 100)
+    return ix, pool, {"n": n, "dim": 96, "lists": 4096, "pq": "24 x 8-bit", "train": min(2_000_000, n),
+                      "epochs": a.ivf_epochs, "nprobe": 16, "rerank": 100, "build_s": build_s}
+
+
+def run_serving(a, H, bf_index, bf_pool):
+    """Open-loop Poisson load on two indexes: the 1M x 128 brute force in its
+    headline form and a 10M x 96 PQIVFIndex (4,096 lists, 24 x 256 PQ);
+    batch sizes log-uniform 1..256, k in {1, 10, 100}, HBM admission budget
+    120 GB."""
     from hora_gb300 import loadgen
-    srv = H.Server(indexes, n_slots=4, hbm_budget_bytes=120 << 30)
-    out = {"workload": "serving mix: Poisson arrivals, batch 1..256 log-uniform, k in {1,10,100}, "
-                       "50/50 brute force 1Mx128 / IVF-PQ 1Mx128, 4 slots, HBM budget 120 GB",
-           "rates": []}
+    ivx, ivf_pool, ivf_desc = build_serving_ivf(a, H)
+    srv = H.Server([bf_index, ivx], n_slots=4, hbm_budget_bytes=120 << 30)
+    out = {"workload": f"serving mix: Poisson arrivals, batch 1..256 log-uniform, k in {{1,10,100}}, "
+                       f"50/50 brute force 1Mx128 / PQIVF {ivf_desc['n'] // 1_000_000}Mx96 "
+                       f"(4096 lists, 24x256 PQ), 4 slots, HBM budget 120 GB",
+           "ivf_index": ivf_desc, "rates": []}
     try:
         for rate in a.serve_rates:
-            out["rates"].append(loadgen.run(srv, pools, rate, a.serve_seconds, seed=int(rate)))
+            out["rates"].append(loadgen.run(srv, [bf_pool, ivf_pool], rate, a.serve_seconds,
+                                            seed=int(rate)))
     finally:
         srv.close()
     return out
@@ -433,7 +464,8 @@ def run_ours(a, dist: Dist):
     if not a.no_ivf:
         ivf, ivx = run_ivf(a, H, base, q, exact)
         if not a.no_serve:
-            serving = run_serving(a, H, [ix, ivx], [q, q])
+            del ivx
+            serving = run_serving(a, H, ix, q)
 
     cpu = None
     if dist.rank == 0:

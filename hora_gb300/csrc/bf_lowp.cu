@@ -90,19 +90,23 @@ struct DrainCtx {
   uint32_t tau_r;
 };
 
-// Rare path, kept out of line so the hot loop stays small: `a` is a raw
-// accumulator (RAW, BF16 forms) or a finished distance; scalars only, so
-// nothing of the hot loop goes through local memory.
+// Rare path, kept out of line so the hot loop stays small: vals are raw
+// accumulators (RAW, BF16 forms) or finished distances.
 template <int MT, int MODE, bool RAW>
-__device__ __noinline__ void drain_one(float a, int j, const DrainCtx &c) {
-  const int64_t row = c.rt + j;
-  if (row >= c.r_end) return;
-  const float d = !RAW ? a : MT == M_L2 ? fmaf(-2.0f, a, c.qa) : (MT == M_IP ? a : -a);
-  if (MODE == TILE_DENSE) {
-    c.cand[c.qid * c.cap + (row - c.r_begin)] = make_key(d, (uint32_t)row);
-  } else if (d < c.tau_d || (d == c.tau_d && (uint32_t)row < c.tau_r)) {
-    uint32_t slot = atomicAdd(c.count + c.qid, 1u);
-    if (slot < (uint32_t)c.cap) c.cand[c.qid * c.cap + slot] = make_key(d, (uint32_t)row);
+__device__ __noinline__ void drain_hits(const float *vals, uint32_t hits, DrainCtx c) {
+  while (hits) {
+    const int j = __ffs(hits) - 1;
+    hits &= hits - 1;
+    const int64_t row = c.rt + j;
+    if (row >= c.r_end) continue;
+    const float a = vals[j];
+    const float d = !RAW ? a : MT == M_L2 ? fmaf(-2.0f, a, c.qa) : (MT == M_IP ? a : -a);
+    if (MODE == TILE_DENSE) {
+      c.cand[c.qid * c.cap + (row - c.r_begin)] = make_key(d, (uint32_t)row);
+    } else if (d < c.tau_d || (d == c.tau_d && (uint32_t)row < c.tau_r)) {
+      uint32_t slot = atomicAdd(c.count + c.qid, 1u);
+      if (slot < (uint32_t)c.cap) c.cand[c.qid * c.cap + slot] = make_key(d, (uint32_t)row);
+    }
   }
 }
 
@@ -279,31 +283,42 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       tc::fence_before_sync();
       tc::mbar_arrive(acc_empty + b);
       if (FAST) {
-        if (qid < 0) continue;
+        uint32_t hits = 0;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const float a = __uint_as_float(v[j]);
-          const bool hit = MODE == TILE_DENSE || (MT == M_IP ? a <= thr : a >= thr);
-          if (hit) drain_one<MT, MODE, true>(a, j, c);
+          const bool hit = MT == M_IP ? a <= thr : a >= thr;
+          hits |= (uint32_t)hit << j;
+        }
+        if (MODE == TILE_DENSE) hits = 0xffffffffu;
+        if (qid >= 0 && hits) {
+          float f[32];  // only on the rare path
+#pragma unroll
+          for (int j = 0; j < 32; ++j) f[j] = __uint_as_float(v[j]);
+          drain_hits<MT, MODE, true>(f, hits, c);
         }
         continue;
       }
-      // shuffles need every lane; the append is predicated per lane
+      float f[32];
+      uint32_t hits = 0;
+      {
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        float dot = __uint_as_float(v[j]);
-        if (PREC == HORA_PREC_FP8) dot *= qs * __shfl_sync(0xffffffffu, xs, j);
-        float d;
-        if (MT == M_L2) {
-          d = fmaf(-2.0f, dot, qa + __shfl_sync(0xffffffffu, xa, j));
-        } else if (MT == M_IP) {
-          d = dot;
-        } else {
-          float den = qa * __shfl_sync(0xffffffffu, xa, j);
-          d = den == 0.0f ? 0.0f : -dot / den;
+        for (int j = 0; j < 32; ++j) {
+          float dot = __uint_as_float(v[j]);
+          if (PREC == HORA_PREC_FP8) dot *= qs * __shfl_sync(0xffffffffu, xs, j);
+          if (MT == M_L2) {
+            f[j] = fmaf(-2.0f, dot, qa + __shfl_sync(0xffffffffu, xa, j));
+          } else if (MT == M_IP) {
+            f[j] = dot;
+          } else {
+            float den = qa * __shfl_sync(0xffffffffu, xa, j);
+            f[j] = den == 0.0f ? 0.0f : -dot / den;
+          }
+          hits |= (uint32_t)(f[j] <= tau_d) << j;
         }
-        if (qid >= 0 && (MODE == TILE_DENSE || d <= tau_d)) drain_one<MT, MODE, false>(d, j, c);
       }
+      if (MODE == TILE_DENSE) hits = 0xffffffffu;
+      if (qid >= 0 && hits) drain_hits<MT, MODE, false>(f, hits, c);
     }
   }
   tc::fence_before_sync();

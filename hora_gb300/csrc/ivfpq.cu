@@ -57,9 +57,45 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
 __host__ __device__ __forceinline__ uint64_t instance_seed(uint64_t seed, uint64_t inst) {
   return mix64(seed ^ mix64(inst * 0xD1B54A32D192ED03ull + 0x9E3779B97F4A7C15ull));
 }
-__device__ __forceinline__ double rng_unit(uint64_t &s) {
-  s += 0x9E3779B97F4A7C15ull;
-  return (double)(mix64(s) >> 11) * (1.0 / 9007199254740992.0);
+constexpr uint64_t kRngStep = 0x9E3779B97F4A7C15ull;
+
+// The probability walk of Kmeans::split_center (kmeans.rs:150-193) for one
+// empty centre, evaluated by one warp 32 candidates at a time.  The
+// sequential walk visits centres start, start+1, ... (mod C); a centre with
+// a non-zero count takes the next draw u (53 bits) of the splitmix64 stream
+// and is picked when u / 2^53 < count / batch, tested exactly as
+// u * batch < count * 2^53.  Draw number t uses state s + t * kRngStep, so
+// lane l computes its own draw from the number of non-zero centres before
+// it in the window; the pick and the stream position after it are those of
+// the sequential walk.  All 32 lanes call it; returns -1 after max_windows.
+template <typename CountT>
+__device__ int split_pick_warp(const CountT *counts, int C, int start, uint64_t batch,
+                               uint64_t &s, int64_t max_windows) {
+  const int lane = threadIdx.x & 31;
+  int base = start;
+  for (int64_t w = 0; w < max_windows; ++w) {
+    const int cand = (base + lane) % C;
+    const uint64_t cnt = (uint64_t)counts[cand];
+    const bool nz = cnt > 0;
+    const unsigned nzb = __ballot_sync(0xffffffffu, nz);
+    bool acc = false;
+    if (nz) {
+      const unsigned before = __popc(nzb & ((1u << lane) - 1u));
+      const uint64_t u = mix64(s + (uint64_t)(before + 1) * kRngStep) >> 11;
+      const uint64_t lo = u * batch, hi = __umul64hi(u, batch);
+      const uint64_t rhi = cnt >> 11, rlo = cnt << 53;
+      acc = hi < rhi || (hi == rhi && lo < rlo);
+    }
+    const unsigned ab = __ballot_sync(0xffffffffu, acc);
+    if (ab) {
+      const int first = __ffs(ab) - 1;
+      s += (uint64_t)__popc(nzb & (0xffffffffu >> (31 - first))) * kRngStep;
+      return (base + first) % C;
+    }
+    s += (uint64_t)__popc(nzb) * kRngStep;
+    base = (base + 32) % C;
+  }
+  return -1;
 }
 
 // ---------------------------------------------------------------------------
@@ -197,29 +233,26 @@ __global__ void center_sum_kernel(const float *X, int64_t ld, const uint32_t *me
   centers[(int64_t)c * ld + j] = out;
 }
 
-// Kmeans::split_center (kmeans.rs:150-193), sequential like the reference.
-// A draw at pick_percent == 0 can never accept, so none is taken there (the
-// oracle does the same).  The walk is bounded; status 1 = gave up.
+// Kmeans::split_center (kmeans.rs:150-193): the empty centres in index
+// order, each picking its source with split_pick_warp.  One warp; the walk
+// is bounded, status 1 = gave up.
 __global__ void split_kernel(float *centers, int64_t ld, int64_t dim, int64_t *counts, int C,
                              int64_t batch, uint64_t *rng_state, int *status) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (threadIdx.x >= 32 || blockIdx.x != 0) return;
+  const int lane = threadIdx.x;
   uint64_t s = *rng_state;
   const float lo = 1.0f - 1.0f / 1024.0f, hi = 1.0f + 1.0f / 1024.0f;
   for (int i = 0; i < C; ++i) {
-    if (counts[i] != 0) continue;
-    int sc = (i + 1) % C;
-    int64_t guard = 0;
-    for (;;) {
-      double p = (double)counts[sc] / (double)batch;
-      if (p > 0.0 && rng_unit(s) < p) break;
-      sc = (sc + 1) % C;
-      if (++guard > ((int64_t)1 << 26)) {
+    if (counts[i] != 0) continue;  // uniform: every lane reads the same count
+    const int sc = split_pick_warp(counts, C, (i + 1) % C, (uint64_t)batch, s, (int64_t)1 << 21);
+    if (sc < 0) {
+      if (lane == 0) {
         *status = 1;
         *rng_state = s;
-        return;
       }
+      return;
     }
-    for (int64_t j = 0; j < dim; ++j) {
+    for (int64_t j = lane; j < dim; j += 32) {
       float v = centers[(int64_t)sc * ld + j];
       if (j % 2 == 0) {
         centers[(int64_t)i * ld + j] = __fmul_rn(v, lo);
@@ -229,10 +262,15 @@ __global__ void split_kernel(float *centers, int64_t ld, int64_t dim, int64_t *c
         centers[(int64_t)sc * ld + j] = __fmul_rn(v, lo);
       }
     }
-    counts[i] = counts[sc] / 2;
-    counts[sc] -= counts[i];
+    __syncwarp();
+    if (lane == 0) {
+      const int64_t half = counts[sc] / 2;
+      counts[i] = half;
+      counts[sc] -= half;
+    }
+    __syncwarp();
   }
-  *rng_state = s;
+  if (lane == 0) *rng_state = s;
 }
 
 // ---------------------------------------------------------------------------
@@ -364,38 +402,42 @@ __global__ void __launch_bounds__(256) pq_kmeans_kernel(
       for (int u = 0; u < DM; ++u) cent[j * DM + u] = out[u];
     }
     __syncthreads();
-    if (ep < epochs - 1 && threadIdx.x == 0) {
+    if (ep < epochs - 1 && threadIdx.x < 32) {
+      // split_center by warp 0 (split_pick_warp); lane 0 owns the counts
+      const int lane = threadIdx.x;
       const float lo_ = 1.0f - 1.0f / 1024.0f, hi_ = 1.0f + 1.0f / 1024.0f;
-      for (int i = 0; i < K; ++i) {
-        if (cnt[i] != 0) continue;
-        int sc = (i + 1) % K;
-        int64_t guard = 0;
-        bool gave_up = false;
-        for (;;) {
-          double p = (double)cnt[sc] / (double)n;
-          if (p > 0.0 && rng_unit(rng) < p) break;
-          sc = (sc + 1) % K;
-          if (++guard > ((int64_t)1 << 24)) {
-            gave_up = true;
+      for (int i0 = 0; i0 < K; i0 += 32) {
+        // empty centres of this window in index order; a split only ever
+        // empties the centre being filled, so the set ahead stays valid
+        unsigned empty = __ballot_sync(0xffffffffu, i0 + lane < K && cnt[i0 + lane] == 0);
+        while (empty) {
+          const int i = i0 + __ffs(empty) - 1;
+          empty &= empty - 1;
+          const int sc = split_pick_warp(cnt, K, (i + 1) % K, (uint64_t)n, rng, (int64_t)1 << 19);
+          if (sc < 0) {
+            if (lane == 0) atomicExch(status, 1);
+            i0 = K;
             break;
           }
-        }
-        if (gave_up) {
-          atomicExch(status, 1);
-          break;
-        }
-        for (int u = 0; u < len; ++u) {
-          float v = cent[sc * DM + u];
-          if (u % 2 == 0) {
-            cent[i * DM + u] = __fmul_rn(v, lo_);
-            cent[sc * DM + u] = __fmul_rn(v, hi_);
-          } else {
-            cent[i * DM + u] = __fmul_rn(v, hi_);
-            cent[sc * DM + u] = __fmul_rn(v, lo_);
+          if (lane < len) {
+            const int u = lane;
+            float v = cent[sc * DM + u];
+            if (u % 2 == 0) {
+              cent[i * DM + u] = __fmul_rn(v, lo_);
+              cent[sc * DM + u] = __fmul_rn(v, hi_);
+            } else {
+              cent[i * DM + u] = __fmul_rn(v, hi_);
+              cent[sc * DM + u] = __fmul_rn(v, lo_);
+            }
           }
+          __syncwarp();
+          if (lane == 0) {
+            const int64_t half = cnt[sc] / 2;
+            cnt[i] = half;
+            cnt[sc] -= half;
+          }
+          __syncwarp();
         }
-        cnt[i] = cnt[sc] / 2;
-        cnt[sc] -= cnt[i];
       }
     }
     __syncthreads();
@@ -469,82 +511,215 @@ __global__ void pair_scatter_kernel(const uint64_t *probes, int64_t nq, int pmax
   pslot[pos] = (uint32_t)j;
 }
 
-// CTA-wide selection of the k smallest of L 32-bit order keys held in smem
-// (radix select on 8-bit digits; ties at the k-th key go to the lowest
-// positions).  sel receives k positions (unordered).  L, k uniform.
+// CTA-wide selection of the k smallest of L 32-bit order keys held in smem:
+// radix select on 11/11/10-bit digits whose histogram updates are
+// aggregated per warp (one shared atomic per distinct digit and warp
+// instruction, so keys crowded into one digit do not serialise); ties at the
+// k-th key go to the lowest positions.  sel receives the k positions
+// (unordered).  L and k are uniform, 0 < k < L.  hist: kSelBins u32, zero on
+// entry and on return; scratch: 48 ints.
+constexpr int kSelBins = 2048;
+
+// Warp 0: the bin whose cumulative count first reaches rem among nbins
+// (32 times a power of two); out[0] = bin, out[1] = keys below it.  Lane l owns bins
+// [l*nb, l*nb+nb) and sums them in a rotated order (conflict-free banks).
+__device__ __forceinline__ void warp_find_bin(const uint32_t *hist, int nbins, uint32_t rem,
+                                              int *out) {
+  const int lane = threadIdx.x & 31, nb = nbins >> 5;  // nb: a power of two
+  uint32_t s = 0;
+#pragma unroll 8
+  for (int i = 0; i < nb; ++i) s += hist[lane * nb + ((i + lane) & (nb - 1))];
+  uint32_t inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  const uint32_t exc = inc - s;
+  const bool mine = exc < rem && inc >= rem;
+  if (mine) {
+    uint32_t run = exc;
+    int d = lane * nb + nb - 1;
+    for (int i = 0; i < nb; ++i) {
+      const uint32_t b = hist[lane * nb + i];
+      if (run + b >= rem) {
+        d = lane * nb + i;
+        break;
+      }
+      run += b;
+    }
+    out[0] = d;
+    out[1] = (int)run;
+  }
+}
+
 __device__ void cta_select_k(const uint32_t *keys, int L, int k, int *sel, uint32_t *hist,
                              int *scratch) {
-  // scratch: [0] prefix bits, [1] remaining k, [2] count below, [3] digit, [4..] scan
+  // scratch: [0] remaining k, [1] digit, [2] below, [3] taken, [5] count at the k-th key,
+  // [8..8+nwarps) scan
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) {
-    scratch[0] = 0;
-    scratch[1] = k;
+    scratch[0] = k;
+    scratch[3] = 0;
   }
   __syncthreads();
   uint32_t prefix = 0, mask = 0;
-  for (int shift = 24; shift >= 0; shift -= 8) {
-    for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
-    __syncthreads();
-    for (int i = threadIdx.x; i < L; i += blockDim.x) {
-      uint32_t v = keys[i];
-      if ((v & mask) == prefix) atomicAdd(&hist[(v >> shift) & 255u], 1u);
+  for (int pass = 0; pass < 3; ++pass) {
+    const int shift = pass == 0 ? 21 : pass == 1 ? 10 : 0;
+    const uint32_t dmask = pass == 2 ? 1023u : 2047u;
+    for (int i0 = 0; i0 < L; i0 += blockDim.x) {
+      const int i = i0 + threadIdx.x;
+      const uint32_t v = i < L ? keys[i] : 0u;
+      const bool p = i < L && (v & mask) == prefix;
+      const unsigned pm = __ballot_sync(0xffffffffu, p);
+      if (p) {
+        const uint32_t dig = (v >> shift) & dmask;
+        const unsigned peers = __match_any_sync(pm, dig);
+        if (lane == __ffs(peers) - 1) atomicAdd(&hist[dig], (uint32_t)__popc(peers));
+      }
     }
     __syncthreads();
-    if (threadIdx.x < 32) warp_find_digit(hist, (uint32_t)scratch[1], scratch + 2);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      scratch[1] -= scratch[3];  // keys below the chosen digit
-      scratch[3] = scratch[2];
+    if (warp == 0) {
+      warp_find_bin(hist, (int)dmask + 1, (uint32_t)scratch[0], scratch + 1);
+      __syncwarp();
+      const int d = scratch[1];
+      const uint32_t at_d = hist[d];
+      const int below = scratch[2];
+      __syncwarp();
+      for (int b = lane; b <= (int)dmask; b += 32) hist[b] = 0;
+      if (lane == 0) {
+        scratch[0] -= below;
+        scratch[5] = (int)at_d;
+      }
     }
     __syncthreads();
-    prefix |= ((uint32_t)scratch[3]) << shift;
-    mask |= 255u << shift;
-    __syncthreads();
+    prefix |= (uint32_t)scratch[1] << shift;
+    mask |= dmask << shift;
   }
   const uint32_t kth = prefix;
-  const int need_eq = scratch[1];  // how many keys equal to kth are taken
-  // positions of keys < kth (any order) and the first need_eq keys == kth
-  __shared__ int n_lt, n_eq;
-  if (threadIdx.x == 0) {
-    n_lt = 0;
-    n_eq = 0;
+  const int need_eq = scratch[0];  // keys equal to kth that are taken (>= 1)
+  const bool all_eq = scratch[5] == need_eq;
+  // keys below kth (and, when every key equal to kth is taken, those too)
+  for (int i0 = 0; i0 < L; i0 += blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    const uint32_t v = i < L ? keys[i] : 0xffffffffu;
+    const bool p = i < L && (v < kth || (all_eq && v == kth));
+    const unsigned pm = __ballot_sync(0xffffffffu, p);
+    if (pm) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(&scratch[3], __popc(pm));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (p) sel[base + __popc(pm & ((1u << lane) - 1u))] = i;
+    }
+  }
+  if (all_eq) {
+    __syncthreads();
+    return;
   }
   __syncthreads();
-  // keys < kth
-  for (int i = threadIdx.x; i < L; i += blockDim.x)
-    if (keys[i] < kth) sel[atomicAdd(&n_lt, 1)] = i;
-  __syncthreads();
-  const int base_lt = n_lt;
-  // keys == kth in position order: chunked block scan
-  for (int c0 = 0; c0 < L; c0 += blockDim.x) {
-    int i = c0 + threadIdx.x;
-    int f = (i < L && keys[i] == kth) ? 1 : 0;
-    unsigned b = __ballot_sync(0xffffffffu, f);
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) scratch[4 + w] = __popc(b);
+  const int base_lt = scratch[3];
+  // keys equal to kth in position order: chunked block scan
+  int run = 0;
+  const int nw = blockDim.x >> 5;
+  for (int i0 = 0; i0 < L && run < need_eq; i0 += blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    const bool f = i < L && keys[i] == kth;
+    const unsigned b = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) scratch[8 + warp] = __popc(b);
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int run = n_eq;
-      for (int x = 0; x < (int)(blockDim.x >> 5); ++x) {
-        int v = scratch[4 + x];
-        scratch[4 + x] = run;
-        run += v;
-      }
-      n_eq = run;
-    }
-    __syncthreads();
+    int before = run;
+    for (int x = 0; x < warp; ++x) before += scratch[8 + x];
+    int total = 0;
+    for (int x = 0; x < nw; ++x) total += scratch[8 + x];
     if (f) {
-      int r = scratch[4 + w] + __popc(b & ((1u << lane) - 1u));
+      const int r = before + __popc(b & ((1u << lane) - 1u));
       if (r < need_eq) sel[base_lt + r] = i;
     }
+    run += total;
     __syncthreads();
   }
 }
 
 constexpr int kAdcThreads = 256;
-constexpr int kAdcChunk = 4096;
+constexpr int kAdcChunk = 2048;
 
-// One CTA handles `per` consecutive (query, list) pairs (sorted by list).
+// The sum over subspaces of LUT[m][code[m]] in subspace order (pq_idx.rs
+// 180-186), with the code row read VB bytes at a time (VB divides M and the
+// row pitch, so every load is aligned); KC = K when it is a compile-time 256.
+template <int VB, int KC>
+__device__ __forceinline__ float adc_row(const uint8_t *code, const float *lut, int M, int Kr) {
+  const int K = KC ? KC : Kr;  // a constant K folds the table offsets into the loads
+  float d = 0.0f;
+  if (VB == 16) {
+    const uint4 *p = reinterpret_cast<const uint4 *>(code);
+    for (int g = 0; g < M / 16; ++g) {
+      const uint4 w = __ldg(p + g);
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        const uint32_t wt = t < 4 ? w.x : t < 8 ? w.y : t < 12 ? w.z : w.w;
+        d = __fadd_rn(d, lut[(g * 16 + t) * K + ((wt >> (8 * (t & 3))) & 255u)]);
+      }
+    }
+  } else if (VB == 8) {
+    const uint2 *p = reinterpret_cast<const uint2 *>(code);
+    for (int g = 0; g < M / 8; ++g) {
+      const uint2 w = __ldg(p + g);
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const uint32_t wt = t < 4 ? w.x : w.y;
+        d = __fadd_rn(d, lut[(g * 8 + t) * K + ((wt >> (8 * (t & 3))) & 255u)]);
+      }
+    }
+  } else if (VB == 4) {
+    const uint32_t *p = reinterpret_cast<const uint32_t *>(code);
+    for (int g = 0; g < M / 4; ++g) {
+      const uint32_t w = __ldg(p + g);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) d = __fadd_rn(d, lut[(g * 4 + t) * K + ((w >> (8 * t)) & 255u)]);
+    }
+  } else {
+    for (int m = 0; m < M; ++m) d = __fadd_rn(d, lut[m * K + __ldg(code + m)]);
+  }
+  return d;
+}
+
+// LUT[m][j] = sum_t (z_t - C[m][j][t])^2 in t order (pq_idx.rs:170-179); the
+// DM floats of a codeword are one aligned vector load.
 template <int DM>
+__device__ __forceinline__ float lut_entry(const float *cj, const float *zq, int len) {
+  float c[DM];
+  if (DM % 4 == 0) {
+#pragma unroll
+    for (int u = 0; u < DM; u += 4) {
+      const float4 t = __ldg(reinterpret_cast<const float4 *>(cj + u));
+      c[u] = t.x;
+      c[u + 1] = t.y;
+      c[u + 2] = t.z;
+      c[u + 3] = t.w;
+    }
+  } else if (DM == 2) {
+    const float2 t = __ldg(reinterpret_cast<const float2 *>(cj));
+    c[0] = t.x;
+    c[DM - 1] = t.y;
+  } else {
+#pragma unroll
+    for (int u = 0; u < DM; ++u) c[u] = __ldg(cj + u);
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int u = 0; u < DM; ++u) {
+    if (u < len) {
+      const float t = __fsub_rn(zq[u], c[u]);
+      s = __fadd_rn(s, __fmul_rn(t, t));
+    }
+  }
+  return s;
+}
+
+// One CTA handles `per` consecutive (query, list) pairs (sorted by list):
+// LUT, ADC scan of the list in chunks, and the pair's kk best (distance,
+// row) keys -> cand[(q * pmax + slot) * kk ...].
+template <int DM, int VB>
 __global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
     const float *Q, int64_t ldq, const float *centers, int64_t ldc, const float *books,
     const uint8_t *codes, const uint32_t *items, const int64_t *offs, const uint8_t *trained,
@@ -552,12 +727,20 @@ __global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
     int K, const int *sb, const int *sl, int kk, int pmax, uint64_t *cand) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float *lut = reinterpret_cast<float *>(smraw);                       // M x K
-  uint32_t *dkeys = reinterpret_cast<uint32_t *>(lut + M * K);         // kAdcChunk + kk
-  int *sel = reinterpret_cast<int *>(dkeys + kAdcChunk + 1024);        // kk
-  uint32_t *hist = reinterpret_cast<uint32_t *>(sel + 1024);           // 256
-  int *scratch = reinterpret_cast<int *>(hist + 256);                  // 4 + 32
-  uint32_t *rows = reinterpret_cast<uint32_t *>(scratch + 40);         // kAdcChunk + kk (row ids)
-  __shared__ float zq[1024];
+  uint32_t *hist = reinterpret_cast<uint32_t *>(lut + M * K);          // kSelBins
+  uint32_t *dkeys = hist + kSelBins;                                   // kAdcChunk + kk
+  uint32_t *rows = dkeys + kAdcChunk + kk;                             // kAdcChunk + kk
+  int *sel = reinterpret_cast<int *>(rows + kAdcChunk + kk);           // kk
+  int *scratch = sel + kk;                                             // 48
+  int *sbs = scratch + 48;                                             // M subspace starts
+  int *sls = sbs + M;                                                  // M subspace lengths
+  __shared__ __align__(16) float zq[1024];
+  for (int b = threadIdx.x; b < kSelBins; b += blockDim.x) hist[b] = 0;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    sbs[m] = sb[m];
+    sls[m] = sl[m];
+  }
+  const int kbits = 31 - __clz(K);  // K = 2^sub_bits
   for (int64_t pi = (int64_t)blockIdx.x * per; pi < min(npairs, (int64_t)(blockIdx.x + 1) * per); ++pi) {
     const int64_t q = pq[pi];
     const int c = (int)pc[pi];
@@ -566,39 +749,28 @@ __global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
     const int64_t lo = offs[c], L = offs[c + 1] - lo;
     if (!trained[c] || L == 0) {
       for (int r = threadIdx.x; r < kk; r += blockDim.x) out[r] = kEmptyKey;
-      __syncthreads();
       continue;
     }
     // z = q - c_list over the covered dimensions (pq_idx.rs:158-161)
-    int dcov = sb[M - 1] + sl[M - 1];
+    const int dcov = sb[M - 1] + sl[M - 1];
+    __syncthreads();  // the previous pair is done with zq and the LUT
     for (int t = threadIdx.x; t < dcov; t += blockDim.x)
       zq[t] = __fsub_rn(Q[q * ldq + t], centers[(int64_t)c * ldc + t]);
     __syncthreads();
-    // LUT[m][j] = sum_t (z_t - C[m][j][t])^2 (pq_idx.rs:170-179)
     const float *book = books + (int64_t)c * M * K * DM;
     for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
-      int m = e / K;
-      const float *cj = book + (int64_t)e * DM;
-      const int b = sb[m], len = sl[m];
-      float s = 0.0f;
-#pragma unroll
-      for (int u = 0; u < DM; ++u) {
-        if (u < len) {
-          float t = __fsub_rn(zq[b + u], cj[u]);
-          s = __fadd_rn(s, __fmul_rn(t, t));
-        }
-      }
-      lut[e] = s;
+      const int m = e >> kbits;
+      lut[e] = lut_entry<DM>(book + (int64_t)e * DM, zq + sbs[m], sls[m]);
     }
     __syncthreads();
-    // scan in chunks; running k best kept at the head of dkeys/rows
+    // scan in chunks; running kk best kept at the head of dkeys/rows
     int held = 0;
-    for (int64_t c0 = 0; c0 < L; c0 += kAdcChunk - kk) {
-      const int ch = (int)((int64_t)(kAdcChunk - kk) < L - c0 ? (int64_t)(kAdcChunk - kk) : L - c0);
+    const uint8_t *lcodes = codes + lo * M;
+    for (int64_t c0 = 0; c0 < L; c0 += kAdcChunk) {
+      const int ch = (int)(kAdcChunk < L - c0 ? (int64_t)kAdcChunk : L - c0);
       for (int i = threadIdx.x; i < ch; i += blockDim.x) {
-        const uint8_t *code = codes + (lo + c0 + i) * M;
-        float d = 0.0f;
-        for (int m = 0; m < M; ++m) d = __fadd_rn(d, lut[m * K + code[m]]);
+        const float d = K == 256 ? adc_row<VB, 256>(lcodes + (c0 + i) * M, lut, M, K)
+                                 : adc_row<VB, 0>(lcodes + (c0 + i) * M, lut, M, K);
         dkeys[held + i] = f2ord(d);
         rows[held + i] = items[lo + c0 + i];
       }
@@ -606,32 +778,34 @@ __global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
       const int tot = held + ch;
       if (tot <= kk) {
         held = tot;
-        __syncthreads();
         continue;
       }
       cta_select_k(dkeys, tot, kk, sel, hist, scratch);
-      __syncthreads();
       // gather the selection to the head (through registers: sel is unordered)
+      static_assert(kAdcThreads * 4 >= 1024, "kk <= 1024 is held in 4 registers a thread");
       uint32_t kv[4], rv[4];
-      int nmine = 0;
-      for (int r = threadIdx.x; r < kk; r += blockDim.x) {
-        kv[nmine] = dkeys[sel[r]];
-        rv[nmine] = rows[sel[r]];
-        ++nmine;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int r = threadIdx.x + t * kAdcThreads;
+        if (r < kk) {
+          kv[t] = dkeys[sel[r]];
+          rv[t] = rows[sel[r]];
+        }
       }
       __syncthreads();
-      nmine = 0;
-      for (int r = threadIdx.x; r < kk; r += blockDim.x) {
-        dkeys[r] = kv[nmine];
-        rows[r] = rv[nmine];
-        ++nmine;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int r = threadIdx.x + t * kAdcThreads;
+        if (r < kk) {
+          dkeys[r] = kv[t];
+          rows[r] = rv[t];
+        }
       }
       held = kk;
       __syncthreads();
     }
     for (int r = threadIdx.x; r < kk; r += blockDim.x)
       out[r] = r < held ? (((uint64_t)dkeys[r] << 32) | rows[r]) : kEmptyKey;
-    __syncthreads();
   }
 }
 
@@ -850,7 +1024,7 @@ int ivf_build(hora_index *h) {
     }
     if (ep < epochs - 1) {
       ProfScope ps("coarse_split", s);
-      split_kernel<<<1, 1, 0, s>>>(v.centers.as<float>(), h->ld, h->dim, cnt.as<int64_t>(), C, T,
+      split_kernel<<<1, 32, 0, s>>>(v.centers.as<float>(), h->ld, h->dim, cnt.as<int64_t>(), C, T,
                                    d_rng, d_status);
       HORA_LAUNCHED();
     }
@@ -960,23 +1134,35 @@ int ivf_set_codebooks(hora_index *h, const float *centers, const float *codebook
   return HORA_OK;
 }
 
-template <int DM>
-static int launch_adc(IvfState &v, SearchWorkspace &ws, const float *Q, int64_t ldq, int64_t ldc,
-                      int64_t npairs, int per, int kk, int pmax, uint64_t *cand, cudaStream_t s) {
-  size_t smem = sizeof(float) * v.n_sub * v.K + sizeof(uint32_t) * (kAdcChunk + 1024) +
-                sizeof(int) * 1024 + 256 * 4 + 40 * 4 + sizeof(uint32_t) * (kAdcChunk + 1024);
+template <int DM, int VB>
+static int launch_adc_vb(IvfState &v, SearchWorkspace &ws, const float *Q, int64_t ldq, int64_t ldc,
+                         int64_t npairs, int per, int kk, int pmax, uint64_t *cand, cudaStream_t s) {
+  // LUT, histogram, keys + rows of a chunk and the carried kk, selection, scratch
+  size_t smem = sizeof(float) * v.n_sub * v.K + sizeof(uint32_t) * kSelBins +
+                2 * sizeof(uint32_t) * (kAdcChunk + kk) + sizeof(int) * kk + sizeof(int) * 48 +
+                2 * sizeof(int) * v.n_sub;
   if (smem > 200 * 1024) return fail(HORA_ECAP, "IVF-PQ: LUT too large for shared memory");
-  HORA_CUDA_TRY(cudaFuncSetAttribute(adc_scan_kernel<DM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  HORA_CUDA_TRY(cudaFuncSetAttribute(adc_scan_kernel<DM, VB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   unsigned grid = (unsigned)ceil_div(npairs, per);
   if (grid == 0) return HORA_OK;
   ProfScope ps("adc_scan", s);
-  adc_scan_kernel<DM><<<grid, kAdcThreads, smem, s>>>(
+  adc_scan_kernel<DM, VB><<<grid, kAdcThreads, smem, s>>>(
       Q, ldq, v.centers.as<float>(), ldc, v.books.as<float>(), v.codes.as<uint8_t>(),
       v.items.as<uint32_t>(), v.offsets.as<int64_t>(), v.trained.as<uint8_t>(), ws.pair_q.as<uint32_t>(),
       ws.pair_c.as<uint32_t>(), ws.pair_slot.as<uint32_t>(), npairs, per, (int)v.n_sub, (int)v.K,
       v.sub_begin_d.as<int>(), v.sub_len_d.as<int>(), kk, pmax, cand);
   HORA_LAUNCHED();
   return HORA_OK;
+}
+
+// Code rows are n_sub bytes apart: the widest load that divides n_sub.
+template <int DM>
+static int launch_adc(IvfState &v, SearchWorkspace &ws, const float *Q, int64_t ldq, int64_t ldc,
+                      int64_t npairs, int per, int kk, int pmax, uint64_t *cand, cudaStream_t s) {
+  if (v.n_sub % 16 == 0) return launch_adc_vb<DM, 16>(v, ws, Q, ldq, ldc, npairs, per, kk, pmax, cand, s);
+  if (v.n_sub % 8 == 0) return launch_adc_vb<DM, 8>(v, ws, Q, ldq, ldc, npairs, per, kk, pmax, cand, s);
+  if (v.n_sub % 4 == 0) return launch_adc_vb<DM, 4>(v, ws, Q, ldq, ldc, npairs, per, kk, pmax, cand, s);
+  return launch_adc_vb<DM, 1>(v, ws, Q, ldq, ldc, npairs, per, kk, pmax, cand, s);
 }
 
 int ivf_pmax(const hora_index *h, int64_t nprobe) {

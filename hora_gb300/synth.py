@@ -41,3 +41,23 @@ def mixture(n: int, d: int, n_centers: int = 1024, stream: int = 1, seed: int = 
         out[lo:hi] = c[u]
         out[lo:hi] += g.standard_normal((hi - lo, d), dtype=np.float32)
     return out
+
+
+def mixture_device(n: int, d: int, n_centers: int = 1024, stream: int = 1, seed: int = SEED,
+                   spread: float = 3.0, device: str = "cuda", chunk: int = 1 << 20):
+    """The same mixture law drawn by torch on the device (for index sizes
+    too large to draw on the host quickly).  Seeded, but not the numbers
+    mixture() draws: centres come from stream 1000 of the seed, points from
+    `stream`, so calls with different streams share the centres."""
+    import torch
+    gc = torch.Generator(device=device)
+    gc.manual_seed((seed * 1_000_003 + 1000) & 0x7FFFFFFFFFFFFFFF)
+    c = torch.randn((n_centers, d), generator=gc, device=device) * spread
+    g = torch.Generator(device=device)
+    g.manual_seed((seed * 1_000_003 + stream) & 0x7FFFFFFFFFFFFFFF)
+    out = torch.empty((n, d), dtype=torch.float32, device=device)
+    for lo in range(0, n, chunk):
+        hi = min(n, lo + chunk)
+        u = torch.randint(0, n_centers, (hi - lo,), generator=g, device=device)
+        out[lo:hi] = c[u] + torch.randn((hi - lo, d), generator=g, device=device)
+    return out

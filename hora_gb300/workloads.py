@@ -1,6 +1,7 @@
 """The benchmark configurations as runnable workloads (for profiling runs).
 
     python -m hora_gb300.workloads ivfpq [--queries N] [--epochs E] [--nprobe P]
+                                         [--n ROWS] [--lists C]
     python -m hora_gb300.workloads bf [--queries N] [--precision fp32|bf16|fp8]
 
 ivfpq: IVFPQIndex over the 1M x 128 Gaussian mixture, 1,024 lists, 32 x
@@ -17,15 +18,17 @@ import time
 import numpy as np
 
 
-def ivfpq(queries: int = 1024, epochs: int = 25, nprobe: int = 16, n: int = 1_000_000):
+def ivfpq(queries: int = 1024, epochs: int = 25, nprobe: int = 16, n: int = 1_000_000,
+          lists: int = 1024):
     import torch
 
     import hora_gb300 as H
     from hora_gb300 import synth
     X = synth.mixture(n, 128, 1024, stream=1)
     q = synth.mixture(queries, 128, 1024, stream=2)
-    ix = H.IVFPQIndex(128, H.IVFPQParams(n_sub=32, sub_bits=8, n_kmeans_center=1024,
-                                         search_n_center=nprobe, train_epoch=epochs))
+    ix = H.IVFPQIndex(128, H.IVFPQParams(n_sub=32, sub_bits=8,
+                                         n_kmeans_center=lists, search_n_center=nprobe,
+                                         train_epoch=epochs))
     ix.set_option(H.Option.TRAIN_SIZE, min(500_000, n))
     ix.madd(torch.from_numpy(X).cuda(), None)
     t0 = time.perf_counter()
@@ -58,9 +61,11 @@ def main():
     ap.add_argument("--epochs", type=int, default=25)
     ap.add_argument("--nprobe", type=int, default=16)
     ap.add_argument("--precision", default="bf16")
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--lists", type=int, default=1024)
     a = ap.parse_args()
     if a.workload == "ivfpq":
-        print(json.dumps(ivfpq(a.queries, a.epochs, a.nprobe)))
+        print(json.dumps(ivfpq(a.queries, a.epochs, a.nprobe, a.n, a.lists)))
     else:
         print(json.dumps(bf(a.queries, a.precision)))
 

@@ -463,9 +463,16 @@ int horo_kmeans_split(float *centers, int64_t *counts, int64_t n_center, int64_t
     int64_t s = (i + 1) % n_center;
     int64_t guard = 0;
     for (;;) {
-      double p = (double)counts[s] / (double)batch_size;
-      /* a draw at p == 0 can never accept; both builds skip it */
-      if (p > 0.0 && horo_rng_unit(rng_state) < p) break;
+      /* accept with probability p = counts[s] / batch_size: the draw u is a
+       * 53-bit integer and u / 2^53 < counts / batch is tested exactly as
+       * u * batch < counts * 2^53 (128-bit).  A draw at p == 0 can never
+       * accept; both builds skip it. */
+      if (counts[s] > 0) {
+        uint64_t u = horo_rng_next(rng_state) >> 11;
+        unsigned __int128 lhs = (unsigned __int128)u * (uint64_t)batch_size;
+        unsigned __int128 rhs = (unsigned __int128)(uint64_t)counts[s] << 53;
+        if (lhs < rhs) break;
+      }
       s = (s + 1) % n_center;
       if (++guard > (int64_t)1 << 40) return -2;
     }
