@@ -90,23 +90,59 @@ struct DrainCtx {
   uint32_t tau_r;
 };
 
-// Rare path, kept out of line so the hot loop stays small: vals are raw
-// accumulators (RAW, BF16 forms) or finished distances.
+// v[j] for a lane-dependent j without local memory: a 5-level select tree
+// over the 32 accumulator registers (31 selects, rare path only).
+__device__ __forceinline__ uint32_t pick32(const uint32_t (&v)[32], int j) {
+  uint32_t a[16], b[8], c[4];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) a[i] = (j & 16) ? v[i + 16] : v[i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) b[i] = (j & 8) ? a[i + 8] : a[i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) c[i] = (j & 4) ? b[i + 4] : b[i];
+  const uint32_t d0 = (j & 2) ? c[2] : c[0], d1 = (j & 2) ? c[3] : c[1];
+  return (j & 1) ? d1 : d0;
+}
+
+// The columns of a 32-column slice that cleared the threshold (`hits`):
+// v holds raw accumulators (RAW, BF16 forms) or finished distances.  Dense
+// mode stores every column at its row's slot; filter mode runs the exact key
+// test against the query's current R-th key and reserves all survivors'
+// slots with one atomic.
 template <int MT, int MODE, bool RAW>
-__device__ __noinline__ void drain_hits(const float *vals, uint32_t hits, DrainCtx c) {
+__device__ __forceinline__ float drain_dist(uint32_t bits, float qa) {
+  const float a = __uint_as_float(bits);
+  return !RAW ? a : MT == M_L2 ? fmaf(-2.0f, a, qa) : (MT == M_IP ? a : -a);
+}
+
+template <int MT, int MODE, bool RAW>
+__device__ __forceinline__ void drain_mask(const uint32_t (&v)[32], uint32_t hits, const DrainCtx &c) {
+  uint64_t *out = c.cand + c.qid * c.cap;
+  if (MODE == TILE_DENSE) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int64_t row = c.rt + j;
+      if (row < c.r_end) out[row - c.r_begin] = make_key(drain_dist<MT, MODE, RAW>(v[j], c.qa), (uint32_t)row);
+    }
+    return;
+  }
+  uint32_t keep = 0;
   while (hits) {
     const int j = __ffs(hits) - 1;
     hits &= hits - 1;
     const int64_t row = c.rt + j;
     if (row >= c.r_end) continue;
-    const float a = vals[j];
-    const float d = !RAW ? a : MT == M_L2 ? fmaf(-2.0f, a, c.qa) : (MT == M_IP ? a : -a);
-    if (MODE == TILE_DENSE) {
-      c.cand[c.qid * c.cap + (row - c.r_begin)] = make_key(d, (uint32_t)row);
-    } else if (d < c.tau_d || (d == c.tau_d && (uint32_t)row < c.tau_r)) {
-      uint32_t slot = atomicAdd(c.count + c.qid, 1u);
-      if (slot < (uint32_t)c.cap) c.cand[c.qid * c.cap + slot] = make_key(d, (uint32_t)row);
-    }
+    const float d = drain_dist<MT, MODE, RAW>(pick32(v, j), c.qa);
+    if (d < c.tau_d || (d == c.tau_d && (uint32_t)row < c.tau_r)) keep |= 1u << j;
+  }
+  if (!keep) return;
+  uint32_t slot = atomicAdd(c.count + c.qid, (uint32_t)__popc(keep));
+  while (keep) {
+    const int j = __ffs(keep) - 1;
+    keep &= keep - 1;
+    if (slot < (uint32_t)c.cap)
+      out[slot] = make_key(drain_dist<MT, MODE, RAW>(pick32(v, j), c.qa), (uint32_t)(c.rt + j));
+    ++slot;
   }
 }
 
@@ -291,34 +327,29 @@ __global__ void __launch_bounds__(kLpThreads, 1)
           hits |= (uint32_t)hit << j;
         }
         if (MODE == TILE_DENSE) hits = 0xffffffffu;
-        if (qid >= 0 && hits) {
-          float f[32];  // only on the rare path
-#pragma unroll
-          for (int j = 0; j < 32; ++j) f[j] = __uint_as_float(v[j]);
-          drain_hits<MT, MODE, true>(f, hits, c);
-        }
+        if (qid >= 0 && hits) drain_mask<MT, MODE, true>(v, hits, c);
         continue;
       }
-      float f[32];
+      // finished distances replace the accumulators in place
       uint32_t hits = 0;
-      {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          float dot = __uint_as_float(v[j]);
-          if (PREC == HORA_PREC_FP8) dot *= qs * __shfl_sync(0xffffffffu, xs, j);
-          if (MT == M_L2) {
-            f[j] = fmaf(-2.0f, dot, qa + __shfl_sync(0xffffffffu, xa, j));
-          } else if (MT == M_IP) {
-            f[j] = dot;
-          } else {
-            float den = qa * __shfl_sync(0xffffffffu, xa, j);
-            f[j] = den == 0.0f ? 0.0f : -dot / den;
-          }
-          hits |= (uint32_t)(f[j] <= tau_d) << j;
+      for (int j = 0; j < 32; ++j) {
+        float dot = __uint_as_float(v[j]);
+        if (PREC == HORA_PREC_FP8) dot *= qs * __shfl_sync(0xffffffffu, xs, j);
+        float d;
+        if (MT == M_L2) {
+          d = fmaf(-2.0f, dot, qa + __shfl_sync(0xffffffffu, xa, j));
+        } else if (MT == M_IP) {
+          d = dot;
+        } else {
+          float den = qa * __shfl_sync(0xffffffffu, xa, j);
+          d = den == 0.0f ? 0.0f : -dot / den;
         }
+        v[j] = __float_as_uint(d);
+        hits |= (uint32_t)(d <= tau_d) << j;
       }
       if (MODE == TILE_DENSE) hits = 0xffffffffu;
-      if (qid >= 0 && hits) drain_hits<MT, MODE, false>(f, hits, c);
+      if (qid >= 0 && hits) drain_mask<MT, MODE, false>(v, hits, c);
     }
   }
   tc::fence_before_sync();

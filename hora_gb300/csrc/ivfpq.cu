@@ -308,11 +308,16 @@ __device__ __forceinline__ float l2_sub(const float *a, const float *b) {
 template <int DM>
 __global__ void __launch_bounds__(256) pq_kmeans_kernel(
     const float *Z, int64_t npos, const int64_t *toff, int M, int K, const int *sl, int epochs,
-    uint64_t seed, int accum_f64, uint8_t *asg_g, float *books, uint8_t *trained, int *status) {
+    uint64_t seed, int accum_f64, uint8_t *asg_g, uint32_t *mem_g, float *books, uint8_t *trained,
+    int *status) {
   extern __shared__ __align__(16) float sm[];
   float *cent = sm;                                  // K x DM
   int64_t *cnt = reinterpret_cast<int64_t *>(cent + K * DM + (K * DM) % 2);  // K
+  int *ccount = reinterpret_cast<int *>(cnt + K);    // K members per centre
+  int *cstart = ccount + K;                          // K first member slot
+  int *ccur = cstart + K;                            // K scatter cursor
   __shared__ float mean[DM];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int c = blockIdx.x / M, m = blockIdx.x % M;
   const int64_t lo = toff[c], n = toff[c + 1] - lo;
   const int len = sl[m];
@@ -324,6 +329,7 @@ __global__ void __launch_bounds__(256) pq_kmeans_kernel(
   }
   const float *z = Z + ((int64_t)m * npos + lo) * DM;
   uint8_t *asg = asg_g + (int64_t)m * npos + lo;
+  uint32_t *members = mem_g + (int64_t)m * npos + lo;
   // init_center
   if (threadIdx.x < DM) {
     int u = threadIdx.x;
@@ -367,32 +373,78 @@ __global__ void __launch_bounds__(256) pq_kmeans_kernel(
       asg[i] = (uint8_t)best;
     }
     __syncthreads();
-    // update_center: per centre, members in item order
+    // update_center: per centre, members in item order.  The members are
+    // bucketed by centre first (a stable counting sort), so each centre's
+    // thread reads only its own members.
+    for (int j = threadIdx.x; j < K; j += blockDim.x) ccount[j] = 0;
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&ccount[asg[i]], 1);
+    __syncthreads();
+    if (warp == 0) {
+      // exclusive scan of the counts (lane l owns centres l*per .. l*per+per-1)
+      const int per = (K + 31) / 32;
+      int run = 0;
+      for (int t = 0; t < per; ++t) {
+        const int j = lane * per + t;
+        run += j < K ? ccount[j] : 0;
+      }
+      int inc = run;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+      }
+      int at = inc - run;
+      for (int t = 0; t < per; ++t) {
+        const int j = lane * per + t;
+        if (j < K) {
+          cstart[j] = at;
+          ccur[j] = at;
+          at += ccount[j];
+        }
+      }
+      __syncwarp();
+      // stable scatter in item order, 32 items at a time
+      for (int64_t i0 = 0; i0 < n; i0 += 32) {
+        const int64_t i = i0 + lane;
+        const bool live = i < n;
+        const unsigned act = __ballot_sync(0xffffffffu, live);
+        if (live) {
+          const int a = asg[i];
+          const unsigned peers = __match_any_sync(act, a);
+          const int rank = __popc(peers & ((1u << lane) - 1u));
+          const int base = ccur[a];
+          members[base + rank] = (uint32_t)i;
+          __syncwarp(act);
+          if (rank == 0) ccur[a] = base + __popc(peers);
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
     for (int j = threadIdx.x; j < K; j += blockDim.x) {
-      int64_t cn = 0;
+      const int b = cstart[j], cn = ccount[j];
       float out[DM];
       if (accum_f64) {
         double s[DM];
 #pragma unroll
         for (int u = 0; u < DM; ++u) s[u] = 0.0;
-        for (int64_t i = 0; i < n; ++i)
-          if (asg[i] == j) {
-            ++cn;
+        for (int p = b; p < b + cn; ++p) {
+          const float *zr = z + (int64_t)members[p] * DM;
 #pragma unroll
-            for (int u = 0; u < DM; ++u) s[u] += (double)z[i * DM + u];
-          }
+          for (int u = 0; u < DM; ++u) s[u] += (double)zr[u];
+        }
 #pragma unroll
         for (int u = 0; u < DM; ++u) out[u] = cn ? (float)(s[u] / (double)cn) : 0.0f;
       } else {
         float s[DM];
 #pragma unroll
         for (int u = 0; u < DM; ++u) s[u] = 0.0f;
-        for (int64_t i = 0; i < n; ++i)
-          if (asg[i] == j) {
-            ++cn;
+        for (int p = b; p < b + cn; ++p) {
+          const float *zr = z + (int64_t)members[p] * DM;
 #pragma unroll
-            for (int u = 0; u < DM; ++u) s[u] = __fadd_rn(s[u], z[i * DM + u]);
-          }
+          for (int u = 0; u < DM; ++u) s[u] = __fadd_rn(s[u], zr[u]);
+        }
 #pragma unroll
         for (int u = 0; u < DM; ++u) out[u] = cn ? __fdiv_rn(s[u], (float)cn) : 0.0f;
       }
@@ -404,7 +456,6 @@ __global__ void __launch_bounds__(256) pq_kmeans_kernel(
     __syncthreads();
     if (ep < epochs - 1 && threadIdx.x < 32) {
       // split_center by warp 0 (split_pick_warp); lane 0 owns the counts
-      const int lane = threadIdx.x;
       const float lo_ = 1.0f - 1.0f / 1024.0f, hi_ = 1.0f + 1.0f / 1024.0f;
       for (int i0 = 0; i0 < K; i0 += 32) {
         // empty centres of this window in index order; a split only ever
@@ -847,13 +898,13 @@ static int dm_bucket(int dmax) { return dmax <= 1 ? 1 : dmax <= 2 ? 2 : dmax <= 
 
 template <int DM>
 static int launch_pq_kmeans(IvfState &v, const float *Z, int64_t npos, const int64_t *toff,
-                            int epochs, uint64_t seed, int accum, uint8_t *asg, int *status,
+                            int epochs, uint64_t seed, int accum, uint8_t *asg, uint32_t *mem, int *status,
                             cudaStream_t s) {
-  int smem = (int)(v.K * DM * 4 + 8 + v.K * 8 + 16);
+  int smem = (int)(v.K * DM * 4 + 8 + v.K * 8 + 3 * v.K * 4 + 16);
   HORA_CUDA_TRY(cudaFuncSetAttribute(pq_kmeans_kernel<DM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   ProfScope ps("pq_kmeans", s);
   pq_kmeans_kernel<DM><<<(unsigned)(v.n_list * v.n_sub), 256, smem, s>>>(
-      Z, npos, toff, (int)v.n_sub, (int)v.K, v.sub_len_d.as<int>(), epochs, seed, accum, asg,
+      Z, npos, toff, (int)v.n_sub, (int)v.K, v.sub_len_d.as<int>(), epochs, seed, accum, asg, mem,
       v.books.as<float>(), v.trained.as<uint8_t>(), status);
   HORA_LAUNCHED();
   return HORA_OK;
@@ -1055,12 +1106,13 @@ int ivf_build(hora_index *h) {
     toff[c + 1] = (int64_t)trows.size();
   }
   const int64_t npos = (int64_t)trows.size();
-  DevBuf d_toff, d_trows, d_tlist, Z, asg;
+  DevBuf d_toff, d_trows, d_tlist, Z, asg, mem;
   HORA_TRY(d_toff.reserve(sizeof(int64_t) * (C + 1)));
   HORA_TRY(d_trows.reserve(sizeof(uint32_t) * std::max<int64_t>(npos, 1)));
   HORA_TRY(d_tlist.reserve(sizeof(uint32_t) * std::max<int64_t>(npos, 1)));
   HORA_TRY(Z.reserve(sizeof(float) * std::max<int64_t>(npos, 1) * v.n_sub * v.dmax));
   HORA_TRY(asg.reserve(std::max<int64_t>(npos, 1) * v.n_sub));
+  HORA_TRY(mem.reserve(sizeof(uint32_t) * std::max<int64_t>(npos, 1) * v.n_sub));
   HORA_CUDA_TRY(cudaMemcpyAsync(d_toff.ptr, toff.data(), sizeof(int64_t) * (C + 1), cudaMemcpyHostToDevice, s));
   if (npos) {
     HORA_CUDA_TRY(cudaMemcpyAsync(d_trows.ptr, trows.data(), sizeof(uint32_t) * npos, cudaMemcpyHostToDevice, s));
@@ -1075,11 +1127,11 @@ int ivf_build(hora_index *h) {
   HORA_TRY(v.trained.reserve(C));
   HORA_CUDA_TRY(cudaMemsetAsync(v.trained.ptr, 0, C, s));
   switch (v.dmax) {
-    case 1: HORA_TRY(launch_pq_kmeans<1>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
-    case 2: HORA_TRY(launch_pq_kmeans<2>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
-    case 4: HORA_TRY(launch_pq_kmeans<4>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
-    case 8: HORA_TRY(launch_pq_kmeans<8>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
-    default: HORA_TRY(launch_pq_kmeans<16>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), d_status, s)); break;
+    case 1: HORA_TRY(launch_pq_kmeans<1>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), mem.as<uint32_t>(), d_status, s)); break;
+    case 2: HORA_TRY(launch_pq_kmeans<2>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), mem.as<uint32_t>(), d_status, s)); break;
+    case 4: HORA_TRY(launch_pq_kmeans<4>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), mem.as<uint32_t>(), d_status, s)); break;
+    case 8: HORA_TRY(launch_pq_kmeans<8>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), mem.as<uint32_t>(), d_status, s)); break;
+    default: HORA_TRY(launch_pq_kmeans<16>(v, Z.as<float>(), npos, d_toff.as<int64_t>(), epochs, h->seed, h->accum_f64, asg.as<uint8_t>(), mem.as<uint32_t>(), d_status, s)); break;
   }
   // ---- codes of every member ----
   HORA_TRY(v.codes.reserve(std::max<int64_t>(n, 1) * v.n_sub));
