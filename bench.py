@@ -269,7 +269,7 @@ def run_ivf(a, H, base, q, exact):
             st = ix.train_nprobe(tq, max_nprobe=128, recall_target=1.0, epochs=20)
             train_s = time.perf_counter() - t0
             ix.set_option(H.Option.LEARNED_NPROBE, 1)
-            for margin in (0.5, 1.0):
+            for margin in ((-1.0, -0.5, 0.0, 0.5) if p1 == 1 else (0.0, 0.5)):
                 ix.set_option(H.Option.NPROBE_MARGIN, margin)
                 r = timed(0)
                 r["mean_nprobe"] = float(np.maximum(ix.predict_nprobe(q), p1).mean())
@@ -390,7 +390,10 @@ def run_ours(a, dist: Dist):
                        "p50_ms": float(np.percentile(step_ms, 50)),
                        "p99_ms": float(np.percentile(step_ms, 99))}
 
-    ok = [f for f in order if "qps" in forms.get(f, {}) and (forms[f]["recall@10"] or 0) >= 0.95]
+    # without the exact form in --forms (profiling runs) recall is unknown and
+    # the fastest listed form is timed
+    ok = [f for f in order if "qps" in forms.get(f, {}) and
+          (exact is None or (forms[f]["recall@10"] or 0) >= 0.95)]
     head = max(ok, key=lambda f: forms[f]["qps"]) if ok else "fp32"
     prec = {"fp32": H.Precision.FP32, "bf16": H.Precision.BF16, "fp8": H.Precision.FP8}[head]
     ix.set_option(H.Option.PRECISION, prec)

@@ -187,33 +187,68 @@ int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint
 
 // Exact FP32 rerank: one thread per candidate walks the dimensions in order
 // (bit-identical to the scan kernel and the reference's scalar loops).
+// Exact FP32 distance of each query's R candidate rows (reference op order:
+// one running sum over the dimensions in order).  One CTA per query; a warp
+// takes 32 candidates at a time and reads their rows 64 dimensions at a time
+// (two rows per coalesced 512-byte load) into a padded shared tile (row
+// stride 65 floats: conflict-free column reads); each lane then sums its own
+// row from the tile in dimension order.
+constexpr int kRrWarps = 4, kRrSlab = 64;
 template <int MT>
-__global__ void rerank_exact_kernel(const float *Q, int64_t ld, const float *X, int64_t dim,
-                                    const float *qnorm, const float *xnorm, const uint64_t *in,
-                                    int R, uint64_t *outk) {
+__global__ void __launch_bounds__(kRrWarps * 32) rerank_exact_kernel(
+    const float *Q, int64_t ld, const float *X, int64_t dim, const float *qnorm, const float *xnorm,
+    const uint64_t *in, int R, uint64_t *outk) {
+  __shared__ float tile[kRrWarps][32][kRrSlab + 1];
+  extern __shared__ float qs[];  // ld floats: the query row
   const int64_t q = blockIdx.x;
-  const float *qq = Q + q * ld;
-  for (int r = threadIdx.x; r < R; r += blockDim.x) {
-    uint64_t key = in[q * R + r];
-    if (key == kEmptyKey) {
-      outk[q * R + r] = kEmptyKey;
-      continue;
-    }
-    uint32_t row = key_row(key);
-    const float4 *x4 = reinterpret_cast<const float4 *>(X + (int64_t)row * ld);
-    const float4 *q4 = reinterpret_cast<const float4 *>(qq);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t t = threadIdx.x; t < ld; t += blockDim.x) qs[t] = Q[q * ld + t];
+  __syncthreads();
+  const int64_t n4 = (dim + 3) / 4;  // the zero-padded columns up to 4*n4 add exact zeros
+  float(*tw)[kRrSlab + 1] = tile[warp];
+  const int half = lane >> 4, c4 = lane & 15;
+  for (int r0 = warp * 32; r0 < R; r0 += kRrWarps * 32) {
+    const int r = r0 + lane;
+    const uint64_t key = r < R ? in[q * R + r] : kEmptyKey;
     float s = 0.0f;
-    const int64_t n4 = (dim + 3) / 4;
-    for (int64_t t = 0; t < n4; ++t) {
-      float4 a = q4[t], b = x4[t];
+    for (int64_t d0 = 0; d0 < 4 * n4; d0 += kRrSlab) {
+      const int w = (int)(4 * n4 - d0 < kRrSlab ? 4 * n4 - d0 : kRrSlab);  // multiple of 4
+      // 8 rows' loads in flight per lane before any is stored
+      for (int jb = 0; jb < 16; jb += 8) {
+        float4 vv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int jj = 2 * (jb + u) + half;
+          const uint64_t kj = __shfl_sync(0xffffffffu, key, jj);
+          vv[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          if (kj != kEmptyKey && 4 * c4 < w)
+            vv[u] = __ldg(reinterpret_cast<const float4 *>(X + (int64_t)key_row(kj) * ld + d0) + c4);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int jj = 2 * (jb + u) + half;
+          if (4 * c4 < w) {
+            tw[jj][4 * c4] = vv[u].x;
+            tw[jj][4 * c4 + 1] = vv[u].y;
+            tw[jj][4 * c4 + 2] = vv[u].z;
+            tw[jj][4 * c4 + 3] = vv[u].w;
+          }
+        }
+      }
+      __syncwarp();
       constexpr int OP = MT == M_COS ? M_IP : MT;
-      s = dist_op<OP>(s, a.x, b.x);
-      s = dist_op<OP>(s, a.y, b.y);
-      s = dist_op<OP>(s, a.z, b.z);
-      s = dist_op<OP>(s, a.w, b.w);
+      for (int t = 0; t < w; ++t) s = dist_op<OP>(s, qs[d0 + t], tw[lane][t]);
+      __syncwarp();
     }
-    if (MT == M_COS) s = cosine_from_dot(s, qnorm[q], xnorm[row]);
-    outk[q * R + r] = make_key(s, row);
+    if (r < R) {
+      if (key == kEmptyKey) {
+        outk[q * R + r] = kEmptyKey;
+      } else {
+        const uint32_t row = key_row(key);
+        if (MT == M_COS) s = cosine_from_dot(s, qnorm[q], xnorm[row]);
+        outk[q * R + r] = make_key(s, row);
+      }
+    }
   }
 }
 
@@ -224,11 +259,14 @@ int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, 
   if (ld % 4) return fail(HORA_EINVAL, "rerank: pitch not a multiple of 4");
   ProfScope ps("rerank_exact", s);
   unsigned g = (unsigned)nq;
+  const size_t qb = sizeof(float) * (size_t)ld;  // the query row in dynamic shared memory
+  if (qb > 48 * 1024) return fail(HORA_EINVAL, "rerank: dimension too large");
+  constexpr int T = kRrWarps * 32;
   switch (metric) {
-    case M_L2: rerank_exact_kernel<M_L2><<<g, 128, 0, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
-    case M_L1: rerank_exact_kernel<M_L1><<<g, 128, 0, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
-    case M_IP: rerank_exact_kernel<M_IP><<<g, 128, 0, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
-    case M_COS: rerank_exact_kernel<M_COS><<<g, 128, 0, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
+    case M_L2: rerank_exact_kernel<M_L2><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
+    case M_L1: rerank_exact_kernel<M_L1><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
+    case M_IP: rerank_exact_kernel<M_IP><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
+    case M_COS: rerank_exact_kernel<M_COS><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
     default: return fail(HORA_EMETRIC, "unknown method");
   }
   HORA_LAUNCHED();

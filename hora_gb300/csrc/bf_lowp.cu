@@ -19,8 +19,9 @@
 // tiles), warp 1 owns TMEM (4 accumulator buffers of 128 columns) and issues
 // tcgen05.mma per tile, warps 2-17 drain the accumulators with tcgen05.ld (one
 // query row per TMEM lane, 32 columns per warp; the buffer is released as
-// soon as it is in registers), build a hit mask against the query's current
-// R-th key and hand the rare hits to an out-of-line append.  Every mbarrier
+// soon as it is in registers), test the slice's extreme against the query's
+// current R-th key and, on a hit, stage the keys in shared memory (flushed to
+// the query's list 8 at a time, one atomic per flush).  Every mbarrier
 // wait is bounded; a CTA that gives up raises an error flag read by the host,
 // waits for its MMAs and frees TMEM.
 #include <cuda_bf16.h>
@@ -42,6 +43,11 @@ constexpr int kLpThreads = 576;      // 18 warps
 constexpr int kLpEpiThreads = 512;   // warps 2..17
 constexpr int kLpTilesPerCta = 32;   // 4,096 rows per CTA
 constexpr int kLpMaxStages = 8;
+// Filter-mode hits are staged per drain thread in shared memory and
+// appended to the query's global list kLpHitBuf at a time (one atomic per
+// flush instead of one per hit, off the per-tile critical path).
+constexpr int kLpHitBuf = 8;
+constexpr int kLpHitBytes = kLpHitBuf * kLpEpiThreads * 8;
 
 struct LowpState {
   int prec = 0, metric = 0;
@@ -84,9 +90,10 @@ constexpr uint32_t kNormBytesA = 2 * kNormHalfA, kNormBytesB = 2 * kNormHalfB;
 struct DrainCtx {
   uint64_t *cand;
   uint32_t *count;
+  uint64_t *hb;  // this thread's staging column (stride kLpEpiThreads)
   int64_t qid, rt, r_begin, r_end;
   int cap;
-  float qa, tau_d;
+  float qa, tau_d;  // the query's current R-th key (distance, row)
   uint32_t tau_r;
 };
 
@@ -106,43 +113,46 @@ __device__ __forceinline__ uint32_t pick32(const uint32_t (&v)[32], int j) {
 
 // The columns of a 32-column slice that cleared the threshold (`hits`):
 // v holds raw accumulators (RAW, BF16 forms) or finished distances.  Dense
-// mode stores every column at its row's slot; filter mode runs the exact key
-// test against the query's current R-th key and reserves all survivors'
-// slots with one atomic.
+// mode stores every column at its row's slot; filter mode stages the hits that
+// pass the exact key test in this thread's shared-memory column.
 template <int MT, int MODE, bool RAW>
 __device__ __forceinline__ float drain_dist(uint32_t bits, float qa) {
   const float a = __uint_as_float(bits);
   return !RAW ? a : MT == M_L2 ? fmaf(-2.0f, a, qa) : (MT == M_IP ? a : -a);
 }
 
-template <int MT, int MODE, bool RAW>
-__device__ __forceinline__ void drain_mask(const uint32_t (&v)[32], uint32_t hits, const DrainCtx &c) {
+// Appends the staged keys to the query's list: one atomic reserves the slots.
+__device__ __forceinline__ void flush_hits(const DrainCtx &c, int &nb) {
+  uint32_t slot = atomicAdd(c.count + c.qid, (uint32_t)nb);
   uint64_t *out = c.cand + c.qid * c.cap;
-  if (MODE == TILE_DENSE) {
+  for (int i = 0; i < nb; ++i, ++slot)
+    if (slot < (uint32_t)c.cap) out[slot] = c.hb[i * kLpEpiThreads];
+  nb = 0;
+}
+
+template <int MT, int MODE, bool RAW>
+__device__ __forceinline__ void drain_mask(const uint32_t (&v)[32], uint32_t hits, const DrainCtx &c,
+                                           int &nb) {
+  if constexpr (MODE == TILE_DENSE) {
+    uint64_t *out = c.cand + c.qid * c.cap;
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
       const int64_t row = c.rt + j;
       if (row < c.r_end) out[row - c.r_begin] = make_key(drain_dist<MT, MODE, RAW>(v[j], c.qa), (uint32_t)row);
     }
-    return;
-  }
-  uint32_t keep = 0;
-  while (hits) {
-    const int j = __ffs(hits) - 1;
-    hits &= hits - 1;
-    const int64_t row = c.rt + j;
-    if (row >= c.r_end) continue;
-    const float d = drain_dist<MT, MODE, RAW>(pick32(v, j), c.qa);
-    if (d < c.tau_d || (d == c.tau_d && (uint32_t)row < c.tau_r)) keep |= 1u << j;
-  }
-  if (!keep) return;
-  uint32_t slot = atomicAdd(c.count + c.qid, (uint32_t)__popc(keep));
-  while (keep) {
-    const int j = __ffs(keep) - 1;
-    keep &= keep - 1;
-    if (slot < (uint32_t)c.cap)
-      out[slot] = make_key(drain_dist<MT, MODE, RAW>(pick32(v, j), c.qa), (uint32_t)(c.rt + j));
-    ++slot;
+  } else {
+    // the exact key test: only keys below the R-th key are offered, so a
+    // rescan after an overflow makes progress even through long runs of ties
+    while (hits) {
+      const int j = __ffs(hits) - 1;
+      hits &= hits - 1;
+      const int64_t row = c.rt + j;
+      if (row >= c.r_end) continue;
+      const float d = drain_dist<MT, MODE, RAW>(pick32(v, j), c.qa);
+      if (!(d < c.tau_d || (d == c.tau_d && (uint32_t)row < c.tau_r))) continue;
+      c.hb[nb * kLpEpiThreads] = make_key(d, (uint32_t)row);
+      if (++nb == kLpHitBuf) flush_hits(c, nb);
+    }
   }
 }
 
@@ -262,7 +272,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       }
       // all MMAs of this thread complete before TMEM is released
       tc::mma_commit(done);
-      tc::mbar_wait(done, 0, abort, 1u << 20);
+      tc::mbar_wait(done, 0, abort, tc::kWaitCycles, /*ignore_abort=*/true);
     }
   } else {
     // ---------------- drain ----------------
@@ -280,7 +290,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     float tau_d = __int_as_float(0x7f800000);
     uint32_t tau_r = 0xffffffffu;  // fewer than R keys yet: every finite distance passes
     if (MODE == TILE_FILTER && qid >= 0) {
-      uint64_t tk = p.best[qid * p.k + (p.k - 1)];
+      const uint64_t tk = p.best[qid * p.k + (p.k - 1)];
       if (tk != kEmptyKey) {
         tau_d = key_dist(tk);
         tau_r = key_row(tk);
@@ -297,7 +307,9 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       const float slack = 1e-6f * (fabsf(qa) + fabsf(tau_d)) + 1e-30f;
       thr = MT == M_L2 ? 0.5f * (qa - tau_d) - slack : (MT == M_IP ? tau_d + slack : -tau_d - slack);
     }
-    DrainCtx c{p.cand, p.count, qid, 0, p.r_begin, p.r_end, p.cap, qa, tau_d, tau_r};
+    uint64_t *hbuf = reinterpret_cast<uint64_t *>(bars + 32);
+    DrainCtx c{p.cand, p.count, hbuf + (threadIdx.x - 64), qid, 0, p.r_begin, p.r_end, p.cap, qa, tau_d, tau_r};
+    int nb = 0;  // keys staged in this thread's column
     for (int t = 0; t < T; ++t) {
       const int b = t % kLpNB, jb = t / kLpNB;
       c.rt = row0 + (int64_t)t * kLpBN + h * 32;
@@ -319,15 +331,32 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       tc::fence_before_sync();
       tc::mbar_arrive(acc_empty + b);
       if (FAST) {
-        uint32_t hits = 0;
+        if (qid < 0) continue;
+        if constexpr (MODE == TILE_DENSE) {
+          drain_mask<MT, MODE, true>(v, 0xffffffffu, c, nb);
+        } else {
+          // the slice's extreme (one min/max per column) decides whether any
+          // column can hit; the hit mask is built only then
+          float e[16];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const float a = __uint_as_float(v[j]);
-          const bool hit = MT == M_IP ? a <= thr : a >= thr;
-          hits |= (uint32_t)hit << j;
+          for (int i = 0; i < 16; ++i) {
+            const float x = __uint_as_float(v[i]), y = __uint_as_float(v[i + 16]);
+            e[i] = MT == M_IP ? fminf(x, y) : fmaxf(x, y);
+          }
+#pragma unroll
+          for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+            for (int i = 0; i < w; ++i) e[i] = MT == M_IP ? fminf(e[i], e[i + w]) : fmaxf(e[i], e[i + w]);
+          if (MT == M_IP ? e[0] <= thr : e[0] >= thr) {
+            uint32_t hits = 0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const float a = __uint_as_float(v[j]);
+              hits |= (uint32_t)(MT == M_IP ? a <= thr : a >= thr) << j;
+            }
+            drain_mask<MT, MODE, true>(v, hits, c, nb);
+          }
         }
-        if (MODE == TILE_DENSE) hits = 0xffffffffu;
-        if (qid >= 0 && hits) drain_mask<MT, MODE, true>(v, hits, c);
         continue;
       }
       // finished distances replace the accumulators in place
@@ -349,8 +378,9 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         hits |= (uint32_t)(d <= tau_d) << j;
       }
       if (MODE == TILE_DENSE) hits = 0xffffffffu;
-      if (qid >= 0 && hits) drain_mask<MT, MODE, false>(v, hits, c);
+      if (qid >= 0 && hits) drain_mask<MT, MODE, false>(v, hits, c, nb);
     }
+    if (qid >= 0 && nb > 0) flush_hits(c, nb);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -479,14 +509,15 @@ static int make_tmap_norm(CUtensorMap *m, const void *ptr, int64_t rows) {
 
 static int lp_smem_bytes(int nkb, int stages, bool fold) {
   return 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) +
-         stages * (nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0)) + 32 * 8;
+         stages * (nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0)) + 32 * 8 + kLpHitBytes;
 }
 
-// Ring depth: as many base tiles as fit in ~200 KB of shared memory.
+// Ring depth: as many base tiles as fit in ~220 KB of shared memory beside
+// the query tile and the hit staging.
 static int lp_stages(int nkb, bool fold) {
-  const int fixed = 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) + 32 * 8;
+  const int fixed = 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) + 32 * 8 + kLpHitBytes;
   const int stage = nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0);
-  return std::max(2, std::min(kLpMaxStages, (200 * 1024 - fixed) / stage));
+  return std::max(2, std::min(kLpMaxStages, (220 * 1024 - fixed) / stage));
 }
 
 template <int PREC, int MT, int MODE>

@@ -569,41 +569,6 @@ __global__ void pair_scatter_kernel(const uint64_t *probes, int64_t nq, int pmax
 // k-th key go to the lowest positions.  sel receives the k positions
 // (unordered).  L and k are uniform, 0 < k < L.  hist: kSelBins u32, zero on
 // entry and on return; scratch: 48 ints.
-constexpr int kSelBins = 2048;
-
-// Warp 0: the bin whose cumulative count first reaches rem among nbins
-// (32 times a power of two); out[0] = bin, out[1] = keys below it.  Lane l owns bins
-// [l*nb, l*nb+nb) and sums them in a rotated order (conflict-free banks).
-__device__ __forceinline__ void warp_find_bin(const uint32_t *hist, int nbins, uint32_t rem,
-                                              int *out) {
-  const int lane = threadIdx.x & 31, nb = nbins >> 5;  // nb: a power of two
-  uint32_t s = 0;
-#pragma unroll 8
-  for (int i = 0; i < nb; ++i) s += hist[lane * nb + ((i + lane) & (nb - 1))];
-  uint32_t inc = s;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += y;
-  }
-  const uint32_t exc = inc - s;
-  const bool mine = exc < rem && inc >= rem;
-  if (mine) {
-    uint32_t run = exc;
-    int d = lane * nb + nb - 1;
-    for (int i = 0; i < nb; ++i) {
-      const uint32_t b = hist[lane * nb + i];
-      if (run + b >= rem) {
-        d = lane * nb + i;
-        break;
-      }
-      run += b;
-    }
-    out[0] = d;
-    out[1] = (int)run;
-  }
-}
-
 __device__ void cta_select_k(const uint32_t *keys, int L, int k, int *sel, uint32_t *hist,
                              int *scratch) {
   // scratch: [0] remaining k, [1] digit, [2] below, [3] taken, [5] count at the k-th key,

@@ -36,13 +36,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: gives up after `limit` polls or when *abort is set; on giving
-// up it raises *abort (shared) and the caller unwinds.
+// try_wait with a suspend-time hint: the thread sleeps until the phase
+// completes or about `hint_ns` pass, instead of spinning on issue slots.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+// About two seconds of SM clocks: no wait of a healthy pipeline comes near it.
+constexpr long long kWaitCycles = 4000000000ll;
+// Bounded wait: the thread sleeps in try_wait between checks; gives up when
+// *abort is raised by another thread (unless ignore_abort) or after
+// max_cycles SM clocks, in which case it raises *abort itself.  The caller
+// unwinds on false.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
-                                          uint32_t limit = (1u << 24)) {
-  for (uint32_t i = 0; i < limit; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (*abort) return false;
+                                          long long max_cycles = kWaitCycles, bool ignore_abort = false) {
+  const long long t0 = clock64();
+  for (;;) {
+    if (mbar_try_wait_sleep(bar, parity, 1000000u)) return true;
+    if (!ignore_abort && *abort) return false;
+    if (clock64() - t0 > max_cycles) break;
   }
   *abort = 1;
   return false;

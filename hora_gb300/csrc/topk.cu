@@ -15,6 +15,28 @@
 namespace hora {
 
 constexpr int kMergeThreads = 512;
+constexpr int kSelectThreads = 256;
+
+// Ascending bitonic sort of P (a power of two, <= 512) keys in shared memory
+// by one warp: no block barriers, so the CTA's other warps are free.
+__device__ __forceinline__ void warp_bitonic_sort(uint64_t *sk, int P) {
+  const int lane = threadIdx.x & 31;
+  for (int size = 2; size <= P; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = lane; i < (P >> 1); i += 32) {
+        const int lo = 2 * i - (i & (stride - 1));
+        const int hi = lo + stride;
+        const bool asc = (lo & size) == 0;
+        const uint64_t a = sk[lo], b = sk[hi];
+        if ((a > b) == asc) {
+          sk[lo] = b;
+          sk[hi] = a;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
 
 __device__ __forceinline__ void block_bitonic_sort(uint64_t *sk, int P) {
   for (int size = 2; size <= P; size <<= 1) {
@@ -106,15 +128,18 @@ __global__ void __launch_bounds__(kMergeThreads) merge_topk_kernel(
 
 // Merge without duplicates (candidate rows are disjoint from the rows already
 // in the list: chunks and lists never overlap): radix-select the k-th
-// smallest of the c + k keys on 8-bit digits, gather the k winners and sort
-// only those.  Cheaper than sorting all c + k keys when c >> k.
-__global__ void __launch_bounds__(kMergeThreads) merge_select_kernel(
+// smallest of the c + k keys, gather the k winners and sort only those.
+// Digits of 11/11/10 bits from the top of the 64-bit key (distance bits
+// first, then the row), histogram updates aggregated per warp; the select
+// stops as soon as the digit holding the k-th key holds exactly the keys
+// still needed (usually once the distance bits are resolved).
+__global__ void __launch_bounds__(kSelectThreads) merge_select_kernel(
     uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n,
     uint8_t *ovf_flag, uint32_t *ovf_counter) {
   extern __shared__ uint64_t sk[];
-  __shared__ uint32_t hist[256];
-  __shared__ int dig[2];
-  __shared__ int n_sel;
+  __shared__ uint32_t hist[kSelBins];
+  __shared__ int sc[8];  // [0] live, [1] digit, [2] below, [3] taken, [4] remaining, [5] at digit
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t q = blockIdx.x;
   uint32_t c = dense_n > 0 ? (uint32_t)dense_n : count[q];
   if (c == 0) return;
@@ -124,52 +149,170 @@ __global__ void __launch_bounds__(kMergeThreads) merge_select_kernel(
   uint64_t *bq = best + q * k;
   // live keys: candidates, then the list's non-empty prefix
   const int n = (int)c + k;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) sk[i] = i < (int)c ? cq[i] : bq[i - c];
-  __syncthreads();
-  // count the non-empty keys (the list may be partially empty)
-  if (threadIdx.x == 0) n_sel = 0;
+  if (threadIdx.x == 0) {
+    sc[0] = 0;
+    sc[3] = 0;
+  }
+  for (int b = threadIdx.x; b < kSelBins; b += blockDim.x) hist[b] = 0;
   __syncthreads();
   int live = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) live += sk[i] != kEmptyKey;
-  atomicAdd(&n_sel, live);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const uint64_t v = i < (int)c ? cq[i] : bq[i - c];
+    sk[i] = v;
+    live += v != kEmptyKey;
+  }
+  live = __reduce_add_sync(0xffffffffu, live);
+  if (lane == 0) atomicAdd(&sc[0], live);
   __syncthreads();
-  const int nl = n_sel;
+  const int nl = sc[0];
   const int want = nl < k ? nl : k;
   uint64_t *sel = sk + n;  // want keys
   if (want > 0) {
     uint64_t prefix = 0, mask = 0;
-    uint32_t rem = (uint32_t)want;
-    for (int shift = 56; shift >= 0; shift -= 8) {
-      for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
-      __syncthreads();
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        uint64_t v = sk[i];
-        if (v != kEmptyKey && (v & mask) == prefix) atomicAdd(&hist[(v >> shift) & 255u], 1u);
+    int rem = want;
+    for (int pass = 0; pass < 6; ++pass) {
+      const int shift = pass == 0 ? 53 : pass == 1 ? 42 : pass == 2 ? 32 : pass == 3 ? 21 : pass == 4 ? 10 : 0;
+      const uint32_t dmask = (pass == 2 || pass == 5) ? 1023u : 2047u;
+      for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const uint64_t v = i < n ? sk[i] : kEmptyKey;
+        const bool p = v != kEmptyKey && (v & mask) == prefix;
+        const unsigned pm = __ballot_sync(0xffffffffu, p);
+        if (p) {
+          const uint32_t dig = (uint32_t)(v >> shift) & dmask;
+          const unsigned peers = __match_any_sync(pm, dig);
+          if (lane == __ffs(peers) - 1) atomicAdd(&hist[dig], (uint32_t)__popc(peers));
+        }
       }
       __syncthreads();
-      if (threadIdx.x < 32) warp_find_digit(hist, rem, dig);
+      if (warp == 0) {
+        warp_find_bin(hist, (int)dmask + 1, (uint32_t)rem, sc + 1);
+        __syncwarp();
+        const int at = (int)hist[sc[1]];
+        const int below = sc[2];
+        __syncwarp();
+        for (int b = lane; b <= (int)dmask; b += 32) hist[b] = 0;
+        if (lane == 0) {
+          sc[4] = rem - below;
+          sc[5] = at;
+        }
+      }
       __syncthreads();
-      rem -= (uint32_t)dig[1];
-      prefix |= (uint64_t)dig[0] << shift;
-      mask |= (uint64_t)0xff << shift;
-      __syncthreads();
+      rem = sc[4];
+      prefix |= (uint64_t)sc[1] << shift;
+      mask |= (uint64_t)dmask << shift;
+      if (sc[5] == rem) break;  // every key under this prefix is taken
     }
-    // keys are distinct, so exactly `want` keys are <= the k-th key
-    if (threadIdx.x == 0) n_sel = 0;
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      uint64_t v = sk[i];
-      if (v != kEmptyKey && v <= prefix) sel[atomicAdd(&n_sel, 1)] = v;
+    // the winners: keys whose masked top bits are <= the prefix
+    for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+      const int i = i0 + threadIdx.x;
+      const uint64_t v = i < n ? sk[i] : kEmptyKey;
+      const bool p = v != kEmptyKey && (v & mask) <= prefix;
+      const unsigned pm = __ballot_sync(0xffffffffu, p);
+      if (pm) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&sc[3], __popc(pm));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int slot = base + __popc(pm & ((1u << lane) - 1u));
+        if (p && slot < want) sel[slot] = v;  // (keys are distinct: exactly want pass)
+      }
     }
     __syncthreads();
     int P = 1;
     while (P < want) P <<= 1;
     for (int i = want + threadIdx.x; i < P; i += blockDim.x) sel[i] = kEmptyKey;
     __syncthreads();
-    block_bitonic_sort(sel, P);
+    if (P <= 512) {
+      if (warp == 0) warp_bitonic_sort(sel, P);
+      __syncthreads();
+    } else {
+      block_bitonic_sort(sel, P);
+    }
   }
   for (int i = threadIdx.x; i < k; i += blockDim.x) bq[i] = i < want ? sel[i] : kEmptyKey;
   if (threadIdx.x == 0) {
+    if (dense_n <= 0) count[q] = 0;
+    if (ovf) {
+      ovf_flag[q] = 1;
+      atomicAdd(ovf_counter, 1u);
+    }
+  }
+}
+
+// The same merge with one warp per query (8 queries per CTA) for k <= 256:
+// the keys stay in global memory (L1-resident across the passes), the
+// histogram is warp-private (8-bit digits, updates aggregated per digit), the
+// winners are sorted by the warp; no block barrier anywhere, so the warps of
+// a CTA never wait for one another.
+constexpr int kWmWarps = 8, kWmMaxK = 256;
+__global__ void __launch_bounds__(kWmWarps * 32) merge_warp_kernel(
+    uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n, int64_t nq,
+    uint8_t *ovf_flag, uint32_t *ovf_counter) {
+  __shared__ uint32_t hist_all[kWmWarps][256];
+  __shared__ uint64_t sel_all[kWmWarps][kWmMaxK];
+  __shared__ int dig_all[kWmWarps][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t q = (int64_t)blockIdx.x * kWmWarps + warp;
+  if (q >= nq) return;
+  uint32_t *hist = hist_all[warp];
+  uint64_t *sel = sel_all[warp];
+  int *dig = dig_all[warp];
+  uint32_t c = dense_n > 0 ? (uint32_t)dense_n : count[q];
+  if (c == 0) return;
+  const bool ovf = c > (uint32_t)cap;
+  if (ovf) c = cap;
+  const uint64_t *cq = cand + q * cap;
+  uint64_t *bq = best + q * k;
+  const int n = (int)c + k;
+  int live = 0;
+  for (int i = lane; i < n; i += 32) live += (i < (int)c ? cq[i] : bq[i - c]) != kEmptyKey;
+  live = __reduce_add_sync(0xffffffffu, live);
+  const int want = live < k ? live : k;
+  if (want > 0) {
+    uint64_t prefix = 0, mask = 0;
+    int rem = want;
+    for (int shift = 56; shift >= 0; shift -= 8) {
+      for (int b = lane; b < 256; b += 32) hist[b] = 0;
+      __syncwarp();
+      for (int i0 = 0; i0 < n; i0 += 32) {
+        const int i = i0 + lane;
+        const uint64_t v = i < n ? (i < (int)c ? cq[i] : bq[i - c]) : kEmptyKey;
+        const bool p = v != kEmptyKey && (v & mask) == prefix;
+        const unsigned pm = __ballot_sync(0xffffffffu, p);
+        if (p) {
+          const uint32_t d = (uint32_t)(v >> shift) & 255u;
+          const unsigned peers = __match_any_sync(pm, d);
+          if (lane == __ffs(peers) - 1) atomicAdd(&hist[d], (uint32_t)__popc(peers));
+        }
+      }
+      __syncwarp();
+      warp_find_digit(hist, (uint32_t)rem, dig);
+      __syncwarp();
+      const int d = dig[0], at = (int)hist[d];
+      rem -= dig[1];
+      prefix |= (uint64_t)d << shift;
+      mask |= (uint64_t)0xff << shift;
+      __syncwarp();
+      if (at == rem) break;  // every key under this prefix is taken
+    }
+    int taken = 0;
+    for (int i0 = 0; i0 < n; i0 += 32) {
+      const int i = i0 + lane;
+      const uint64_t v = i < n ? (i < (int)c ? cq[i] : bq[i - c]) : kEmptyKey;
+      const bool p = v != kEmptyKey && (v & mask) <= prefix;
+      const unsigned pm = __ballot_sync(0xffffffffu, p);
+      const int slot = taken + __popc(pm & ((1u << lane) - 1u));
+      if (p && slot < want) sel[slot] = v;
+      taken += __popc(pm);
+    }
+    int P = 1;
+    while (P < want) P <<= 1;
+    for (int i = want + lane; i < P; i += 32) sel[i] = kEmptyKey;
+    __syncwarp();
+    warp_bitonic_sort(sel, P);
+  }
+  for (int i = lane; i < k; i += 32) bq[i] = i < want ? sel[i] : kEmptyKey;
+  if (lane == 0) {
     if (dense_n <= 0) count[q] = 0;
     if (ovf) {
       ovf_flag[q] = 1;
@@ -197,13 +340,20 @@ int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *cou
     attr = true;
   }
   const int cmax = dense_n > 0 ? dense_n : cap;
+  if (!qlist && k <= kWmMaxK) {
+    ProfScope ps("topk_merge", s);
+    merge_warp_kernel<<<(unsigned)ceil_div(nlist, (int64_t)kWmWarps), kWmWarps * 32, 0, s>>>(
+        best, k, cand, count, cap, dense_n, nlist, ovf_flag, ovf_counter);
+    HORA_LAUNCHED();
+    return HORA_OK;
+  }
   if (!qlist) {
     int P = 1;
     while (P < k) P <<= 1;
     const size_t smem = (size_t)(cmax + k + P) * 8;
     if (smem <= 200 * 1024) {
       ProfScope ps("topk_merge", s);
-      merge_select_kernel<<<(unsigned)nlist, kMergeThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
+      merge_select_kernel<<<(unsigned)nlist, kSelectThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
                                                                        ovf_flag, ovf_counter);
       HORA_LAUNCHED();
       return HORA_OK;
