@@ -269,7 +269,7 @@ def run_ivf(a, H, base, q, exact):
             st = ix.train_nprobe(tq, max_nprobe=128, recall_target=1.0, epochs=20)
             train_s = time.perf_counter() - t0
             ix.set_option(H.Option.LEARNED_NPROBE, 1)
-            for margin in ((-1.0, -0.5, 0.0, 0.5) if p1 == 1 else (0.0, 0.5)):
+            for margin in ((-2.0, -1.5, -1.0, -0.5, 0.0) if p1 == 1 else (0.0, 0.5)):
                 ix.set_option(H.Option.NPROBE_MARGIN, margin)
                 r = timed(0)
                 r["mean_nprobe"] = float(np.maximum(ix.predict_nprobe(q), p1).mean())

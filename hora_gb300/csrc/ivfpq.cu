@@ -545,6 +545,22 @@ __global__ void pair_hist_kernel(const uint64_t *probes, int64_t nq, int pmax, i
   atomicAdd(reinterpret_cast<unsigned long long *>(cnt + key_row(k)), 1ull);
 }
 
+// Per query: the number of ADC candidates its probe slots [jbegin, nprobe)
+// hold ((nprobe - jbegin) x R, contiguous from slot jbegin), and empty keys
+// in any slot of that range whose probe is empty (no pair was formed), so
+// the merge reads exactly the slots this call wrote.
+__global__ void pair_counts_kernel(const uint64_t *probes, int64_t nq, int pmax, int jbegin,
+                                   const uint32_t *nprobe_q, int R, uint64_t *cand, uint32_t *count) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nq * pmax) return;
+  const int64_t q = t / pmax;
+  const int j = (int)(t % pmax);
+  const int p = nprobe_q ? min((int)nprobe_q[q], pmax) : pmax;
+  if (j == 0) count[q] = (uint32_t)(p > jbegin ? (p - jbegin) * R : 0);
+  if (j >= jbegin && j < p && probes[t] == kEmptyKey)
+    for (int r = 0; r < R; ++r) cand[t * R + r] = kEmptyKey;
+}
+
 __global__ void pair_scatter_kernel(const uint64_t *probes, int64_t nq, int pmax, int jbegin,
                                     const uint32_t *nprobe_q, int C, const int64_t *off,
                                     int64_t *cursor, uint32_t *pq, uint32_t *pc, uint32_t *pslot) {
@@ -1255,9 +1271,20 @@ int ivf_adc_merge(hora_index *h, int64_t nq, int pmax, int jbegin, const uint32_
         ws.pair_q.as<uint32_t>(), ws.pair_c.as<uint32_t>(), ws.pair_slot.as<uint32_t>());
     HORA_LAUNCHED();
   }
-  // LUT + ADC scan + per-pair R best
+  // LUT + ADC scan + per-pair R best; the merge reads only the slots written
+  // (the grouped merge for very wide rerank lists reads every slot)
+  const int width = pmax * R;
+  const bool grouped = !(R <= 256 || merge_smem_bytes(R, width) <= 200 * 1024);
   HORA_TRY(ws.ivf_cand.reserve(sizeof(uint64_t) * nq * pmax * R));
-  HORA_CUDA_TRY(cudaMemsetAsync(ws.ivf_cand.ptr, 0xff, sizeof(uint64_t) * nq * pmax * R, s));
+  if (grouped) HORA_CUDA_TRY(cudaMemsetAsync(ws.ivf_cand.ptr, 0xff, sizeof(uint64_t) * nq * pmax * R, s));
+  HORA_TRY(ws.count.reserve(sizeof(uint32_t) * std::max<int64_t>(nq, 1)));
+  {
+    ProfScope ps("ivf_pairs", s);
+    pair_counts_kernel<<<ceil_div(tot, 256), 256, 0, s>>>(ws.probes.as<uint64_t>(), nq, pmax, jbegin,
+                                                         d_nprobe, R, ws.ivf_cand.as<uint64_t>(),
+                                                         ws.count.as<uint32_t>());
+    HORA_LAUNCHED();
+  }
   const int per = 4;
   switch (v.dmax) {
     case 1: HORA_TRY(launch_adc<1>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
@@ -1266,13 +1293,15 @@ int ivf_adc_merge(hora_index *h, int64_t nq, int pmax, int jbegin, const uint32_
     case 8: HORA_TRY(launch_adc<8>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
     default: HORA_TRY(launch_adc<16>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
   }
-  // per-query merge of the candidates (pq_idx.rs:429-436)
-  const int width = pmax * R;
+  // per-query merge of the candidates (pq_idx.rs:429-436): each query's
+  // slots [jbegin, nprobe) are contiguous, so the merge reads
+  // count[q] = (nprobe - jbegin) x R keys from slot jbegin
   HORA_TRY(ws.ovf_flag.reserve(nq));
   HORA_TRY(ws.ovf_counter.reserve(4));
-  if (merge_smem_bytes(R, width) <= 200 * 1024) {
-    HORA_TRY(launch_merge_topk(M, R, ws.ivf_cand.as<uint64_t>(), nullptr, width, width, nullptr, nq,
-                               ws.ovf_flag.as<uint8_t>(), ws.ovf_counter.as<uint32_t>(), s));
+  if (!grouped) {
+    HORA_TRY(launch_merge_topk(M, R, ws.ivf_cand.as<uint64_t>() + (int64_t)jbegin * R, ws.count.as<uint32_t>(),
+                               width, 0, nullptr, nq, ws.ovf_flag.as<uint8_t>(),
+                               ws.ovf_counter.as<uint32_t>(), s));
   } else {
     // merge probe slots in groups that fit one shared-memory sort
     int grp = std::max(1, (16384 - R) / R);
