@@ -259,6 +259,23 @@ def run_ivf(a, H, base, q, exact):
     out = {"workload": "IVFPQIndex 1Mx128 mixture, 1024 lists, 32x8-bit PQ, train 500k, "
                        f"{a.ivf_epochs} epochs, 10k queries, k=10, exact rerank of 100 ADC candidates",
            "build_s": build_s, "sweep": {str(k): v for k, v in sweep.items()}}
+    # the reference's CPU search (oracle port, ADC only) on the GPU-built index
+    try:
+        from oracle import oracle as O
+        O.build()
+        ex = ix.export()
+        ex["metric"] = O.EUCLIDEAN
+        ns, threads = 1000, os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ci, _ = O.ivfpq_search(ex, q[:ns], 10, 2, threads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"kind": "port", "nprobe": 2, "queries": ns, "cores": threads,
+                               "qps": ns / dt, "seconds": dt,
+                               "recall@10": recall_at(ci, ex10[:ns], 10) if ex10 is not None else None,
+                               "note": "ADC distances only (reference semantics, no rerank)"}
+        del ex
+    except Exception as e:  # the CPU leg is a reported baseline only
+        out["cpu_baseline"] = {"error": str(e)}
     # learned nprobe (trained on queries from the same distribution, disjoint from the bench's)
     try:
         tq = synth.mixture(a.ivf_train_queries, DIM, N_CENTERS, stream=7)
@@ -269,7 +286,7 @@ def run_ivf(a, H, base, q, exact):
             st = ix.train_nprobe(tq, max_nprobe=128, recall_target=1.0, epochs=20)
             train_s = time.perf_counter() - t0
             ix.set_option(H.Option.LEARNED_NPROBE, 1)
-            for margin in ((-2.0, -1.5, -1.0, -0.5, 0.0) if p1 == 1 else (0.0, 0.5)):
+            for margin in ((-2.0, -1.5, -1.25, -1.0, -0.5, 0.0) if p1 == 1 else (0.0, 0.5)):
                 ix.set_option(H.Option.NPROBE_MARGIN, margin)
                 r = timed(0)
                 r["mean_nprobe"] = float(np.maximum(ix.predict_nprobe(q), p1).mean())
@@ -332,6 +349,73 @@ def run_serving(a, H, bf_index, bf_pool):
                                             seed=int(rate)))
     finally:
         srv.close()
+    return out
+
+
+def run_form_extras(a, H, ix, base, q, dq, exact, head_prec):
+    """Config-2 items beside the headline: the BF16 form with the 4,096-candidate
+    rerank the configuration names, the other three metrics (exact FP32 and
+    BF16 + rerank; Manhattan has no tensor-core form), and the returned
+    distances and ids of a query sample against the FP64 exact oracle."""
+    import torch
+    from oracle import oracle as O
+    nq = q.shape[0]
+    out = {}
+
+    def timed(index, k, reps=2):
+        ids_d = torch.empty((nq, k), dtype=torch.int64, device="cuda")
+        dist_d = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+        index.search_batch(dq, k, ids_out=ids_d, dist_out=dist_d)
+        ms = []
+        for _ in range(reps):
+            index.search_batch(dq, k, ids_out=ids_d, dist_out=dist_d)
+            ms.append(json.loads(index.idx_info())["last_search_ms"])
+        torch.cuda.synchronize()
+        return float(np.median(ms)), ids_d.cpu().numpy(), dist_d.cpu().numpy()
+
+    # BF16 with a 4,096-candidate exact rerank
+    ix.set_option(H.Option.PRECISION, H.Precision.BF16)
+    ix.set_option(H.Option.RERANK, 4096)
+    ms, ids, _ = timed(ix, K, reps=1)
+    H._lib.profile_report()
+    H._lib.profile(True)
+    ms, ids, _ = timed(ix, K, reps=1)
+    H._lib.profile(False)
+    kern = {k: {"launches": v[0], "ms": v[1] / 2} for k, v in H._lib.profile_report().items()}
+    out["bf16_rerank_4096"] = {"qps": nq / (ms / 1e3), "ms": ms, "kernels_per_search": kern,
+                               "recall@10": recall_at(ids, exact, 10) if exact is not None else None,
+                               "recall@100": recall_at(ids, exact, K) if exact is not None else None}
+    ix.set_option(H.Option.RERANK, 0)
+    ix.set_option(H.Option.PRECISION, head_prec)
+
+    # the other metrics, each on its own index over the same base
+    out["metrics"] = {}
+    xb = torch.from_numpy(base).cuda()
+    for name, mt in (("DotProduct", H.Metric.DotProduct), ("CosineSimilarity", H.Metric.CosineSimilarity),
+                     ("Manhattan", H.Metric.Manhattan)):
+        m = H.BruteForceIndex(DIM)
+        m.madd(xb, None)
+        m.build(mt)
+        ms32, ids32, _ = timed(m, K)
+        r = {"fp32_qps": nq / (ms32 / 1e3)}
+        if mt != H.Metric.Manhattan:
+            m.set_option(H.Option.PRECISION, H.Precision.BF16)
+            ms16, ids16, _ = timed(m, K)
+            r.update(bf16_qps=nq / (ms16 / 1e3), bf16_recall_at_10=recall_at(ids16, ids32, 10),
+                     bf16_recall_at_100=recall_at(ids16, ids32, K))
+        out["metrics"][name] = r
+        del m
+    del xb
+
+    # a query sample against the FP64 exact oracle (Euclidean, headline form)
+    ns = 32
+    ids_h, d_h = ix.search_batch(q[:ns], K)
+    O.build()
+    i64, d64 = O.bf_exact_f64(base, q[:ns], K, O.EUCLIDEAN, threads=os.cpu_count() or 1)
+    rel = np.abs(d_h.astype(np.float64) - d64) / np.maximum(np.abs(d64), 1e-30)
+    out["fp64_check"] = {"queries": ns, "recall@10": recall_at(ids_h.astype(np.int64), i64, 10),
+                         "recall@100": recall_at(ids_h.astype(np.int64), i64, K),
+                         "max_rel_dist_err": float(rel.max()), "mean_rel_dist_err": float(rel.mean())}
     return out
 
 
@@ -462,6 +546,7 @@ def run_ours(a, dist: Dist):
         roof["traffic"] = None
         roof["share_of_step"] = ms / (t_dev * 1e3)
 
+    extras = run_form_extras(a, H, ix, base, q, dq, exact, prec) if not a.small and dist.rank == 0 else None
     config1 = run_config1(H, dist.rank == 0) if not a.small else None
     ivf, serving = None, None
     if not a.no_ivf:
@@ -492,7 +577,7 @@ def run_ours(a, dist: Dist):
             "forms": forms, "p50_ms": float(np.percentile(step_ms, 50)),
             "p99_ms": float(np.percentile(step_ms, 99)), "wall_s": t_wall,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "ivfpq": ivf,
-            "serving": serving, "config1": config1,
+            "serving": serving, "config1": config1, "form_extras": extras,
             "gpu_launches": launches, "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
         }
         print(json.dumps(line), flush=True)

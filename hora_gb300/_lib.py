@@ -32,6 +32,10 @@ class IVFPQParamsC(C.Structure):
                 ("search_n_center", C.c_uint64), ("train_epoch", C.c_uint64)]
 
 
+class PQParamsC(C.Structure):
+    _fields_ = [("n_sub", C.c_uint64), ("sub_bits", C.c_uint64), ("train_epoch", C.c_uint64)]
+
+
 _lib = None
 
 vp = C.c_void_p
@@ -51,6 +55,7 @@ SIGNATURES = {
     "hora_profile_enable": (C.c_int, [C.c_int]),
     "hora_profile_report": (C.c_int, [C.c_char_p, u64]),
     "hora_ivfpq_params_default": (None, [C.POINTER(IVFPQParamsC)]),
+    "hora_pq_params_default": (None, [C.POINTER(PQParamsC)]),
     "hora_index_create": (C.c_int, [C.c_int, u64, vp, C.POINTER(vp)]),
     "hora_index_free": (C.c_int, [vp]),
     "hora_add": (C.c_int, [vp, vp, vp, u64]),

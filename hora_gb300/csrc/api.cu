@@ -200,10 +200,18 @@ void hora_ivfpq_params_default(hora_ivfpq_params *p) {
   p->train_epoch = 100;
 }
 
+void hora_pq_params_default(hora_pq_params *p) {
+  if (!p) return;
+  // PQParams::default (src/index/pq_params.rs:32-41)
+  p->n_sub = 4;
+  p->sub_bits = 4;
+  p->train_epoch = 100;
+}
+
 int hora_index_create(int kind, uint64_t dim, const void *params, hora_index **out) {
   if (!out) return fail(HORA_EINVAL, "out is null");
   *out = nullptr;
-  if (kind != HORA_INDEX_BRUTE_FORCE && kind != HORA_INDEX_IVFPQ)
+  if (kind != HORA_INDEX_BRUTE_FORCE && kind != HORA_INDEX_IVFPQ && kind != HORA_INDEX_PQ)
     return fail(HORA_EINVAL, "unknown index kind");
   if (dim == 0) return fail(HORA_EINVAL, "dimension must be positive");
   if (dim >= (1ull << 20)) return fail(HORA_ECAP, "dimension too large");
@@ -211,9 +219,20 @@ int hora_index_create(int kind, uint64_t dim, const void *params, hora_index **o
   h->kind = kind;
   h->dim = dim;
   h->ld = (uint64_t)round_up((int64_t)dim, 4);
-  if (kind == HORA_INDEX_IVFPQ) {
+  if (kind == HORA_INDEX_IVFPQ || kind == HORA_INDEX_PQ) {
     hora_ivfpq_params_default(&h->ivf);
-    if (params) h->ivf = *reinterpret_cast<const hora_ivfpq_params *>(params);
+    if (kind == HORA_INDEX_IVFPQ && params) h->ivf = *reinterpret_cast<const hora_ivfpq_params *>(params);
+    if (kind == HORA_INDEX_PQ) {
+      // a flat PQIndex is the IVF machinery with one list centred at zero
+      hora_pq_params pq;
+      hora_pq_params_default(&pq);
+      if (params) pq = *reinterpret_cast<const hora_pq_params *>(params);
+      h->ivf.n_sub = pq.n_sub;
+      h->ivf.sub_bits = pq.sub_bits;
+      h->ivf.train_epoch = pq.train_epoch;
+      h->ivf.n_kmeans_center = 1;
+      h->ivf.search_n_center = 1;
+    }
     const hora_ivfpq_params &p = h->ivf;
     if (dim > 1024) {
       delete h;
@@ -308,6 +327,8 @@ int hora_build(hora_index *h, int metric) {
     HORA_CUDA_TRY(cudaStreamSynchronize(h->stream));
     return HORA_OK;
   }
+  if (h->kind == HORA_INDEX_PQ && metric == M_COS)
+    return fail(HORA_EMETRIC, "PQIndex: CosineSimilarity is not supported (NaN in the reference)");
   int rc = ivf_build(h);
   h->built = rc == HORA_OK;
   return rc;
@@ -420,9 +441,13 @@ int hora_search_nodes(hora_index *h, const float *queries, uint64_t nq, uint64_t
   return search_common(h, queries, nq, k, 0, ids_out, dist_out, vecs_out);
 }
 
+static const char *index_name(int kind) {
+  return kind == HORA_INDEX_BRUTE_FORCE ? "BruteForceIndex" : kind == HORA_INDEX_PQ ? "PQIndex" : "IVFPQIndex";
+}
+
 int hora_name(const hora_index *h, const char **out) {
   if (!h || !out) return fail(HORA_EINVAL, "null argument");
-  *out = h->kind == HORA_INDEX_BRUTE_FORCE ? "BruteForceIndex" : "IVFPQIndex";
+  *out = index_name(h->kind);
   return HORA_OK;
 }
 
@@ -454,7 +479,7 @@ int hora_clear(hora_index *h) {
 int hora_idx_info(const hora_index *h, char *buf, uint64_t cap) {
   if (!h || !buf || cap == 0) return fail(HORA_EINVAL, "null argument");
   std::string s = "{";
-  s += std::string("\"name\":\"") + (h->kind == HORA_INDEX_BRUTE_FORCE ? "BruteForceIndex" : "IVFPQIndex") + "\"";
+  s += std::string("\"name\":\"") + index_name(h->kind) + "\"";
   s += ",\"dimension\":" + std::to_string(h->dim);
   s += ",\"nodes\":" + std::to_string(h->n);
   s += std::string(",\"metric\":\"") + metric_name(h->metric) + "\"";
@@ -467,7 +492,7 @@ int hora_idx_info(const hora_index *h, char *buf, uint64_t cap) {
                                              h->xsq64.bytes + ivf_device_bytes(h));
   s += ",\"last_search_ms\":" + std::to_string(h->last_ms.load());
   s += ",\"last_overflow_rescans\":" + std::to_string(h->last_retries.load());
-  if (h->kind == HORA_INDEX_IVFPQ) {
+  if (h->kind != HORA_INDEX_BRUTE_FORCE) {
     std::string iv;
     ivf_info(h, iv);
     s += ",\"ivfpq\":" + iv;
@@ -509,7 +534,7 @@ int hora_dump(hora_index *h, const char *path) {
   }
   ok = ok && (n == 0 || (std::fwrite(rows.data(), 4, rows.size(), f) == rows.size() &&
                          std::fwrite(ids.data(), 8, n, f) == n));
-  if (ok && h->kind == HORA_INDEX_IVFPQ) ok = ivf_dump(h, f) == HORA_OK;
+  if (ok && h->kind != HORA_INDEX_BRUTE_FORCE && h->built) ok = ivf_dump(h, f) == HORA_OK;
   std::fclose(f);
   return ok ? HORA_OK : fail(HORA_EIO, std::string("unable to write file ") + path);
 }
@@ -529,12 +554,14 @@ int hora_load(const char *path, hora_index **out) {
             std::fread(&dim, 8, 1, f) == 1 && std::fread(&metric, 4, 1, f) == 1 &&
             std::fread(&built, 4, 1, f) == 1 && std::fread(&n, 8, 1, f) == 1 &&
             std::fread(&ivf, sizeof(ivf), 1, f) == 1 && std::fread(opts, sizeof(opts), 1, f) == 1;
-  if (!ok || dim == 0 || dim >= (1ull << 20) || n >= UINT32_MAX || kind > 1) {
+  if (!ok || dim == 0 || dim >= (1ull << 20) || n >= UINT32_MAX || kind > HORA_INDEX_PQ) {
     std::fclose(f);
     return fail(HORA_EIO, "corrupt index file");
   }
   hora_index *h = nullptr;
-  int rc = hora_index_create((int)kind, dim, kind == HORA_INDEX_IVFPQ ? &ivf : nullptr, &h);
+  hora_pq_params pq{ivf.n_sub, ivf.sub_bits, ivf.train_epoch};
+  const void *params = kind == HORA_INDEX_IVFPQ ? (const void *)&ivf : kind == HORA_INDEX_PQ ? (const void *)&pq : nullptr;
+  int rc = hora_index_create((int)kind, dim, params, &h);
   if (rc) {
     std::fclose(f);
     return rc;
@@ -556,7 +583,7 @@ int hora_load(const char *path, hora_index **out) {
     return rc ? rc : fail(HORA_EIO, "corrupt index file");
   }
   h->metric = (int)metric;
-  if (kind == HORA_INDEX_IVFPQ && built) {
+  if (kind != HORA_INDEX_BRUTE_FORCE && built) {
     rc = ivf_load(h, f);
     if (rc) {
       std::fclose(f);

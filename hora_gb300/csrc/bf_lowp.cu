@@ -694,7 +694,8 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   p.r_begin = 0;
   p.r_end = c0;
   HORA_TRY(launch_lp(prec, h->metric, TILE_DENSE, ta, L, p, s));
-  HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, (int)c0, nullptr, nq, flags, ovc, s));
+  // bestR is an intermediate list: only its R-th key (the threshold) needs its place
+  HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, (int)c0, nullptr, nq, flags, ovc, s, false));
   int64_t done = c0;
   const int64_t max_chunk = (int64_t)60000 * kLpBN * kLpTilesPerCta;
   while (done < n) {
@@ -705,7 +706,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     p.r_begin = done;
     p.r_end = done + c;
     HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, ta, L, p, s));
-    HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s));
+    HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s, false));
     done += c;
   }
   // overflow rescans over gathered query rows

@@ -43,6 +43,9 @@ struct IvfState {
   std::vector<int64_t> h_offsets;
   std::vector<uint8_t> h_trained;
   int64_t max_list = 0;
+  // metric of the PQ stages: Euclidean inside an IVF-PQ index (pq_idx.rs:71),
+  // the build metric for a flat PQIndex (pq_idx.rs:198-202)
+  int pq_metric = M_L2;
 };
 
 void ivf_state_free(IvfState *p) { delete p; }
@@ -292,15 +295,35 @@ __global__ void residual_gather_kernel(const float *X, int64_t ld, const float *
     z[u] = u < sl[m] ? __fsub_rn(X[r * ld + sb[m] + u], centers[c * ld + sb[m] + u]) : 0.0f;
 }
 
-template <int DM>
-__device__ __forceinline__ float l2_sub(const float *a, const float *b) {
+// metric(z, c) over a DM-wide sub-vector in dimension order (the padding
+// beyond the subspace's length is zero on both sides and adds exact zeros)
+template <int MT, int DM>
+__device__ __forceinline__ float sub_dist(const float *a, const float *b) {
   float s = 0.0f;
 #pragma unroll
-  for (int u = 0; u < DM; ++u) {
-    float t = __fsub_rn(a[u], b[u]);
-    s = __fadd_rn(s, __fmul_rn(t, t));
-  }
+  for (int u = 0; u < DM; ++u) s = dist_op<MT>(s, a[u], b[u]);
   return s;
+}
+
+// Kmeans::search_data's argmin (kmeans.rs:127-148): strict '<' from centre 0
+template <int MT, int DM>
+__device__ __forceinline__ int sub_argmin(const float *z, const float *cent, int K) {
+  int best = 0;
+  float bd = sub_dist<MT, DM>(z, cent);
+  for (int j = 1; j < K; ++j) {
+    const float d = sub_dist<MT, DM>(z, cent + j * DM);
+    if (d < bd) {
+      bd = d;
+      best = j;
+    }
+  }
+  return best;
+}
+
+template <int DM>
+__device__ __forceinline__ int sub_argmin_mt(int mt, const float *z, const float *cent, int K) {
+  return mt == M_L1 ? sub_argmin<M_L1, DM>(z, cent, K)
+                    : mt == M_IP ? sub_argmin<M_IP, DM>(z, cent, K) : sub_argmin<M_L2, DM>(z, cent, K);
 }
 
 // One CTA per (list, subspace) instance: Kmeans::train on the list's
@@ -308,8 +331,8 @@ __device__ __forceinline__ float l2_sub(const float *a, const float *b) {
 template <int DM>
 __global__ void __launch_bounds__(256) pq_kmeans_kernel(
     const float *Z, int64_t npos, const int64_t *toff, int M, int K, const int *sl, int epochs,
-    uint64_t seed, int accum_f64, uint8_t *asg_g, uint32_t *mem_g, float *books, uint8_t *trained,
-    int *status) {
+    uint64_t seed, int accum_f64, int mt, uint8_t *asg_g, uint32_t *mem_g, float *books,
+    uint8_t *trained, int *status) {
   extern __shared__ __align__(16) float sm[];
   float *cent = sm;                                  // K x DM
   int64_t *cnt = reinterpret_cast<int64_t *>(cent + K * DM + (K * DM) % 2);  // K
@@ -361,16 +384,7 @@ __global__ void __launch_bounds__(256) pq_kmeans_kernel(
       float zi[DM];
 #pragma unroll
       for (int u = 0; u < DM; ++u) zi[u] = z[i * DM + u];
-      int best = 0;
-      float bd = l2_sub<DM>(zi, cent);
-      for (int j = 1; j < K; ++j) {
-        float d = l2_sub<DM>(zi, cent + j * DM);
-        if (d < bd) {
-          bd = d;
-          best = j;
-        }
-      }
-      asg[i] = (uint8_t)best;
+      asg[i] = (uint8_t)sub_argmin_mt<DM>(mt, zi, cent, K);
     }
     __syncthreads();
     // update_center: per centre, members in item order.  The members are
@@ -501,7 +515,7 @@ __global__ void __launch_bounds__(256) pq_kmeans_kernel(
 template <int DM>
 __global__ void __launch_bounds__(256) pq_encode_kernel(
     const float *X, int64_t ld, const float *centers, const uint32_t *items, const int64_t *offs,
-    const float *books, int M, int K, const int *sb, const int *sl, uint8_t *codes) {
+    const float *books, int M, int K, const int *sb, const int *sl, int mt, uint8_t *codes) {
   extern __shared__ __align__(16) float cb[];  // K x DM
   const int c = blockIdx.x, m = blockIdx.y;
   const int64_t lo = offs[c], n = offs[c + 1] - lo;
@@ -516,16 +530,7 @@ __global__ void __launch_bounds__(256) pq_encode_kernel(
 #pragma unroll
     for (int u = 0; u < DM; ++u)
       zi[u] = u < len ? __fsub_rn(X[r * ld + b + u], centers[(int64_t)c * ld + b + u]) : 0.0f;
-    int best = 0;
-    float bd = l2_sub<DM>(zi, cb);
-    for (int j = 1; j < K; ++j) {
-      float d = l2_sub<DM>(zi, cb + j * DM);
-      if (d < bd) {
-        bd = d;
-        best = j;
-      }
-    }
-    codes[(lo + i) * M + m] = (uint8_t)best;
+    codes[(lo + i) * M + m] = (uint8_t)sub_argmin_mt<DM>(mt, zi, cb, K);
   }
 }
 
@@ -715,9 +720,10 @@ __device__ __forceinline__ float adc_row(const uint8_t *code, const float *lut, 
   return d;
 }
 
-// LUT[m][j] = sum_t (z_t - C[m][j][t])^2 in t order (pq_idx.rs:170-179); the
-// DM floats of a codeword are one aligned vector load.
-template <int DM>
+// LUT[m][j] = metric(z[range_m], C[m][j]) in t order (pq_idx.rs:170-179):
+// Euclidean inside IVF-PQ, the build metric for a flat PQIndex; the DM floats
+// of a codeword are one aligned vector load.
+template <int MT, int DM>
 __device__ __forceinline__ float lut_entry(const float *cj, const float *zq, int len) {
   float c[DM];
   if (DM % 4 == 0) {
@@ -739,12 +745,8 @@ __device__ __forceinline__ float lut_entry(const float *cj, const float *zq, int
   }
   float s = 0.0f;
 #pragma unroll
-  for (int u = 0; u < DM; ++u) {
-    if (u < len) {
-      const float t = __fsub_rn(zq[u], c[u]);
-      s = __fadd_rn(s, __fmul_rn(t, t));
-    }
-  }
+  for (int u = 0; u < DM; ++u)
+    if (u < len) s = dist_op<MT>(s, zq[u], c[u]);
   return s;
 }
 
@@ -756,7 +758,7 @@ __global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
     const float *Q, int64_t ldq, const float *centers, int64_t ldc, const float *books,
     const uint8_t *codes, const uint32_t *items, const int64_t *offs, const uint8_t *trained,
     const uint32_t *pq, const uint32_t *pc, const uint32_t *pslot, int64_t npairs, int per, int M,
-    int K, const int *sb, const int *sl, int kk, int pmax, uint64_t *cand) {
+    int K, const int *sb, const int *sl, int mt, int kk, int pmax, uint64_t *cand) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float *lut = reinterpret_cast<float *>(smraw);                       // M x K
   uint32_t *hist = reinterpret_cast<uint32_t *>(lut + M * K);          // kSelBins
@@ -790,9 +792,21 @@ __global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
       zq[t] = __fsub_rn(Q[q * ldq + t], centers[(int64_t)c * ldc + t]);
     __syncthreads();
     const float *book = books + (int64_t)c * M * K * DM;
-    for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
-      const int m = e >> kbits;
-      lut[e] = lut_entry<DM>(book + (int64_t)e * DM, zq + sbs[m], sls[m]);
+    if (mt == M_L2) {
+      for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
+        const int m = e >> kbits;
+        lut[e] = lut_entry<M_L2, DM>(book + (int64_t)e * DM, zq + sbs[m], sls[m]);
+      }
+    } else if (mt == M_L1) {
+      for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
+        const int m = e >> kbits;
+        lut[e] = lut_entry<M_L1, DM>(book + (int64_t)e * DM, zq + sbs[m], sls[m]);
+      }
+    } else {
+      for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
+        const int m = e >> kbits;
+        lut[e] = lut_entry<M_IP, DM>(book + (int64_t)e * DM, zq + sbs[m], sls[m]);
+      }
     }
     __syncthreads();
     // scan in chunks; running kk best kept at the head of dkeys/rows
@@ -885,7 +899,7 @@ static int launch_pq_kmeans(IvfState &v, const float *Z, int64_t npos, const int
   HORA_CUDA_TRY(cudaFuncSetAttribute(pq_kmeans_kernel<DM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   ProfScope ps("pq_kmeans", s);
   pq_kmeans_kernel<DM><<<(unsigned)(v.n_list * v.n_sub), 256, smem, s>>>(
-      Z, npos, toff, (int)v.n_sub, (int)v.K, v.sub_len_d.as<int>(), epochs, seed, accum, asg, mem,
+      Z, npos, toff, (int)v.n_sub, (int)v.K, v.sub_len_d.as<int>(), epochs, seed, accum, v.pq_metric, asg, mem,
       v.books.as<float>(), v.trained.as<uint8_t>(), status);
   HORA_LAUNCHED();
   return HORA_OK;
@@ -899,7 +913,7 @@ static int launch_pq_encode(IvfState &v, const float *X, int64_t ld, cudaStream_
   pq_encode_kernel<DM><<<grid, 256, smem, s>>>(X, ld, v.centers.as<float>(), v.items.as<uint32_t>(),
                                                v.offsets.as<int64_t>(), v.books.as<float>(),
                                                (int)v.n_sub, (int)v.K, v.sub_begin_d.as<int>(),
-                                               v.sub_len_d.as<int>(), v.codes.as<uint8_t>());
+                                               v.sub_len_d.as<int>(), v.pq_metric, v.codes.as<uint8_t>());
   HORA_LAUNCHED();
   return HORA_OK;
 }
@@ -916,6 +930,7 @@ static int encode_all(hora_index *h, IvfState &v, cudaStream_t s) {
 }
 
 static void init_layout(hora_index *h, IvfState &v) {
+  v.pq_metric = h->kind == HORA_INDEX_PQ ? h->metric : M_L2;
   v.n_list = (int64_t)h->ivf.n_kmeans_center;
   v.n_sub = (int64_t)h->ivf.n_sub;
   v.sub_bits = (int64_t)h->ivf.sub_bits;
@@ -1015,8 +1030,10 @@ int ivf_build(hora_index *h) {
   uint64_t *d_rng = state.as<uint64_t>();
   int *d_status = reinterpret_cast<int *>(state.as<char>() + 8);
 
-  // ---- coarse k-means on the first T items ----
-  {
+  // ---- coarse k-means on the first T items (a flat PQIndex has one list
+  //      centred at zero: no coarse stage, residual = the vector itself) ----
+  const bool flat = h->kind == HORA_INDEX_PQ;
+  if (!flat) {
     ProfScope ps("coarse_init", s);
     coarse_init_kernel<<<ceil_div(h->dim, 128), 128, 0, s>>>(X, h->ld, T, h->dim, C, h->accum_f64,
                                                              v.centers.as<float>());
@@ -1029,7 +1046,7 @@ int ivf_build(hora_index *h) {
     HORA_TRY(ensure_norms(h, s));
     HORA_TRY(v.cnorm.reserve(sizeof(float) * C));
   }
-  for (int ep = 0; ep < epochs; ++ep) {
+  for (int ep = 0; ep < (flat ? 0 : epochs); ++ep) {
     if (h->metric == M_COS)
       HORA_TRY(launch_row_norms(v.centers.as<float>(), C, h->ld, h->dim, v.cnorm.as<float>(), nullptr, s));
     TileParams p;
@@ -1183,7 +1200,7 @@ static int launch_adc_vb(IvfState &v, SearchWorkspace &ws, const float *Q, int64
       Q, ldq, v.centers.as<float>(), ldc, v.books.as<float>(), v.codes.as<uint8_t>(),
       v.items.as<uint32_t>(), v.offsets.as<int64_t>(), v.trained.as<uint8_t>(), ws.pair_q.as<uint32_t>(),
       ws.pair_c.as<uint32_t>(), ws.pair_slot.as<uint32_t>(), npairs, per, (int)v.n_sub, (int)v.K,
-      v.sub_begin_d.as<int>(), v.sub_len_d.as<int>(), kk, pmax, cand);
+      v.sub_begin_d.as<int>(), v.sub_len_d.as<int>(), v.pq_metric, kk, pmax, cand);
   HORA_LAUNCHED();
   return HORA_OK;
 }
@@ -1364,7 +1381,7 @@ int ivf_search_keys(hora_index *h, int64_t nq, int k, int64_t nprobe, const uint
 
 int ivf_layout(const hora_index *h, uint64_t *n_list, uint64_t *n_sub, uint64_t *sub_bits,
                uint64_t *dmax) {
-  if (h->kind != HORA_INDEX_IVFPQ) return fail(HORA_EINVAL, "not an IVF-PQ index");
+  if (h->kind == HORA_INDEX_BRUTE_FORCE) return fail(HORA_EINVAL, "not a PQ index");
   int64_t sd = (int64_t)h->dim / (int64_t)h->ivf.n_sub;
   if (n_list) *n_list = h->ivf.n_kmeans_center;
   if (n_sub) *n_sub = h->ivf.n_sub;
@@ -1375,7 +1392,7 @@ int ivf_layout(const hora_index *h, uint64_t *n_list, uint64_t *n_sub, uint64_t 
 
 int ivf_export(const hora_index *h, float *centers, int64_t *offsets, int64_t *items,
                float *codebooks, uint8_t *codes, uint8_t *trained) {
-  if (h->kind != HORA_INDEX_IVFPQ) return fail(HORA_EINVAL, "not an IVF-PQ index");
+  if (h->kind == HORA_INDEX_BRUTE_FORCE) return fail(HORA_EINVAL, "not a PQ index");
   if (!h->ivfs) return fail(HORA_ENOTBUILT, "index not built");
   const IvfState &v = *h->ivfs;
   const int64_t C = v.n_list, n = v.n_items;

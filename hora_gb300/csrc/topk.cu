@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kMergeThreads) merge_topk_kernel(
 // still needed (usually once the distance bits are resolved).
 __global__ void __launch_bounds__(kSelectThreads) merge_select_kernel(
     uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n,
-    uint8_t *ovf_flag, uint32_t *ovf_counter) {
+    uint8_t *ovf_flag, uint32_t *ovf_counter, int sorted) {
   extern __shared__ uint64_t sk[];
   __shared__ uint32_t hist[kSelBins];
   __shared__ int sc[8];  // [0] live, [1] digit, [2] below, [3] taken, [4] remaining, [5] at digit
@@ -218,16 +218,44 @@ __global__ void __launch_bounds__(kSelectThreads) merge_select_kernel(
       }
     }
     __syncthreads();
-    int P = 1;
-    while (P < want) P <<= 1;
-    for (int i = want + threadIdx.x; i < P; i += blockDim.x) sel[i] = kEmptyKey;
-    __syncthreads();
-    if (P <= 512) {
-      if (warp == 0) warp_bitonic_sort(sel, P);
+    if (sorted) {
+      int P = 1;
+      while (P < want) P <<= 1;
+      for (int i = want + threadIdx.x; i < P; i += blockDim.x) sel[i] = kEmptyKey;
       __syncthreads();
-    } else {
-      block_bitonic_sort(sel, P);
+      if (P <= 512) {
+        if (warp == 0) warp_bitonic_sort(sel, P);
+        __syncthreads();
+      } else {
+        block_bitonic_sort(sel, P);
+      }
+    } else if (warp == 0) {
+      // unordered winners: only the largest must sit last (it is the
+      // scan's threshold); keys are distinct, so one position holds it
+      uint64_t mx = 0;
+      int at = 0;
+      for (int i = lane; i < want; i += 32)
+        if (sel[i] >= mx) {
+          mx = sel[i];
+          at = i;
+        }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t m2 = __shfl_xor_sync(0xffffffffu, mx, o);
+        const int a2 = __shfl_xor_sync(0xffffffffu, at, o);
+        if (m2 > mx) {
+          mx = m2;
+          at = a2;
+        }
+      }
+      if (lane == 0 && at != want - 1) {
+        const uint64_t t = sel[want - 1];
+        sel[want - 1] = mx;
+        sel[at] = t;
+      }
+      __syncwarp();
     }
+    __syncthreads();
   }
   for (int i = threadIdx.x; i < k; i += blockDim.x) bq[i] = i < want ? sel[i] : kEmptyKey;
   if (threadIdx.x == 0) {
@@ -329,7 +357,7 @@ int merge_smem_bytes(int k, int cap) {
 
 int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap,
                       int dense_n, const int *qlist, int64_t nlist, uint8_t *ovf_flag,
-                      uint32_t *ovf_counter, cudaStream_t s) {
+                      uint32_t *ovf_counter, cudaStream_t s, bool sorted) {
   if (nlist <= 0) return HORA_OK;
   static bool attr = false;
   if (!attr) {
@@ -354,7 +382,7 @@ int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *cou
     if (smem <= 200 * 1024) {
       ProfScope ps("topk_merge", s);
       merge_select_kernel<<<(unsigned)nlist, kSelectThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
-                                                                       ovf_flag, ovf_counter);
+                                                                       ovf_flag, ovf_counter, sorted ? 1 : 0);
       HORA_LAUNCHED();
       return HORA_OK;
     }

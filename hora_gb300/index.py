@@ -18,7 +18,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from ._lib import IVFPQParamsC, check, lib
+from ._lib import IVFPQParamsC, PQParamsC, check, lib
 
 NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
 
@@ -90,6 +90,27 @@ class IVFPQParams:
 
 
 @dataclass
+class PQParams:
+    """PQParams with the reference defaults (src/index/pq_params.rs:32-41)
+    and its consuming builder setters (:15-30)."""
+    n_sub: int = 4
+    sub_bits: int = 4
+    train_epoch: int = 100
+
+    def with_n_sub(self, v):
+        self.n_sub = v
+        return self
+
+    def with_sub_bits(self, v):
+        self.sub_bits = v
+        return self
+
+    def with_train_epoch(self, v):
+        self.train_epoch = v
+        return self
+
+
+@dataclass
 class Node:
     """core::node::Node: a vector and its optional id (src/core/node.rs:93-97)."""
     vectors: np.ndarray
@@ -118,6 +139,9 @@ class _Index:
         if isinstance(params, IVFPQParams):
             self._cp = IVFPQParamsC(params.n_sub, params.sub_bits, params.n_kmeans_center,
                                     params.search_n_center, params.train_epoch)
+            p = C.cast(C.pointer(self._cp), C.c_void_p)
+        elif isinstance(params, PQParams):
+            self._cp = PQParamsC(params.n_sub, params.sub_bits, params.train_epoch)
             p = C.cast(C.pointer(self._cp), C.c_void_p)
         check(lib().hora_index_create(self.kind, dimension, p, C.byref(self._h)))
 
@@ -318,6 +342,16 @@ class IVFPQIndex(_Index):
 
 
 PQIVFIndex = IVFPQIndex
+
+
+class PQIndex(IVFPQIndex):
+    """PQIndex<f32, u64> (src/index/pq_idx.rs:21-265): product quantization of
+    the raw vectors, codebooks trained with the build metric, every item
+    scanned by ADC.  layout()/export() report one list centred at zero."""
+    kind = 2
+
+    def __init__(self, dimension: int, params: PQParams | None = None, _handle=None):
+        _Index.__init__(self, dimension, params if params is not None else PQParams(), _handle)
 
 
 class Server:

@@ -73,7 +73,8 @@ typedef enum {
 typedef enum {
   HORA_INDEX_BRUTE_FORCE = 0, /* BruteForceIndex */
   HORA_INDEX_IVFPQ = 1,       /* IVFPQIndex */
-  HORA_INDEX_PQIVF = 1        /* README name of the same index */
+  HORA_INDEX_PQIVF = 1,       /* README name of the same index */
+  HORA_INDEX_PQ = 2           /* PQIndex (flat; src/index/pq_idx.rs:21-265) */
 } hora_index_kind;
 
 /* Scoring precision of brute-force search (GPU-only knob).  The approximate
@@ -99,6 +100,13 @@ typedef struct {
   uint64_t train_epoch;     /* default 100 */
 } hora_ivfpq_params;
 
+/* PQParams (src/index/pq_params.rs:8-41). */
+typedef struct {
+  uint64_t n_sub;       /* default 4   */
+  uint64_t sub_bits;    /* default 4   (1..8 supported: u8 codes) */
+  uint64_t train_epoch; /* default 100 */
+} hora_pq_params;
+
 /* GPU-only options, set per handle with hora_set_option(key, value). */
 typedef enum {
   HORA_OPT_PRECISION = 1,      /* hora_precision for brute force, default FP32 */
@@ -119,11 +127,15 @@ typedef enum {
 typedef struct hora_index hora_index;
 
 /* ---- lifecycle --------------------------------------------------------- */
-/* BruteForceIndex::new (bruteforce_idx.rs:25) / IVFPQIndex::new (pq_idx.rs:295).
- * params points to hora_bf_params or hora_ivfpq_params (NULL = defaults). */
+/* BruteForceIndex::new (bruteforce_idx.rs:25) / IVFPQIndex::new (pq_idx.rs:295)
+ * / PQIndex::new (pq_idx.rs:48-90).  params points to hora_bf_params,
+ * hora_ivfpq_params or hora_pq_params (NULL = defaults).  A PQIndex trains
+ * its codebooks on the raw vectors with the build metric (CosineSimilarity
+ * is rejected: the reference's metric is NaN there and its heap panics). */
 int hora_index_create(int kind, uint64_t dim, const void *params, hora_index **out);
 int hora_index_free(hora_index *h);
 void hora_ivfpq_params_default(hora_ivfpq_params *p); /* pq_params.rs:80-91 */
+void hora_pq_params_default(hora_pq_params *p);       /* pq_params.rs:32-41 */
 
 /* ---- ANNIndex ---------------------------------------------------------- */
 /* add_node / add / madd (ann_index.rs:36-59): n vectors with their ids. */
@@ -159,7 +171,8 @@ int hora_get_option(const hora_index *h, int key, double *out);
  * centers n_list x dim; offsets n_list+1; items n (row numbers in insertion
  * order); codebooks n_list x n_sub x 2^sub_bits x dmax; codes n x n_sub in
  * list order; trained n_list.  dmax = dim/n_sub + (dim % (dim/n_sub) != 0).
- * Any output pointer may be NULL. */
+ * Any output pointer may be NULL.  A PQIndex reports one list whose centre
+ * is the zero vector (its codebooks are trained on the raw vectors). */
 int hora_ivfpq_layout(const hora_index *h, uint64_t *n_list, uint64_t *n_sub,
                       uint64_t *sub_bits, uint64_t *dmax);
 int hora_ivfpq_export(const hora_index *h, float *centers, int64_t *offsets, int64_t *items,

@@ -66,6 +66,15 @@ struct IVFPQParams {
   IVFPQParams &train_epoch(uint64_t v) { p.train_epoch = v; return *this; }
 };
 
+// PQParams (src/index/pq_params.rs:8-41), same builder style.
+struct PQParams {
+  hora_pq_params p;
+  PQParams() { hora_pq_params_default(&p); }
+  PQParams &n_sub(uint64_t v) { p.n_sub = v; return *this; }
+  PQParams &sub_bits(uint64_t v) { p.sub_bits = v; return *this; }
+  PQParams &train_epoch(uint64_t v) { p.train_epoch = v; return *this; }
+};
+
 // ANNIndex<f32, T> for one library handle.
 template <class T>
 class ANNIndex {
@@ -190,5 +199,13 @@ class IVFPQIndex : public ANNIndex<T> {
 };
 template <class T>
 using PQIVFIndex = IVFPQIndex<T>;
+
+// PQIndex<f32, T> (src/index/pq_idx.rs:21-265): the flat product-quantized index.
+template <class T>
+class PQIndex : public ANNIndex<T> {
+ public:
+  PQIndex(uint64_t dimension, const PQParams &params = {})
+      : ANNIndex<T>(HORA_INDEX_PQ, dimension, &params.p) {}
+};
 
 }  // namespace hora

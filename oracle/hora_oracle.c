@@ -735,6 +735,101 @@ int horo_ivfpq_search(const float *centers, int64_t n_list, int64_t dim,
 }
 
 /* ------------------------------------------------------------------------ */
+/* Flat PQIndex — src/index/pq_idx.rs:21-265.  No residual; the build metric
+ * drives both the k-means (train_center, pq_idx.rs:122-149) and the LUT
+ * (get_distance_from_vec_range, pq_idx.rs:151-163).                       */
+
+int horo_pq_build(const float *data, int64_t n, int64_t dim, int64_t n_sub, int64_t sub_bits,
+                  int64_t n_epoch, int metric, uint64_t seed, int accum_f64, int64_t train_size,
+                  float *codebooks_out, uint8_t *codes_out) {
+  if (n <= 0 || n_sub <= 0 || dim < n_sub || sub_bits < 1 || sub_bits > 8) return -1;
+  int64_t T = (train_size > 0 && train_size < n) ? train_size : n;
+  int64_t K = (int64_t)1 << sub_bits, dmax = pq_dmax(dim, n_sub);
+  int64_t *b = (int64_t *)malloc(sizeof(int64_t) * (size_t)n_sub);
+  int64_t *e = (int64_t *)malloc(sizeof(int64_t) * (size_t)n_sub);
+  horo_pq_ranges(dim, n_sub, b, e);
+  memset(codebooks_out, 0, sizeof(float) * (size_t)(n_sub * K * dmax));
+  float *sub = (float *)malloc(sizeof(float) * (size_t)(K * dmax));
+  int64_t *a = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+  int rc = 0;
+  for (int64_t m = 0; m < n_sub; ++m) {
+    int64_t len = e[m] - b[m];
+    /* pq_idx.rs:136-141: Kmeans::new(.., self.mt), train on the items */
+    rc = horo_kmeans_train(data, T, dim, b[m], e[m], NULL, K, n_epoch, metric,
+                           horo_rng_instance_seed(seed, 1 + m), accum_f64, sub);
+    if (rc) break;
+    for (int64_t j = 0; j < K; ++j)
+      for (int64_t t = 0; t < len; ++t) codebooks_out[(m * K + j) * dmax + t] = sub[j * len + t];
+    /* pq_idx.rs:143-144: search_data with the same metric */
+    horo_kmeans_assign(data, n, dim, b[m], e[m], NULL, sub, K, metric, a);
+    for (int64_t i = 0; i < n; ++i) codes_out[i * n_sub + m] = (uint8_t)a[i];
+  }
+  free(a);
+  free(sub);
+  free(b);
+  free(e);
+  return rc;
+}
+
+typedef struct {
+  const float *codebooks, *queries;
+  const uint8_t *codes;
+  int64_t n, dim, n_sub, sub_bits, k;
+  int metric;
+  int64_t *idx_out;
+  float *dist_out;
+} pq_ctx;
+
+static void pq_range(void *p, int64_t lo, int64_t hi) {
+  pq_ctx *c = (pq_ctx *)p;
+  int64_t K = (int64_t)1 << c->sub_bits, dmax = pq_dmax(c->dim, c->n_sub);
+  int64_t *b = (int64_t *)malloc(sizeof(int64_t) * (size_t)c->n_sub);
+  int64_t *e = (int64_t *)malloc(sizeof(int64_t) * (size_t)c->n_sub);
+  horo_pq_ranges(c->dim, c->n_sub, b, e);
+  float *lut = (float *)malloc(sizeof(float) * (size_t)(c->n_sub * K));
+  nb_t *tmp = (nb_t *)malloc(sizeof(nb_t) * (size_t)(c->k + 1));
+  heap_t top;
+  heap_init(&top, 1024);
+  for (int64_t qi = lo; qi < hi; ++qi) {
+    const float *q = c->queries + qi * c->dim;
+    /* pq_idx.rs:170-179: LUT[m*K+j] = metric(q[range_m], C[m][j]) */
+    for (int64_t m = 0; m < c->n_sub; ++m)
+      for (int64_t j = 0; j < K; ++j)
+        lut[m * K + j] = horo_metric_f32(q + b[m], c->codebooks + (m * K + j) * dmax, e[m] - b[m],
+                                         c->metric, NULL);
+    /* pq_idx.rs:181-193: push every item, pop down to k */
+    top.len = 0;
+    for (int64_t i = 0; i < c->n; ++i) {
+      float d = 0.0f;
+      const uint8_t *code = c->codes + i * c->n_sub;
+      for (int64_t m = 0; m < c->n_sub; ++m) d += lut[m * K + code[m]];
+      nb_t x = {i, d};
+      heap_push(&top, x);
+    }
+    while (top.len > c->k) (void)heap_pop(&top);
+    int64_t m = 0;
+    while (top.len > 0) tmp[m++] = heap_pop(&top);
+    for (int64_t j = 0; j < c->k; ++j) {
+      c->idx_out[qi * c->k + j] = j < m ? tmp[m - 1 - j].idx : -1;
+      c->dist_out[qi * c->k + j] = j < m ? tmp[m - 1 - j].d : INFINITY;
+    }
+  }
+  heap_free(&top);
+  free(tmp);
+  free(lut);
+  free(b);
+  free(e);
+}
+
+int horo_pq_search(const float *codebooks, const uint8_t *codes, int64_t n, int64_t dim,
+                   int64_t n_sub, int64_t sub_bits, int metric, const float *queries, int64_t nq,
+                   int64_t k, int64_t *idx_out, float *dist_out, int threads) {
+  pq_ctx c = {codebooks, queries, codes, n, dim, n_sub, sub_bits, k, metric, idx_out, dist_out};
+  parallel_for(nq, threads, pq_range, &c);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* MLP oracle for the learned-nprobe gradient check (new; no reference
  * counterpart).  Double precision throughout.                              */
 

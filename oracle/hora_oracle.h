@@ -130,6 +130,16 @@ void horo_mlp_forward(const float *params, int64_t f, int64_t h1, int64_t h2, co
 double horo_mlp_loss_grad(const float *params, int64_t f, int64_t h1, int64_t h2, const float *x,
                           const float *y, int64_t n, float alpha, double *grad_out);
 
+
+/* Flat PQIndex (src/index/pq_idx.rs:21-265): codebooks [n_sub][K][dmax],
+ * codes [n][n_sub]; the build metric drives the k-means and the LUT. */
+int horo_pq_build(const float *data, int64_t n, int64_t dim, int64_t n_sub, int64_t sub_bits,
+                  int64_t n_epoch, int metric, uint64_t seed, int accum_f64, int64_t train_size,
+                  float *codebooks_out, uint8_t *codes_out);
+int horo_pq_search(const float *codebooks, const uint8_t *codes, int64_t n, int64_t dim,
+                   int64_t n_sub, int64_t sub_bits, int metric, const float *queries, int64_t nq,
+                   int64_t k, int64_t *idx_out, float *dist_out, int threads);
+
 #ifdef __cplusplus
 }
 #endif

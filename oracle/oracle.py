@@ -75,6 +75,10 @@ def lib():
         L.horo_ivfpq_search.argtypes = [f32p, i64, i64, i64p, i64p, f32p, u8p, u8p, i64, i64,
                                         C.c_int, f32p, i64, i64, i64, i64p, f32p, C.c_int]
         L.horo_ivf_coarse.argtypes = [f32p, i64, i64, C.c_int, f32p, f32p]
+        L.horo_pq_build.argtypes = [f32p, i64, i64, i64, i64, i64, C.c_int, C.c_uint64, C.c_int, i64,
+                                    f32p, u8p]
+        L.horo_pq_search.argtypes = [f32p, u8p, i64, i64, i64, i64, C.c_int, f32p, i64, i64, i64p,
+                                     f32p, C.c_int]
         L.horo_mlp_forward.argtypes = [f32p, i64, i64, i64, f32p, i64, f32p]
         L.horo_mlp_loss_grad.restype = C.c_double
         L.horo_mlp_loss_grad.argtypes = [f32p, i64, i64, i64, f32p, f32p, i64, C.c_float, f64p]
@@ -236,6 +240,32 @@ def ivfpq_build(data, n_sub, sub_bits, n_list, n_epoch, mt, seed, accum_f64=True
         raise RuntimeError(f"ivfpq build failed rc={rc}")
     return dict(centers=centers, offsets=offs, items=items, codebooks=books, codes=codes,
                 trained=trained, n_sub=n_sub, sub_bits=sub_bits, metric=mt)
+
+
+def pq_build(data, n_sub, sub_bits, n_epoch, mt, seed, accum_f64=True, train_size=0):
+    """Flat PQIndex build (pq_idx.rs:122-149): codebooks [n_sub, K, dmax], codes [n, n_sub]."""
+    data = _f32(data)
+    n, d = data.shape
+    K = 1 << sub_bits
+    books = np.empty((n_sub, K, pq_dmax(d, n_sub)), np.float32)
+    codes = np.empty((n, n_sub), np.uint8)
+    rc = lib().horo_pq_build(_p(data, f32p), n, d, n_sub, sub_bits, n_epoch, mt, seed, int(accum_f64),
+                             train_size, _p(books, f32p), _p(codes, u8p))
+    if rc:
+        raise RuntimeError(f"pq build failed rc={rc}")
+    return dict(codebooks=books, codes=codes, n_sub=n_sub, sub_bits=sub_bits, metric=mt, dim=d)
+
+
+def pq_search(ix, queries, k, threads=1):
+    """Flat PQIndex search_knn_adc (pq_idx.rs:165-193): ids ascending by ADC distance."""
+    queries = _f32(queries)
+    nq, d = queries.shape
+    idx = np.empty((nq, k), np.int64)
+    dist = np.empty((nq, k), np.float32)
+    lib().horo_pq_search(_p(ix["codebooks"], f32p), _p(ix["codes"], u8p), ix["codes"].shape[0], d,
+                         ix["n_sub"], ix["sub_bits"], ix["metric"], _p(queries, f32p), nq, k,
+                         _p(idx, i64p), _p(dist, f32p), threads)
+    return idx, dist
 
 
 def pq_encode(data, list_center, codebook, n_sub, sub_bits):

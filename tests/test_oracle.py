@@ -159,6 +159,34 @@ def test_ivfpq_nprobe_all_equals_flat_adc(oracle):
         np.testing.assert_array_equal(qd[qn], np.array([t[0] for t in ds[:10]], np.float32))
 
 
+@pytest.mark.parametrize("mt", [3, 1, 2])
+def test_flat_pq_is_adc_over_its_own_codes(oracle, mt):
+    # PQIndex (pq_idx.rs:122-193): every code is the metric's argmin over its
+    # subspace's codebook, and search returns the k smallest sequential ADC
+    # sums with LUT[m][j] = metric(q[range_m], C[m][j])
+    rng = np.random.default_rng(mt)
+    X = rng.standard_normal((600, 12)).astype(np.float32)
+    ix = oracle.pq_build(X, 3, 3, 4, mt, 7)
+    b, e = oracle.pq_ranges(12, 3)
+    books, codes = ix["codebooks"], ix["codes"]
+    for i in range(0, 600, 37):
+        for m in range(3):
+            d = [oracle.metric(X[i, b[m]:e[m]], books[m, j, :e[m] - b[m]], mt) for j in range(8)]
+            assert codes[i, m] == int(np.argmin(d))  # first minimum, as the strict '<' scan
+    q = rng.standard_normal((4, 12)).astype(np.float32)
+    qi, qd = oracle.pq_search(ix, q, 6)
+    for n in range(4):
+        lut = [[oracle.metric(q[n, b[m]:e[m]], books[m, j, :e[m] - b[m]], mt) for j in range(8)]
+               for m in range(3)]
+        ds = []
+        for r in range(600):
+            d = np.float32(0)
+            for m in range(3):
+                d = np.float32(d + np.float32(lut[m][codes[r, m]]))
+            ds.append(d)
+        np.testing.assert_array_equal(qd[n], np.sort(np.array(ds, np.float32))[:6])
+
+
 def test_mlp_grad_finite_difference(oracle):
     rng = np.random.default_rng(5)
     f, h1, h2 = 6, 5, 4
