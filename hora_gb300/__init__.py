@@ -9,8 +9,8 @@ errors when the library is missing; there is no CPU fallback.
 from ._lib import HoraError, launches, lib  # noqa: F401
 from .index import (NO_ID, BruteForceIndex, BruteForceParams, IVFPQIndex,  # noqa: F401
                     IVFPQParams, Metric, Node, Option, PQIndex, PQIVFIndex, PQParams, Precision,
-                    Server)
+                    Server, load_reference)
 
 __all__ = ["BruteForceIndex", "BruteForceParams", "IVFPQIndex", "PQIVFIndex", "IVFPQParams",
-           "PQIndex", "PQParams",
+           "PQIndex", "PQParams", "load_reference",
            "Metric", "Node", "Option", "Precision", "Server", "HoraError", "NO_ID", "lib", "launches"]

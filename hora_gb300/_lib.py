@@ -56,6 +56,7 @@ SIGNATURES = {
     "hora_profile_report": (C.c_int, [C.c_char_p, u64]),
     "hora_ivfpq_params_default": (None, [C.POINTER(IVFPQParamsC)]),
     "hora_pq_params_default": (None, [C.POINTER(PQParamsC)]),
+    "hora_load_reference": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(vp)]),
     "hora_index_create": (C.c_int, [C.c_int, u64, vp, C.POINTER(vp)]),
     "hora_index_free": (C.c_int, [vp]),
     "hora_add": (C.c_int, [vp, vp, vp, u64]),

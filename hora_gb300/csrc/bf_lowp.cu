@@ -15,13 +15,15 @@
 // has no tensor-core form and always runs exactly on the CUDA cores.
 //
 // Kernel layout: CTA = 18 warps over 128 queries x 4,096 rows.  Warp 0
-// issues TMA loads (the query tile once, then a 4-8 deep ring of 128-row base
-// tiles), warp 1 owns TMEM (4 accumulator buffers of 128 columns) and issues
-// tcgen05.mma per tile, warps 2-17 drain the accumulators with tcgen05.ld (one
-// query row per TMEM lane, 32 columns per warp; the buffer is released as
-// soon as it is in registers), test the slice's extreme against the query's
-// current R-th key and, on a hit, stage the keys in shared memory (flushed to
-// the query's list 8 at a time, one atomic per flush).  Every mbarrier
+// issues TMA loads (the query tile once, then a ring of 256-row base tiles),
+// warp 1 owns TMEM (2 accumulator buffers of 256 columns) and issues one
+// 128 x 256 tcgen05.mma per K step (a 256-wide N reads the query operand from
+// shared memory once per 256 rows), warps 2-17 drain the accumulators with
+// tcgen05.ld (one query row per TMEM lane, two 32-column slices per warp; the
+// buffer is released once the last slice is in registers), test a slice's
+// extreme against the query's current R-th key and, on a hit, stage the keys
+// in shared memory (flushed to the query's list 8 at a time, one atomic per
+// flush).  Every mbarrier
 // wait is bounded; a CTA that gives up raises an error flag read by the host,
 // waits for its MMAs and frees TMEM.
 #include <cuda_bf16.h>
@@ -37,11 +39,12 @@
 namespace hora {
 
 constexpr int kLpBM = 128;           // queries per CTA (TMEM lanes)
-constexpr int kLpBN = 128;           // base rows per tile (accumulator columns)
-constexpr int kLpNB = 4;             // TMEM accumulator buffers (4 x 128 columns)
+constexpr int kLpBN = 256;           // base rows per tile (accumulator columns, MMA N)
+constexpr int kLpNB = 2;             // TMEM accumulator buffers (2 x 256 columns)
 constexpr int kLpThreads = 576;      // 18 warps
 constexpr int kLpEpiThreads = 512;   // warps 2..17
-constexpr int kLpTilesPerCta = 32;   // 4,096 rows per CTA
+constexpr int kLpTilesPerCta = 16;   // 4,096 rows per CTA
+constexpr int kLpSlices = kLpBN / 4 / 32;  // 32-column slices per drain warp and tile
 constexpr int kLpMaxStages = 8;
 // Filter-mode hits are staged per drain thread in shared memory and
 // appended to the query's global list kLpHitBuf at a time (one atomic per
@@ -312,7 +315,17 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     int nb = 0;  // keys staged in this thread's column
     for (int t = 0; t < T; ++t) {
       const int b = t % kLpNB, jb = t / kLpNB;
-      c.rt = row0 + (int64_t)t * kLpBN + h * 32;
+      const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full + b, jb & 1, abort));
+      if (!ok) break;
+      tc::fence_after_sync();
+      // this warp's 32-column slices of the tile, one at a time; the buffer
+      // goes back to the MMA as soon as the last slice is in registers
+#pragma unroll 1
+      for (int sl = 0; sl < kLpSlices; ++sl) {
+      // tcgen05.ld is warp-collective: lanes that skipped the previous
+      // slice's hit handling wait here for the others
+      __syncwarp();
+      c.rt = row0 + (int64_t)t * kLpBN + (h * kLpSlices + sl) * 32;
       // generic forms: this lane's row factor, broadcast by shuffle below
       float xa = 0.0f, xs = 1.0f;
       if (!FAST) {
@@ -321,15 +334,13 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         if (va) xa = r < p.r_end ? __ldg(va + r) : 0.0f;
         if (PREC == HORA_PREC_FP8) xs = r < p.r_end ? __ldg(p.xscale + r) : 0.0f;
       }
-      const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full + b, jb & 1, abort));
-      if (!ok) break;
-      tc::fence_after_sync();
       uint32_t v[32];
-      tc::tmem_ld32(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + h * 32), v);
+      tc::tmem_ld32(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + (h * kLpSlices + sl) * 32), v);
       tc::tmem_ld_wait();
-      // the accumulator is in registers: hand the TMEM buffer back at once
-      tc::fence_before_sync();
-      tc::mbar_arrive(acc_empty + b);
+      if (sl == kLpSlices - 1) {
+        tc::fence_before_sync();
+        tc::mbar_arrive(acc_empty + b);
+      }
       if (FAST) {
         if (qid < 0) continue;
         if constexpr (MODE == TILE_DENSE) {
@@ -379,6 +390,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       }
       if (MODE == TILE_DENSE) hits = 0xffffffffu;
       if (qid >= 0 && hits) drain_mask<MT, MODE, false>(v, hits, c, nb);
+      }
     }
     if (qid >= 0 && nb > 0) flush_hits(c, nb);
   }
@@ -701,7 +713,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   while (done < n) {
     double grow = (double)cap / (4.0 * R);
     int64_t c = (int64_t)((double)done * std::max(grow, 1.0));
-    c = std::max<int64_t>(c, (int64_t)kLpBN * 64);
+    c = std::max<int64_t>(c, (int64_t)8192);
     c = std::min<int64_t>(round_up(c, kLpBN), std::min<int64_t>(n - done, max_chunk));
     p.r_begin = done;
     p.r_end = done + c;

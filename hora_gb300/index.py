@@ -354,6 +354,16 @@ class PQIndex(IVFPQIndex):
         _Index.__init__(self, dimension, params if params is not None else PQParams(), _handle)
 
 
+def load_reference(path: str, kind):
+    """SerializableIndex::load of a file the reference wrote (bincode of
+    BruteForceIndex / PQIndex / IVFPQIndex<f32, usize>); `kind` is the class."""
+    h = C.c_void_p()
+    check(lib().hora_load_reference(path.encode(), kind.kind, C.byref(h)))
+    obj = kind.__new__(kind)
+    _Index.__init__(obj, 0, None, _handle=h)
+    return obj
+
+
 class Server:
     """Continuous-batching request loop over built indexes (hora_server_*).
 

@@ -182,6 +182,15 @@ int hora_ivfpq_export(const hora_index *h, float *centers, int64_t *offsets, int
  * The parity hook for "PQ codes bit-exact given identical codebooks". */
 int hora_ivfpq_set_codebooks(hora_index *h, const float *centers, const float *codebooks);
 
+/* SerializableIndex::load (ann_index.rs:141-158) of a file the reference
+ * itself wrote with bincode (bruteforce_idx.rs:84-106, pq_idx.rs:243-265,
+ * 488-523), for BruteForceIndex / PQIndex / IVFPQIndex<f32, usize> (kind
+ * names the struct: bincode carries no type tag).  Vectors and ids are
+ * added; a trained PQ / IVF-PQ index takes the file's coarse centres and
+ * codebooks, its lists and codes are recomputed on the GPU and the lists are
+ * checked against the file's.  sub_bits above 8 is HORA_ECAP. */
+int hora_load_reference(const char *path, int kind, hora_index **out);
+
 /* Per-call nprobe override (search_n_center) for sweeps; 0 = the param. */
 int hora_search_nprobe(hora_index *h, const float *queries, uint64_t nq, uint64_t k,
                        uint64_t nprobe, uint64_t *ids_out, float *dist_out);

@@ -4,6 +4,7 @@ import ctypes as C
 import os
 import subprocess
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -41,6 +42,31 @@ def test_params_default_matches_reference(hora):
     # IVFPQParams::default (src/index/pq_params.rs:80-91)
     assert (p.n_sub, p.sub_bits, p.n_kmeans_center, p.search_n_center, p.train_epoch) == \
         (25, 4, 256, 8, 100)
+
+
+def test_pq_params_default_matches_reference(hora):
+    from hora_gb300._lib import PQParamsC
+    p = PQParamsC()
+    hora.lib().hora_pq_params_default(C.byref(p))
+    # PQParams::default (src/index/pq_params.rs:32-41)
+    assert (p.n_sub, p.sub_bits, p.train_epoch) == (4, 4, 100)
+
+
+def test_reference_file_parse_errors_fail_cleanly(hora, tmp_path):
+    # a truncated or malformed bincode file is rejected while parsing, before
+    # any device work (hora_load_reference)
+    from tests import refbin
+    X = np.arange(40, dtype=np.float32).reshape(10, 4)
+    good = refbin.brute_force(X, list(range(10)), 3)
+    L = hora.lib()
+    h = C.c_void_p()
+    for blob in (good[:-3], good[:20], b"", good[:8] + b"\xff" * 8 + good[16:]):
+        p = tmp_path / "bad.bin"
+        p.write_bytes(blob)
+        assert L.hora_load_reference(str(p).encode(), 0, C.byref(h)) == -10  # HORA_EIO
+        assert not h.value
+    assert L.hora_load_reference(b"/nonexistent/file", 0, C.byref(h)) == -10
+    assert L.hora_load_reference(str(tmp_path / "bad.bin").encode(), 7, C.byref(h)) == -1
 
 
 def test_cpp_wrapper_compiles():
