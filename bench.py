@@ -42,7 +42,9 @@ def args_parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--forms", default="fp32,bf16,fp8")
+    ap.add_argument("--forms", default="fp32,bf16,bf16r132,fp8",
+                    help="scoring forms: fp32, bf16, fp8, optionally with an explicit rerank "
+                         "width (bf16r132 = BF16 scoring + exact rerank of 132 candidates)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="queries in the CPU baseline sample")
     ap.add_argument("--small", action="store_true", help="tiny workload for a quick check")
     ap.add_argument("--nq", type=int, default=0, help="override the number of queries (profiling)")
@@ -50,6 +52,8 @@ def args_parse():
     ap.add_argument("--ivf-epochs", type=int, default=25)
     ap.add_argument("--ivf-train-queries", type=int, default=200_000)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the 4k-rerank, other-metric and FP64 sections (profiling runs)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[20_000.0, 200_000.0])
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-ivf-n", type=int, default=10_000_000,
@@ -162,6 +166,14 @@ def make_data(small: bool, nq_override: int = 0):
     base = synth.mixture(n, DIM, N_CENTERS, stream=1)
     q = synth.mixture(nq, DIM, N_CENTERS, stream=2)
     return base, q
+
+
+def form_options(H, form: str):
+    """'fp32' | 'bf16' | 'fp8', optionally followed by r<R> (explicit rerank
+    width; 0 = the library default) -> (precision, rerank)."""
+    base, _, r = form.partition("r")
+    prec = {"fp32": H.Precision.FP32, "bf16": H.Precision.BF16, "fp8": H.Precision.FP8}[base]
+    return prec, int(r) if r else 0
 
 
 def recall_at(ids, exact, r=10):
@@ -352,7 +364,7 @@ def run_serving(a, H, bf_index, bf_pool):
     return out
 
 
-def run_form_extras(a, H, ix, base, q, dq, exact, head_prec):
+def run_form_extras(a, H, ix, base, q, dq, exact, head_prec, head_rerank):
     """Config-2 items beside the headline: the BF16 form with the 4,096-candidate
     rerank the configuration names, the other three metrics (exact FP32 and
     BF16 + rerank; Manhattan has no tensor-core form), and the returned
@@ -385,7 +397,15 @@ def run_form_extras(a, H, ix, base, q, dq, exact, head_prec):
     out["bf16_rerank_4096"] = {"qps": nq / (ms / 1e3), "ms": ms, "kernels_per_search": kern,
                                "recall@10": recall_at(ids, exact, 10) if exact is not None else None,
                                "recall@100": recall_at(ids, exact, K) if exact is not None else None}
-    ix.set_option(H.Option.RERANK, 0)
+    # narrower rerank widths than the default max(2k, k+64)
+    out["bf16_rerank_widths"] = {}
+    for R in (132, 164):
+        ix.set_option(H.Option.RERANK, R)
+        ms, ids, _ = timed(ix, K)
+        out["bf16_rerank_widths"][str(R)] = {
+            "qps": nq / (ms / 1e3), "recall@10": recall_at(ids, exact, 10) if exact is not None else None,
+            "recall@100": recall_at(ids, exact, K) if exact is not None else None}
+    ix.set_option(H.Option.RERANK, head_rerank)
     ix.set_option(H.Option.PRECISION, head_prec)
 
     # the other metrics, each on its own index over the same base
@@ -442,9 +462,10 @@ def run_ours(a, dist: Dist):
     exact = None
     order = [f for f in a.forms.split(",") if f]
     for form in order:
-        prec = {"fp32": H.Precision.FP32, "bf16": H.Precision.BF16, "fp8": H.Precision.FP8}[form]
+        prec, rerank = form_options(H, form)
         try:
             ix.set_option(H.Option.PRECISION, prec)
+            ix.set_option(H.Option.RERANK, rerank)
             ix.search_batch(dq, K, ids_out=ids_d, dist_out=dist_d)
         except H.HoraError as e:
             forms[form] = {"error": str(e)}
@@ -470,7 +491,7 @@ def run_ours(a, dist: Dist):
         dist.barrier()
         dev = sum(step_ms) / 1e3
         forms[form] = {"qps": nq * a.steps / dev, "wall_qps": nq * a.steps / wall,
-                       "recall@10": rec10, "recall@100": rec100,
+                       "rerank": rerank or "default", "recall@10": rec10, "recall@100": rec100,
                        "p50_ms": float(np.percentile(step_ms, 50)),
                        "p99_ms": float(np.percentile(step_ms, 99))}
 
@@ -479,8 +500,9 @@ def run_ours(a, dist: Dist):
     ok = [f for f in order if "qps" in forms.get(f, {}) and
           (exact is None or (forms[f]["recall@10"] or 0) >= 0.95)]
     head = max(ok, key=lambda f: forms[f]["qps"]) if ok else "fp32"
-    prec = {"fp32": H.Precision.FP32, "bf16": H.Precision.BF16, "fp8": H.Precision.FP8}[head]
+    prec, head_rerank = form_options(H, head)
     ix.set_option(H.Option.PRECISION, prec)
+    ix.set_option(H.Option.RERANK, head_rerank)
 
     # ---- headline timed region: device-resident inputs, kernel timing on ----
     for _ in range(a.warmup):
@@ -546,7 +568,8 @@ def run_ours(a, dist: Dist):
         roof["traffic"] = None
         roof["share_of_step"] = ms / (t_dev * 1e3)
 
-    extras = run_form_extras(a, H, ix, base, q, dq, exact, prec) if not a.small and dist.rank == 0 else None
+    extras = run_form_extras(a, H, ix, base, q, dq, exact, prec, head_rerank) \
+        if not a.small and not a.no_extras and dist.rank == 0 else None
     config1 = run_config1(H, dist.rank == 0) if not a.small else None
     ivf, serving = None, None
     if not a.no_ivf:
@@ -569,10 +592,12 @@ def run_ours(a, dist: Dist):
             "metric": "QPS at recall@10>=0.95 (brute force, 1Mx128, k=100)",
             "value": value, "unit": "queries/s", "n_gpus": dist.world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_max / a.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "bf16": "bf16", "fp8": "e4m3"}[head],
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp32": "f32", "bf16": "bf16", "fp8": "e4m3"}[head[:4]],
             "data": "synthetic (seeded gaussian mixture; ann-benchmarks sets unavailable offline)",
             "config": {"workload": WORKLOAD if not a.small else "small check", "n": n, "dim": DIM,
-                       "queries": nq, "k": K, "form": head, "l2_policy": "inputs larger than L2 (512 MB base)",
+                       "queries": nq, "k": K, "form": head, "rerank": head_rerank or "default",
+                       "l2_policy": "inputs larger than L2 (512 MB base)",
                        "parallelism": f"replicas x{dist.world}"},
             "forms": forms, "p50_ms": float(np.percentile(step_ms, 50)),
             "p99_ms": float(np.percentile(step_ms, 99)), "wall_s": t_wall,
