@@ -287,6 +287,17 @@ class BruteForceIndex(_Index):
         super().__init__(dimension, params, _handle)
 
 
+def _knn_graph(self, k: int):
+    """SSGIndex::build_knn_graph (src/index/ssg_idx.rs:69-98): [n, k] row
+    numbers of each row's k nearest other rows, farthest first."""
+    out = np.empty((self.nodes_size(), k), np.uint64)
+    check(lib().hora_knn_graph(self._h, k, C.c_void_p(out.ctypes.data)))
+    return out
+
+
+BruteForceIndex.knn_graph = _knn_graph
+
+
 class IVFPQIndex(_Index):
     """IVFPQIndex<f32, u64> (src/index/pq_idx.rs:267-523), a.k.a. PQIVFIndex."""
     kind = 1

@@ -191,6 +191,13 @@ int hora_ivfpq_set_codebooks(hora_index *h, const float *centers, const float *c
  * checked against the file's.  sub_bits above 8 is HORA_ECAP. */
 int hora_load_reference(const char *path, int kind, hora_index **out);
 
+/* SSGIndex::build_knn_graph (src/index/ssg_idx.rs:69-98) on a built
+ * BruteForceIndex: for every stored row, the row numbers of its k nearest
+ * other rows under the index metric, in the reference's order (max-heap pop
+ * order: farthest first).  Runs the brute-force search with the base's rows
+ * as queries, in the index's precision.  neighbors_out: n x k (host). */
+int hora_knn_graph(hora_index *h, uint64_t k, uint64_t *neighbors_out);
+
 /* Per-call nprobe override (search_n_center) for sweeps; 0 = the param. */
 int hora_search_nprobe(hora_index *h, const float *queries, uint64_t nq, uint64_t k,
                        uint64_t nprobe, uint64_t *ids_out, float *dist_out);
