@@ -439,6 +439,45 @@ def run_form_extras(a, H, ix, base, q, dq, exact, head_prec, head_rerank):
     return out
 
 
+def run_ssg(H, ix, base, cpu_bf_qps):
+    """SSG's data-parallel build steps on the 1Mx128 base (SSGParams defaults,
+    src/index/ssg_params.rs:40-48): the exact kNN graph with init_k = 100
+    (build_knn_graph, ssg_idx.rs:69-98) in the headline form, and the root
+    selection general_kmeans(root_size = 100, epoch = 256) (ssg_idx.rs:388)."""
+    from oracle import oracle as O
+    n = base.shape[0]
+    out = {}
+    t0 = time.perf_counter()
+    g = ix.knn_graph(100)
+    dt = time.perf_counter() - t0
+    rows = np.random.default_rng(1).choice(n, 64, replace=False)
+    threads = os.cpu_count() or 1
+    i_ref, _ = O.bf_search(base, base[rows], 101, O.EUCLIDEAN, threads=threads)
+    hit = 0
+    for r, got in zip(rows, g[rows]):
+        want = [j for j in i_ref[list(rows).index(r)] if j != r][:100]
+        hit += len(set(want) & set(got.tolist()))
+    out["knn_graph"] = {"k": 100, "seconds": dt, "rows_per_s": n / dt, "recall_vs_exact": hit / (64 * 100),
+                        "cpu_estimate_s": n / cpu_bf_qps if cpu_bf_qps else None}
+    del g
+    ex = H.BruteForceIndex(DIM)
+    ex.madd(base, None)
+    ex.build(H.Metric.Euclidean)
+    ex.general_kmeans(100, epoch=1, seed=1)
+    t0 = time.perf_counter()
+    roots = ex.general_kmeans(100, epoch=256, seed=1)
+    dt = time.perf_counter() - t0
+    ns = 50_000
+    t1 = time.perf_counter()
+    O.general_kmeans(base[:ns], 100, 2, O.EUCLIDEAN, seed=1, threads=threads)
+    dc = time.perf_counter() - t1
+    out["general_kmeans"] = {"k": 100, "epoch": 256, "seconds": dt, "roots_distinct": int(len(set(roots.tolist()))),
+                             "cpu_sample": f"{ns} rows, 2 epochs, {threads} threads: {dc:.2f} s",
+                             "cpu_estimate_s": dc * (n / ns) * (256 / 2)}
+    del ex
+    return out
+
+
 # ---- our implementation ------------------------------------------------------------
 def run_ours(a, dist: Dist):
     import torch
@@ -571,6 +610,8 @@ def run_ours(a, dist: Dist):
     extras = run_form_extras(a, H, ix, base, q, dq, exact, prec, head_rerank) \
         if not a.small and not a.no_extras and dist.rank == 0 else None
     config1 = run_config1(H, dist.rank == 0) if not a.small else None
+    ssg = run_ssg(H, ix, base, cpu_sample_qps(base, q, K, 256, os.cpu_count() or 1)[0]) \
+        if not a.small and not a.no_extras and dist.rank == 0 else None
     ivf, serving = None, None
     if not a.no_ivf:
         ivf, ivx = run_ivf(a, H, base, q, exact)
@@ -602,7 +643,7 @@ def run_ours(a, dist: Dist):
             "forms": forms, "p50_ms": float(np.percentile(step_ms, 50)),
             "p99_ms": float(np.percentile(step_ms, 99)), "wall_s": t_wall,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "ivfpq": ivf,
-            "serving": serving, "config1": config1, "form_extras": extras,
+            "serving": serving, "config1": config1, "form_extras": extras, "ssg_build": ssg,
             "gpu_launches": launches, "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
         }
         print(json.dumps(line), flush=True)

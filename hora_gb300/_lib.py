@@ -58,6 +58,7 @@ SIGNATURES = {
     "hora_pq_params_default": (None, [C.POINTER(PQParamsC)]),
     "hora_load_reference": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(vp)]),
     "hora_knn_graph": (C.c_int, [vp, u64, vp]),
+    "hora_general_kmeans": (C.c_int, [vp, u64, u64, vp, u64, vp, vp]),
     "hora_index_create": (C.c_int, [C.c_int, u64, vp, C.POINTER(vp)]),
     "hora_index_free": (C.c_int, [vp]),
     "hora_add": (C.c_int, [vp, vp, vp, u64]),

@@ -109,6 +109,17 @@ __host__ __device__ __forceinline__ uint64_t make_key(float d, uint32_t row) {
 __host__ __device__ __forceinline__ float key_dist(uint64_t k) { return ord2f((uint32_t)(k >> 32)); }
 __host__ __device__ __forceinline__ uint32_t key_row(uint64_t k) { return (uint32_t)k; }
 
+// ---- the splitmix64 stream (shared with the oracle) ----------------------------
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__host__ __device__ __forceinline__ uint64_t instance_seed(uint64_t seed, uint64_t inst) {
+  return mix64(seed ^ mix64(inst * 0xD1B54A32D192ED03ull + 0x9E3779B97F4A7C15ull));
+}
+constexpr uint64_t kRngStep = 0x9E3779B97F4A7C15ull;
+
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 

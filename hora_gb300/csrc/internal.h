@@ -96,6 +96,18 @@ int bf_topk_exact(const BaseView &b, int metric, const float *dQ, const float *d
                   int k, int cand_cap, SearchWorkspace &ws, uint64_t *d_best, cudaStream_t s,
                   int *retries_out);
 
+// ---- k-means pieces (ivfpq.cu) ------------------------------------------------------
+// Stable bucketing of n items by label (labels[i], or key_row(keys[i]) when
+// keys is given): d_offsets (C + 1 entries) and d_members, the items of each
+// bucket in item order.  counts receives the C bucket sizes.
+int sort_labels(const uint64_t *keys, const uint32_t *labels, int64_t n, int C, DevBuf &blk,
+                DevBuf &counts, int64_t *d_offsets, uint32_t *d_members, cudaStream_t s);
+// New centres (pitch ld): per (centre, column) the sum over the bucket's
+// members in item order (f32 adds, or f64 when accum_f64) divided by the
+// count; an empty bucket gets `empty` in every column.
+int launch_center_sum(const float *X, int64_t ld, const uint32_t *members, const int64_t *offsets,
+                      int C, int64_t dim, int accum_f64, float empty, float *centers, cudaStream_t s);
+
 // ---- error helpers ------------------------------------------------------------------
 const char *metric_name(int m);
 

@@ -50,18 +50,6 @@ struct IvfState {
 
 void ivf_state_free(IvfState *p) { delete p; }
 
-// ---------------------------------------------------------------------------
-// device RNG: the splitmix64 stream shared with the oracle
-__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-__host__ __device__ __forceinline__ uint64_t instance_seed(uint64_t seed, uint64_t inst) {
-  return mix64(seed ^ mix64(inst * 0xD1B54A32D192ED03ull + 0x9E3779B97F4A7C15ull));
-}
-constexpr uint64_t kRngStep = 0x9E3779B97F4A7C15ull;
-
 // The probability walk of Kmeans::split_center (kmeans.rs:150-193) for one
 // empty centre, evaluated by one warp 32 candidates at a time.  The
 // sequential walk visits centres start, start+1, ... (mod C); a centre with
@@ -212,28 +200,52 @@ __global__ void label_scatter_kernel(const uint64_t *keys, const uint32_t *label
   }
 }
 
-// new centres: per (centre, column) sequential sum over members in item order
+// new centres: per (centre, column) sequential sum over members in item
+// order; the loads run 8 members ahead of the (order-preserving) adds
 __global__ void center_sum_kernel(const float *X, int64_t ld, const uint32_t *members,
                                   const int64_t *offsets, int C, int64_t dim, int accum_f64,
-                                  float *centers) {
+                                  float empty, float *centers) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)C * dim) return;
   int c = (int)(t / dim);
   int64_t j = t % dim;
   int64_t lo = offsets[c], hi = offsets[c + 1];
-  float out = 0.0f;
+  float out = empty;
   if (hi > lo) {
+    float v[8];
     if (accum_f64) {
       double s = 0.0;
-      for (int64_t p = lo; p < hi; ++p) s += (double)X[(int64_t)members[p] * ld + j];
+      int64_t p = lo;
+      for (; p + 8 <= hi; p += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = X[(int64_t)members[p + u] * ld + j];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += (double)v[u];
+      }
+      for (; p < hi; ++p) s += (double)X[(int64_t)members[p] * ld + j];
       out = (float)(s / (double)(hi - lo));
     } else {
       float s = 0.0f;
-      for (int64_t p = lo; p < hi; ++p) s = __fadd_rn(s, X[(int64_t)members[p] * ld + j]);
+      int64_t p = lo;
+      for (; p + 8 <= hi; p += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = X[(int64_t)members[p + u] * ld + j];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s = __fadd_rn(s, v[u]);
+      }
+      for (; p < hi; ++p) s = __fadd_rn(s, X[(int64_t)members[p] * ld + j]);
       out = __fdiv_rn(s, (float)(hi - lo));
     }
   }
   centers[(int64_t)c * ld + j] = out;
+}
+
+int launch_center_sum(const float *X, int64_t ld, const uint32_t *members, const int64_t *offsets,
+                      int C, int64_t dim, int accum_f64, float empty, float *centers, cudaStream_t s) {
+  center_sum_kernel<<<ceil_div((int64_t)C * dim, 256), 256, 0, s>>>(X, ld, members, offsets, C, dim,
+                                                                    accum_f64, empty, centers);
+  HORA_LAUNCHED();
+  return HORA_OK;
 }
 
 // Kmeans::split_center (kmeans.rs:150-193): the empty centres in index
@@ -858,7 +870,7 @@ __global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
 // ---------------------------------------------------------------------------
 // host side
 
-static int sort_labels(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
+int sort_labels(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
                        DevBuf &blk, DevBuf &counts, int64_t *d_offsets, uint32_t *d_members,
                        cudaStream_t s) {
   int64_t nb = ceil_div(n, kSortBlock);
@@ -1066,10 +1078,8 @@ int ivf_build(hora_index *h) {
                          members.as<uint32_t>(), s));
     {
       ProfScope ps("coarse_update", s);
-      center_sum_kernel<<<ceil_div((int64_t)C * h->dim, 256), 256, 0, s>>>(
-          X, h->ld, members.as<uint32_t>(), moff.as<int64_t>(), C, h->dim, h->accum_f64,
-          v.centers.as<float>());
-      HORA_LAUNCHED();
+      HORA_TRY(launch_center_sum(X, h->ld, members.as<uint32_t>(), moff.as<int64_t>(), C, h->dim,
+                                 h->accum_f64, 0.0f, v.centers.as<float>(), s));
     }
     if (ep < epochs - 1) {
       ProfScope ps("coarse_split", s);

@@ -295,7 +295,32 @@ def _knn_graph(self, k: int):
     return out
 
 
+def _general_kmeans(self, k: int, epoch: int = 256, seed: int = 0, init_rows=None, return_means: bool = False):
+    """kmeans::general_kmeans (src/core/kmeans.rs:216-289) over this index's
+    rows with its metric: the row number nearest to each of the k means after
+    `epoch` rounds (SSG calls it with epoch 256, ssg_idx.rs:388).  The means
+    start at init_rows (k row numbers) or at k rows drawn with replacement
+    from the seeded stream.  Returns roots [k] (uint64), and the means [k, dim]
+    (float32, NaN for a mean that lost all its rows) when return_means."""
+    dim = self.dimension()
+    if self.nodes_size() == 0 and self.built():
+        empty = np.empty(0, np.uint64)
+        return (empty, np.empty((0, dim), np.float32)) if return_means else empty
+    roots = np.empty(k, np.uint64)
+    means = np.empty((k, dim), np.float32) if return_means else None
+    init = None
+    if init_rows is not None:
+        init = np.ascontiguousarray(init_rows, dtype=np.uint64)
+        if init.shape != (k,):
+            raise _lib.HoraError(-1, "init_rows must hold k row numbers")
+    check(lib().hora_general_kmeans(self._h, k, epoch, None if init is None else C.c_void_p(init.ctypes.data),
+                                    seed, C.c_void_p(roots.ctypes.data),
+                                    None if means is None else C.c_void_p(means.ctypes.data)))
+    return (roots, means) if return_means else roots
+
+
 BruteForceIndex.knn_graph = _knn_graph
+BruteForceIndex.general_kmeans = _general_kmeans
 
 
 class IVFPQIndex(_Index):

@@ -198,6 +198,19 @@ int hora_load_reference(const char *path, int kind, hora_index **out);
  * as queries, in the index's precision.  neighbors_out: n x k (host). */
 int hora_knn_graph(hora_index *h, uint64_t k, uint64_t *neighbors_out);
 
+/* kmeans::general_kmeans (src/core/kmeans.rs:216-289; SSG's root selection,
+ * src/index/ssg_idx.rs:388) over the rows of a built BruteForceIndex, with
+ * the index metric.  The k means start as copies of the rows init_rows[0..k)
+ * or, when init_rows is NULL, of k rows drawn with replacement from the
+ * splitmix64 stream of `seed` (the reference draws from an unseeded thread
+ * RNG); epoch rounds of nearest-mean assignment and f32 means (an empty mean
+ * becomes NaN, as in the reference) follow.  roots_out (k, host): per mean,
+ * the row number nearest to it; means_out (k x dim, host) may be NULL.
+ * Writes nothing when the index holds no rows (the reference returns an empty
+ * list).  k <= 32768, else HORA_ECAP. */
+int hora_general_kmeans(hora_index *h, uint64_t k, uint64_t epoch, const uint64_t *init_rows,
+                        uint64_t seed, uint64_t *roots_out, float *means_out);
+
 /* Per-call nprobe override (search_n_center) for sweeps; 0 = the param. */
 int hora_search_nprobe(hora_index *h, const float *queries, uint64_t nq, uint64_t k,
                        uint64_t nprobe, uint64_t *ids_out, float *dist_out);

@@ -11,6 +11,7 @@
  */
 #include "hora_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
@@ -826,6 +827,82 @@ int horo_pq_search(const float *codebooks, const uint8_t *codes, int64_t n, int6
                    int64_t k, int64_t *idx_out, float *dist_out, int threads) {
   pq_ctx c = {codebooks, queries, codes, n, dim, n_sub, sub_bits, k, metric, idx_out, dist_out};
   parallel_for(nq, threads, pq_range, &c);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* kmeans::general_kmeans — src/core/kmeans.rs:216-289.                      */
+
+typedef struct {
+  const float *rows;  /* the side scanned: nodes (assignment) or nodes (roots) */
+  const float *means;
+  int64_t n, dim, k;
+  int metric, roots; /* roots: per mean the nearest node, else per node the nearest mean */
+  int64_t *out;
+} gk_ctx;
+
+static void gk_range(void *arg, int64_t lo, int64_t hi) {
+  const gk_ctx *c = (const gk_ctx *)arg;
+  for (int64_t t = lo; t < hi; ++t) {
+    /* kmeans.rs:240-247 and :276-283: index 0, distance E::max_value(),
+     * strict '<', metric(node, mean) */
+    int64_t idx = 0;
+    float dist = FLT_MAX;
+    const int64_t m = c->roots ? c->n : c->k;
+    for (int64_t i = 0; i < m; ++i) {
+      const float *node = c->roots ? c->rows + i * c->dim : c->rows + t * c->dim;
+      const float *mean = c->roots ? c->means + t * c->dim : c->means + i * c->dim;
+      float d = horo_metric_f32(node, mean, c->dim, c->metric, NULL);
+      if (d < dist) {
+        idx = i;
+        dist = d;
+      }
+    }
+    c->out[t] = idx;
+  }
+}
+
+int horo_general_kmeans(const float *data, int64_t n, int64_t dim, int64_t k, int64_t epoch, int metric,
+                        const int64_t *init_rows, uint64_t seed, int64_t *roots_out, float *means_out,
+                        int threads) {
+  if (n == 0) return 0; /* kmeans.rs:222-224: no roots */
+  float *means = means_out;
+  /* kmeans.rs:228-230: k rows drawn with replacement (seeded stream here) */
+  uint64_t st = horo_rng_instance_seed(seed, 0);
+  for (int64_t i = 0; i < k; ++i) {
+    int64_t r;
+    if (init_rows) {
+      r = init_rows[i];
+    } else {
+      uint64_t u = horo_rng_next(&st);
+      r = (int64_t)(((unsigned __int128)u * (uint64_t)n) >> 64);
+    }
+    if (r < 0 || r >= n) return -1;
+    memcpy(means + i * dim, data + r * dim, sizeof(float) * (size_t)dim);
+  }
+  int64_t *asg = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+  int64_t *cnt = (int64_t *)malloc(sizeof(int64_t) * (size_t)k);
+  float *feat = (float *)malloc(sizeof(float) * (size_t)(k * dim));
+  for (int64_t ep = 0; ep < epoch; ++ep) {
+    gk_ctx c = {data, means, n, dim, k, metric, 0, asg};
+    parallel_for(n, threads, gk_range, &c);
+    /* kmeans.rs:248-254: f32 sums per mean, here in node order */
+    memset(cnt, 0, sizeof(int64_t) * (size_t)k);
+    memset(feat, 0, sizeof(float) * (size_t)(k * dim));
+    for (int64_t j = 0; j < n; ++j) {
+      float *f = feat + asg[j] * dim;
+      for (int64_t t = 0; t < dim; ++t) f[t] += data[j * dim + t];
+      cnt[asg[j]] += 1;
+    }
+    /* kmeans.rs:257-270: divide by the count (0 / 0 = NaN for an empty mean) */
+    for (int64_t i = 0; i < k; ++i)
+      for (int64_t t = 0; t < dim; ++t) means[i * dim + t] = feat[i * dim + t] / (float)cnt[i];
+  }
+  gk_ctx c = {data, means, n, dim, k, metric, 1, roots_out};
+  parallel_for(k, threads, gk_range, &c);
+  free(asg);
+  free(cnt);
+  free(feat);
   return 0;
 }
 

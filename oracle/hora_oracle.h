@@ -140,6 +140,15 @@ int horo_pq_search(const float *codebooks, const uint8_t *codes, int64_t n, int6
                    int64_t n_sub, int64_t sub_bits, int metric, const float *queries, int64_t nq,
                    int64_t k, int64_t *idx_out, float *dist_out, int threads);
 
+/* kmeans::general_kmeans (src/core/kmeans.rs:216-289).  Means start at
+ * data[init_rows[i]] or, when init_rows is NULL, at k rows drawn with
+ * replacement from the splitmix64 stream of `seed` (row = next * n >> 64).
+ * Sums run in node order.  means_out (k x dim) receives the final means;
+ * roots_out (k) per mean the nearest node.  Returns -1 for a bad init row. */
+int horo_general_kmeans(const float *data, int64_t n, int64_t dim, int64_t k, int64_t epoch, int metric,
+                        const int64_t *init_rows, uint64_t seed, int64_t *roots_out, float *means_out,
+                        int threads);
+
 #ifdef __cplusplus
 }
 #endif

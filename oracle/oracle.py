@@ -79,6 +79,8 @@ def lib():
                                     f32p, u8p]
         L.horo_pq_search.argtypes = [f32p, u8p, i64, i64, i64, i64, C.c_int, f32p, i64, i64, i64p,
                                      f32p, C.c_int]
+        L.horo_general_kmeans.argtypes = [f32p, i64, i64, i64, i64, C.c_int, i64p, C.c_uint64, i64p,
+                                          f32p, C.c_int]
         L.horo_mlp_forward.argtypes = [f32p, i64, i64, i64, f32p, i64, f32p]
         L.horo_mlp_loss_grad.restype = C.c_double
         L.horo_mlp_loss_grad.argtypes = [f32p, i64, i64, i64, f32p, f32p, i64, C.c_float, f64p]
@@ -266,6 +268,20 @@ def pq_search(ix, queries, k, threads=1):
                          ix["n_sub"], ix["sub_bits"], ix["metric"], _p(queries, f32p), nq, k,
                          _p(idx, i64p), _p(dist, f32p), threads)
     return idx, dist
+
+
+def general_kmeans(data, k, epoch, mt, seed=0, init_rows=None, threads=1):
+    """kmeans::general_kmeans (kmeans.rs:216-289): (roots [k] int64, means [k, dim])."""
+    data = _f32(data)
+    n, d = data.shape
+    roots = np.zeros(k, np.int64)
+    means = np.zeros((k, d), np.float32)
+    init = None if init_rows is None else np.ascontiguousarray(init_rows, dtype=np.int64)
+    rc = lib().horo_general_kmeans(_p(data, f32p), n, d, k, epoch, mt, _p(init, i64p), seed,
+                                   _p(roots, i64p), _p(means, f32p), threads)
+    if rc:
+        raise ValueError("init row out of range")
+    return roots, means
 
 
 def pq_encode(data, list_center, codebook, n_sub, sub_bits):

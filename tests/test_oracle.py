@@ -203,3 +203,28 @@ def test_mlp_grad_finite_difference(oracle):
         pp[i] -= 2 * eps
         lm, _ = oracle.mlp_loss_grad(pp.astype(np.float32), x, y, f, h1, h2, alpha=2.0)
         assert abs((lp - lm) / (2 * eps) - g[i]) < 2e-2 * max(1.0, abs(g[i]))
+
+
+def test_general_kmeans_oracle_behaviour(oracle):
+    """kmeans::general_kmeans (kmeans.rs:216-289) restated: an epoch-0 run
+    returns the initial rows as roots, a duplicated initial mean loses every
+    tie and becomes 0/0 = NaN with root 0, and well separated clusters seeded
+    one row each converge to their means."""
+    rng = np.random.default_rng(7)
+    cen = np.array([[0, 0], [100, 0], [0, 100]], np.float32)
+    lab = rng.integers(0, 3, 600)
+    X = (cen[lab] + rng.standard_normal((600, 2))).astype(np.float32)
+    init = np.array([int(np.where(lab == c)[0][0]) for c in range(3)], np.int64)
+    roots, _ = oracle.general_kmeans(X, 3, 0, 3, init_rows=init)
+    np.testing.assert_array_equal(roots, init)
+    roots, means = oracle.general_kmeans(X, 3, 5, 3, init_rows=init)
+    for c in range(3):
+        np.testing.assert_allclose(means[c], X[lab == c].mean(0), atol=1e-3)
+        assert lab[roots[c]] == c
+    roots, means = oracle.general_kmeans(X, 3, 3, 3, init_rows=np.array([init[0], init[0], init[1]]))
+    assert np.isnan(means[1]).all() and roots[1] == 0
+    assert np.isfinite(means[[0, 2]]).all()
+    a, ma = oracle.general_kmeans(X, 3, 4, 3, seed=3)
+    b, mb = oracle.general_kmeans(X, 3, 4, 3, seed=3, threads=4)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(ma, mb)
