@@ -743,6 +743,18 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s, false));
     done += c;
   }
+  // exact FP32 rerank of the R candidates, then the k best; launched before
+  // the host learns whether a candidate list overflowed (rare), so the
+  // stream runs on without a round trip, and redone after the rescans
+  HORA_TRY(ws.tmp.reserve(sizeof(uint64_t) * nq * R));
+  auto finish = [&]() -> int {
+    HORA_TRY(launch_rerank_exact(h->metric, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim,
+                                 ws.qnorm.as<float>(), h->xnorm.as<float>(), bestR, nq, R,
+                                 ws.tmp.as<uint64_t>(), s));
+    HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
+    return launch_merge_topk(d_best, k, ws.tmp.as<uint64_t>(), nullptr, R, R, nullptr, nq, flags, ovc, s);
+  };
+  HORA_TRY(finish());
   // overflow rescans over gathered query rows
   uint32_t h_ovc = 0;
   int errflag = 0;
@@ -782,13 +794,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     HORA_CUDA_TRY(cudaStreamSynchronize(s));
   }
   h->last_retries = rounds;
-  // exact FP32 rerank of the R candidates, then the k best
-  HORA_TRY(ws.tmp.reserve(sizeof(uint64_t) * nq * R));
-  HORA_TRY(launch_rerank_exact(h->metric, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim,
-                               ws.qnorm.as<float>(), h->xnorm.as<float>(), bestR, nq, R,
-                               ws.tmp.as<uint64_t>(), s));
-  HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
-  HORA_TRY(launch_merge_topk(d_best, k, ws.tmp.as<uint64_t>(), nullptr, R, R, nullptr, nq, flags, ovc, s));
+  if (rounds > 0) HORA_TRY(finish());
   return HORA_OK;
 }
 

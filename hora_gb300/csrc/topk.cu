@@ -267,13 +267,32 @@ __global__ void __launch_bounds__(kSelectThreads) merge_select_kernel(
   }
 }
 
-// The same merge with one warp per query (8 queries per CTA) for k <= 256:
-// the keys stay in global memory (L1-resident across the passes), the
-// histogram is warp-private (8-bit digits, updates aggregated per digit), the
-// winners are sorted by the warp; no block barrier anywhere, so the warps of
-// a CTA never wait for one another.
-constexpr int kWmWarps = 8, kWmMaxK = 256;
-__global__ void __launch_bounds__(kWmWarps * 32) merge_warp_kernel(
+// The same merge with one warp per query for k <= 256.  Every key (list +
+// candidates) is read once; for up to 32 x kWmRegs keys the warp keeps their
+// high (distance) words in registers, 40 per lane.  The radix select runs on
+// key - kmin, kmin = the smallest high word (low word zero), with its first
+// 8-bit digit at the top of the key range, so the leading bits that every key
+// shares cost no pass and the keys spread over the bins (plain shared
+// atomics, few collisions).  While the selection stays within the distance
+// word it runs on the registers alone, and only the winners' full keys are
+// read again; a selection that needs the row bits (ties), or a larger key
+// set, reads the keys from global memory on each pass.  The winners are
+// sorted only for a final list; an intermediate list (sorted = false) only
+// needs its largest key at k - 1, where the candidate filter reads the
+// threshold.  No block barrier anywhere.
+constexpr int kWmWarps = 8, kWmMaxK = 256, kWmRegs = 40;
+
+__device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t y = __shfl_xor_sync(0xffffffffu, v, o);
+    v = y > v ? y : v;
+  }
+  return v;
+}
+
+template <bool SORTED>
+__global__ void __launch_bounds__(kWmWarps * 32, 3) merge_warp_kernel(
     uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n, int64_t nq,
     uint8_t *ovf_flag, uint32_t *ovf_counter) {
   __shared__ uint32_t hist_all[kWmWarps][256];
@@ -292,52 +311,150 @@ __global__ void __launch_bounds__(kWmWarps * 32) merge_warp_kernel(
   const uint64_t *cq = cand + q * cap;
   uint64_t *bq = best + q * k;
   const int n = (int)c + k;
+  auto key_at = [&](int i) -> uint64_t { return i < (int)c ? cq[i] : bq[i - c]; };
+  const bool inreg = n <= 32 * kWmRegs;
+
+  // one read of every key: live count and the range of the high words (no
+  // live key has the empty key's high word 0xffffffff, which is the largest)
+  uint32_t hw[kWmRegs];
   int live = 0;
-  for (int i = lane; i < n; i += 32) live += (i < (int)c ? cq[i] : bq[i - c]) != kEmptyKey;
+  uint32_t hmin = 0xffffffffu, hmax = 0;
+  if (inreg) {
+#pragma unroll
+    for (int b = 0; b < kWmRegs; b += 8) {
+      uint64_t v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = (b + u) * 32 + lane;
+        v[u] = i < n ? key_at(i) : kEmptyKey;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) hw[b + u] = (uint32_t)(v[u] >> 32);
+    }
+#pragma unroll
+    for (int m = 0; m < kWmRegs; ++m) {
+      const bool ok = hw[m] != 0xffffffffu;
+      live += ok;
+      hmin = min(hmin, hw[m]);
+      hmax = max(hmax, ok ? hw[m] : 0u);
+    }
+  } else {
+    for (int i = lane; i < n; i += 32) {
+      const uint32_t hi = (uint32_t)(key_at(i) >> 32);
+      const bool ok = hi != 0xffffffffu;
+      live += ok;
+      hmin = min(hmin, hi);
+      hmax = max(hmax, ok ? hi : 0u);
+    }
+  }
   live = __reduce_add_sync(0xffffffffu, live);
+  hmin = __reduce_min_sync(0xffffffffu, hmin);
+  hmax = __reduce_max_sync(0xffffffffu, hmax);
+  // every live key lies in [kmin, kmax]; key - kmin keeps the low word and
+  // subtracts hmin from the high one
+  const uint64_t kmin = (uint64_t)hmin << 32, kmax = ((uint64_t)hmax << 32) | 0xffffffffull;
   const int want = live < k ? live : k;
-  if (want > 0) {
+  // the winners are the live keys with key - kmin <= bound
+  uint64_t bound = kmax - kmin;
+  if (want > 0 && want < live) {
+    const uint64_t span = kmax - kmin;
+    int shift = 64 - __clzll((long long)span) - 8;
+    shift = shift < 0 ? 0 : shift;
     uint64_t prefix = 0, mask = 0;
     int rem = want;
-    for (int shift = 56; shift >= 0; shift -= 8) {
+    for (;;) {
       for (int b = lane; b < 256; b += 32) hist[b] = 0;
       __syncwarp();
-      for (int i0 = 0; i0 < n; i0 += 32) {
-        const int i = i0 + lane;
-        const uint64_t v = i < n ? (i < (int)c ? cq[i] : bq[i - c]) : kEmptyKey;
-        const bool p = v != kEmptyKey && (v & mask) == prefix;
-        const unsigned pm = __ballot_sync(0xffffffffu, p);
-        if (p) {
-          const uint32_t d = (uint32_t)(v >> shift) & 255u;
-          const unsigned peers = __match_any_sync(pm, d);
-          if (lane == __ffs(peers) - 1) atomicAdd(&hist[d], (uint32_t)__popc(peers));
+      if (shift >= 32) {
+        // the digit and every fixed bit lie in the high word
+        const uint32_t mh = (uint32_t)(mask >> 32), ph = (uint32_t)(prefix >> 32);
+        const int sh = shift - 32;
+        if (inreg) {
+#pragma unroll
+          for (int m = 0; m < kWmRegs; ++m) {
+            const uint32_t dh = hw[m] - hmin;
+            if (hw[m] != 0xffffffffu && (dh & mh) == ph) atomicAdd(&hist[(dh >> sh) & 255u], 1u);
+          }
+        } else {
+#pragma unroll 4
+          for (int i = lane; i < n; i += 32) {
+            const uint32_t hi = (uint32_t)(key_at(i) >> 32);
+            const uint32_t dh = hi - hmin;
+            if (hi != 0xffffffffu && (dh & mh) == ph) atomicAdd(&hist[(dh >> sh) & 255u], 1u);
+          }
+        }
+      } else {
+#pragma unroll 4
+        for (int i = lane; i < n; i += 32) {
+          const uint64_t v = key_at(i);
+          const uint64_t d = v - kmin;
+          if (v != kEmptyKey && (d & mask) == prefix) atomicAdd(&hist[(uint32_t)(d >> shift) & 255u], 1u);
         }
       }
       __syncwarp();
       warp_find_digit(hist, (uint32_t)rem, dig);
       __syncwarp();
-      const int d = dig[0], at = (int)hist[d];
+      const int dd = dig[0], at = (int)hist[dd];
       rem -= dig[1];
-      prefix |= (uint64_t)d << shift;
+      prefix |= (uint64_t)dd << shift;
       mask |= (uint64_t)0xff << shift;
       __syncwarp();
-      if (at == rem) break;  // every key under this prefix is taken
+      if (at == rem || shift == 0) break;  // every key under this prefix is taken
+      shift = shift >= 8 ? shift - 8 : 0;
     }
+    // the largest d under the prefix (d has no bits above the first digit)
+    bound = prefix | ((1ull << shift) - 1ull);
+  }
+  if (want > 0) {
     int taken = 0;
-    for (int i0 = 0; i0 < n; i0 += 32) {
-      const int i = i0 + lane;
-      const uint64_t v = i < n ? (i < (int)c ? cq[i] : bq[i - c]) : kEmptyKey;
-      const bool p = v != kEmptyKey && (v & mask) <= prefix;
-      const unsigned pm = __ballot_sync(0xffffffffu, p);
-      const int slot = taken + __popc(pm & ((1u << lane) - 1u));
-      if (p && slot < want) sel[slot] = v;
-      taken += __popc(pm);
+    const unsigned below = (1u << lane) - 1u;
+    if (inreg && (uint32_t)bound == 0xffffffffu) {
+      // the test needs the high words only: d <= bound iff hi - hmin <= bound's high word
+      const uint32_t bh = (uint32_t)(bound >> 32);
+#pragma unroll
+      for (int m = 0; m < kWmRegs; ++m) {
+        const bool p = hw[m] != 0xffffffffu && hw[m] - hmin <= bh;
+        const unsigned pm = __ballot_sync(0xffffffffu, p);
+        const int slot = taken + __popc(pm & below);
+        if (p && slot < want) sel[slot] = key_at(m * 32 + lane);
+        taken += __popc(pm);
+      }
+    } else {
+      for (int i0 = 0; i0 < n; i0 += 32) {
+        const int i = i0 + lane;
+        const uint64_t v = i < n ? key_at(i) : kEmptyKey;
+        const bool p = v != kEmptyKey && v - kmin <= bound;
+        const unsigned pm = __ballot_sync(0xffffffffu, p);
+        const int slot = taken + __popc(pm & below);
+        if (p && slot < want) sel[slot] = v;
+        taken += __popc(pm);
+      }
     }
-    int P = 1;
-    while (P < want) P <<= 1;
-    for (int i = want + lane; i < P; i += 32) sel[i] = kEmptyKey;
     __syncwarp();
-    warp_bitonic_sort(sel, P);
+    if (SORTED) {
+      int P = 1;
+      while (P < want) P <<= 1;
+      for (int i = want + lane; i < P; i += 32) sel[i] = kEmptyKey;
+      __syncwarp();
+      warp_bitonic_sort(sel, P);
+    } else if (want == k) {
+      // the largest winner to slot k - 1
+      uint64_t m = 0;
+      int at = -1;
+      for (int i = lane; i < want; i += 32)
+        if (sel[i] >= m) {
+          m = sel[i];
+          at = i;
+        }
+      const uint64_t mx = warp_max_u64(m);
+      const unsigned who = __ballot_sync(0xffffffffu, m == mx && at >= 0);
+      const int src = __shfl_sync(0xffffffffu, at, __ffs(who) - 1);
+      if (lane == 0 && src != want - 1) {
+        sel[src] = sel[want - 1];
+        sel[want - 1] = mx;
+      }
+      __syncwarp();
+    }
   }
   for (int i = lane; i < k; i += 32) bq[i] = i < want ? sel[i] : kEmptyKey;
   if (lane == 0) {
@@ -370,8 +487,13 @@ int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *cou
   const int cmax = dense_n > 0 ? dense_n : cap;
   if (!qlist && k <= kWmMaxK) {
     ProfScope ps("topk_merge", s);
-    merge_warp_kernel<<<(unsigned)ceil_div(nlist, (int64_t)kWmWarps), kWmWarps * 32, 0, s>>>(
-        best, k, cand, count, cap, dense_n, nlist, ovf_flag, ovf_counter);
+    const unsigned grid = (unsigned)ceil_div(nlist, (int64_t)kWmWarps);
+    if (sorted)
+      merge_warp_kernel<true><<<grid, kWmWarps * 32, 0, s>>>(best, k, cand, count, cap, dense_n, nlist,
+                                                                 ovf_flag, ovf_counter);
+    else
+      merge_warp_kernel<false><<<grid, kWmWarps * 32, 0, s>>>(best, k, cand, count, cap, dense_n, nlist,
+                                                                  ovf_flag, ovf_counter);
     HORA_LAUNCHED();
     return HORA_OK;
   }
