@@ -168,11 +168,21 @@ template <int MT, int MODE, bool RAW>
 __device__ __forceinline__ void drain_mask(const uint32_t (&v)[32], uint32_t hits, const DrainCtx &c,
                                            int &nb) {
   if constexpr (MODE == TILE_DENSE) {
-    uint64_t *out = c.cand + c.qid * c.cap;
+    uint64_t *out = c.cand + c.qid * c.cap + (c.rt - c.r_begin);
+    if (c.rt + 32 <= c.r_end) {
+      // a whole slice: 16-byte pair stores (cap is a multiple of 128 and a
+      // slice starts 32 rows into the chunk, so `out` is 16-byte aligned)
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int64_t row = c.rt + j;
-      if (row < c.r_end) out[row - c.r_begin] = make_key(drain_dist<MT, MODE, RAW>(v[j], c.qa), (uint32_t)row);
+      for (int j = 0; j < 32; j += 2) {
+        ulonglong2 kv;
+        kv.x = make_key(drain_dist<MT, MODE, RAW>(v[j], c.qa), (uint32_t)(c.rt + j));
+        kv.y = make_key(drain_dist<MT, MODE, RAW>(v[j + 1], c.qa), (uint32_t)(c.rt + j + 1));
+        *reinterpret_cast<ulonglong2 *>(out + j) = kv;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (c.rt + j < c.r_end) out[j] = make_key(drain_dist<MT, MODE, RAW>(v[j], c.qa), (uint32_t)(c.rt + j));
     }
   } else {
     // the exact key test: only keys below the R-th key are offered, so a
@@ -737,7 +747,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     // more than the merge a smaller chunk adds (measured on 1M x 128, R = 132)
     double grow = std::min((double)cap / (4.0 * R), 1.5);
     int64_t c = (int64_t)((double)done * std::max(grow, 1.0));
-    c = std::max<int64_t>(c, (int64_t)8192);
+    c = std::max<int64_t>(c, (int64_t)4096);
     c = std::min<int64_t>(round_up(c, kLpBN), std::min<int64_t>(n - done, max_chunk));
     p.r_begin = done;
     p.r_end = done + c;
