@@ -193,21 +193,24 @@ int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint
 // (two rows per coalesced 512-byte load) into a padded shared tile (row
 // stride 65 floats: conflict-free column reads); each lane then sums its own
 // row from the tile in dimension order.
-constexpr int kRrWarps = 4, kRrSlab = 64;
+// One CTA per query with ceil(R / 32) warps (at most kRrMaxWarps), so that
+// R = 132 takes one round of five warps rather than two rounds of four.
+constexpr int kRrMaxWarps = 8, kRrSlab = 64;
 template <int MT>
-__global__ void __launch_bounds__(kRrWarps * 32) rerank_exact_kernel(
+__global__ void __launch_bounds__(kRrMaxWarps * 32) rerank_exact_kernel(
     const float *Q, int64_t ld, const float *X, int64_t dim, const float *qnorm, const float *xnorm,
     const uint64_t *in, int R, uint64_t *outk) {
-  __shared__ float tile[kRrWarps][32][kRrSlab + 1];
-  extern __shared__ float qs[];  // ld floats: the query row
+  extern __shared__ float rr_smem[];  // per warp a 32 x (kRrSlab + 1) tile, then the query row
+  const int nw = blockDim.x >> 5;
+  float *qs = rr_smem + nw * 32 * (kRrSlab + 1);
   const int64_t q = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int64_t t = threadIdx.x; t < ld; t += blockDim.x) qs[t] = Q[q * ld + t];
   __syncthreads();
   const int64_t n4 = (dim + 3) / 4;  // the zero-padded columns up to 4*n4 add exact zeros
-  float(*tw)[kRrSlab + 1] = tile[warp];
+  float(*tw)[kRrSlab + 1] = reinterpret_cast<float(*)[kRrSlab + 1]>(rr_smem + warp * 32 * (kRrSlab + 1));
   const int half = lane >> 4, c4 = lane & 15;
-  for (int r0 = warp * 32; r0 < R; r0 += kRrWarps * 32) {
+  for (int r0 = warp * 32; r0 < R; r0 += nw * 32) {
     const int r = r0 + lane;
     const uint64_t key = r < R ? in[q * R + r] : kEmptyKey;
     float s = 0.0f;
@@ -259,9 +262,19 @@ int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, 
   if (ld % 4) return fail(HORA_EINVAL, "rerank: pitch not a multiple of 4");
   ProfScope ps("rerank_exact", s);
   unsigned g = (unsigned)nq;
-  const size_t qb = sizeof(float) * (size_t)ld;  // the query row in dynamic shared memory
-  if (qb > 48 * 1024) return fail(HORA_EINVAL, "rerank: dimension too large");
-  constexpr int T = kRrWarps * 32;
+  const int nw = std::max(1, std::min(kRrMaxWarps, (R + 31) / 32));
+  const int T = nw * 32;
+  // the warps' tiles and the query row in dynamic shared memory
+  const size_t qb = sizeof(float) * ((size_t)nw * 32 * (kRrSlab + 1) + (size_t)ld);
+  if (qb > 200 * 1024) return fail(HORA_EINVAL, "rerank: dimension too large");
+  static size_t attr = 48 * 1024;
+  if (qb > attr) {
+    HORA_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel<M_L2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qb));
+    HORA_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel<M_L1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qb));
+    HORA_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel<M_IP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qb));
+    HORA_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel<M_COS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qb));
+    attr = qb;
+  }
   switch (metric) {
     case M_L2: rerank_exact_kernel<M_L2><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
     case M_L1: rerank_exact_kernel<M_L1><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
