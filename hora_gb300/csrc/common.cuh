@@ -125,6 +125,34 @@ inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
 // ---- device memory -------------------------------------------------------------
 // Grow-only device buffer owned by an index or a search context.
+// Page-locked host memory: the target of asynchronous device-to-host copies.
+struct HostBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  HostBuf() = default;
+  HostBuf(const HostBuf &) = delete;
+  HostBuf &operator=(const HostBuf &) = delete;
+  ~HostBuf() {
+    if (ptr) cudaFreeHost(ptr);
+  }
+  int reserve(size_t want) {
+    if (want <= bytes) return HORA_OK;
+    void *p = nullptr;
+    if (cudaHostAlloc(&p, want, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(HORA_EOOM, "cudaHostAlloc failed");
+    }
+    if (ptr) cudaFreeHost(ptr);
+    ptr = p;
+    bytes = want;
+    return HORA_OK;
+  }
+  template <typename T>
+  T *as() const {
+    return static_cast<T *>(ptr);
+  }
+};
+
 struct DevBuf {
   void *ptr = nullptr;
   size_t bytes = 0;

@@ -70,9 +70,11 @@ int search_core(hora_index *h, SearchWorkspace &ws, cudaStream_t s, const float 
 int prepare_for_concurrent_search(hora_index *h);
 int ensure_norms(hora_index *h, cudaStream_t s);
 // Copies nq x dim queries (host or device) into ws.q with pitch h->ld, checks
-// finiteness and computes f32 norms when the metric needs them.
+// finiteness and computes f32 norms when the metric needs them.  With
+// defer_check, the finiteness of device queries is copied to
+// ws.h_status without waiting; the caller reads it after its own sync.
 int stage_queries(hora_index *h, const float *queries, int64_t nq, SearchWorkspace &ws,
-                  cudaStream_t s);
+                  cudaStream_t s, bool defer_check = false);
 
 // Brute force with the handle's precision option; writes nq x k keys.
 int bf_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,

@@ -83,6 +83,10 @@ struct SearchWorkspace {
   // learned nprobe
   DevBuf feats, pred, npq;
   std::vector<uint8_t> h_flags;
+  // the finiteness flag of device queries, read after the search's last sync
+  DevBuf d_status;
+  HostBuf h_status;
+  bool status_pending = false;
 };
 
 struct BaseView {

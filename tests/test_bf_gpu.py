@@ -132,6 +132,16 @@ def test_nan_rejected(hora, gpu):
     ix.build(hora.Metric.Euclidean)
     with pytest.raises(hora.HoraError):
         ix.search([np.inf, 0, 0, 0], 1)
+    # device-resident queries: checked on the device, reported after the search
+    import torch
+    for prec in (0, 1):
+        ix.set_option(hora.Option.PRECISION, prec)
+        bad = torch.tensor([[1.0, 2.0, 3.0, 4.0], [0.0, np.nan, 0.0, 0.0]], device="cuda")
+        with pytest.raises(hora.HoraError) as e:
+            ix.search_batch(bad, 1)
+        assert e.value.code == -5
+        ids, _ = ix.search_batch(bad[:1].clone(), 1)  # the handle keeps working
+        assert int(ids[0, 0]) == 0
 
 
 def test_search_before_build_and_unknown_metric(hora, gpu):
