@@ -148,6 +148,12 @@ class Clocks:
                 "samples": len(sm)}
 
 
+# DRAM traffic of the BF16 scan in one step of the headline form (1M x 128,
+# 10k queries, R = 132: 8 launches), from one ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum: 320.3 MB read + 41.9 MB written.
+SCAN_TRAFFIC_BYTES_PER_STEP = 362.2e6
+
+
 def peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -604,7 +610,12 @@ def run_ours(a, dist: Dist):
         roof["kernel"] = name
         roof["launches"] = nl
         roof["kernel_ms_per_step"] = ms / a.steps
-        roof["traffic"] = None
+        # DRAM bytes of the same kernel's launches, from one ncu capture of
+        # this workload; only the BF16 headline form was captured
+        roof["traffic"] = SCAN_TRAFFIC_BYTES_PER_STEP * a.steps \
+            if name == "bf16_tc_scan" and head == "bf16r132" and not a.small and nq == 10000 else None
+        roof["traffic_unit"] = "bytes per timed region (dram__bytes_read.sum + dram__bytes_write.sum)"
+        roof["algorithmic_bytes"] = (n * (DIM * 2 + 32)) * a.steps if name == "bf16_tc_scan" else None
         roof["share_of_step"] = ms / (t_dev * 1e3)
 
     extras = run_form_extras(a, H, ix, base, q, dq, exact, prec, head_rerank) \
