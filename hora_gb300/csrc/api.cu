@@ -101,18 +101,20 @@ static int check_device_finite(const float *X, int64_t n, int64_t ld, int64_t di
 int stage_queries(hora_index *h, const float *queries, int64_t nq, SearchWorkspace &ws,
                   cudaStream_t s, bool defer_check) {
   const bool dev = is_device_ptr(queries);
-  if (!dev && !host_all_finite(queries, nq * (int64_t)h->dim))
+  if (!dev && !defer_check && !host_all_finite(queries, nq * (int64_t)h->dim))
     return fail(HORA_ENAN, "invalid float element");
   HORA_TRY(ws.q.reserve(sizeof(float) * nq * h->ld));
   if (h->ld != h->dim) HORA_CUDA_TRY(cudaMemsetAsync(ws.q.ptr, 0, sizeof(float) * nq * h->ld, s));
   HORA_CUDA_TRY(cudaMemcpy2DAsync(ws.q.ptr, h->ld * 4, queries, h->dim * 4, h->dim * 4, nq,
                                   cudaMemcpyDefault, s));
-  if (dev && defer_check) {
+  if (defer_check) {
     HORA_TRY(ws.d_status.reserve(sizeof(uint32_t)));
     HORA_TRY(ws.h_status.reserve(sizeof(uint32_t)));
+    HORA_TRY(ws.ev_status.ensure());
     HORA_CUDA_TRY(cudaMemsetAsync(ws.d_status.ptr, 0, sizeof(uint32_t), s));
     HORA_TRY(launch_check_finite(ws.q.as<float>(), nq, h->ld, h->dim, ws.d_status.as<uint32_t>(), s));
     HORA_CUDA_TRY(cudaMemcpyAsync(ws.h_status.ptr, ws.d_status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaEventRecord(ws.ev_status.ev, s));
     ws.status_pending = true;
   } else if (dev) {
     HORA_TRY(check_device_finite(ws.q.as<float>(), nq, h->ld, h->dim, ws.tmp, s));
@@ -368,8 +370,9 @@ int search_core(hora_index *h, SearchWorkspace &ws, cudaStream_t s, const float 
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   int64_t total = (int64_t)(nq * k);
-  // device queries: their finiteness is read after the final sync below, so
-  // the search does not stop for a host round trip before it starts
+  // the queries' finiteness is checked on the device and read only before
+  // the results are written: no host scan of the queries and no host round
+  // trip before the search (the search paths sync on their own by then)
   int rc = stage_queries(h, queries, (int64_t)nq, ws, s, /*defer_check=*/true);
   if (rc == HORA_OK) rc = ws.keys2.reserve(sizeof(uint64_t) * total);
   uint64_t *keys = ws.keys2.as<uint64_t>();
@@ -378,6 +381,13 @@ int search_core(hora_index *h, SearchWorkspace &ws, cudaStream_t s, const float 
       rc = bf_search_keys(h, (int64_t)nq, (int)k, ws, keys, s);
     else
       rc = ivf_search_keys(h, (int64_t)nq, (int)k, (int64_t)nprobe, nullptr, ws, keys, s);
+  }
+  if (ws.status_pending) {
+    ws.status_pending = false;
+    if (cudaEventSynchronize(ws.ev_status.ev) != cudaSuccess && rc == HORA_OK)
+      rc = fail(HORA_ECUDA, "query check");
+    else if (rc == HORA_OK && *ws.h_status.as<uint32_t>())
+      rc = fail(HORA_ENAN, "invalid float element");
   }
   if (rc == HORA_OK) {
     const bool dev_ids = is_device_ptr(ids_out), dev_dist = is_device_ptr(dist_out);
@@ -414,10 +424,6 @@ int search_core(hora_index *h, SearchWorkspace &ws, cudaStream_t s, const float 
   cudaEventRecord(e1, s);
   cudaError_t se = cudaStreamSynchronize(s);
   if (rc == HORA_OK && se != cudaSuccess) rc = fail(HORA_ECUDA, cudaGetErrorString(se));
-  if (ws.status_pending) {
-    ws.status_pending = false;
-    if (rc == HORA_OK && *ws.h_status.as<uint32_t>()) rc = fail(HORA_ENAN, "invalid float element");
-  }
   float ms = 0;
   if (cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) h->last_ms = ms;
   cudaGetLastError();

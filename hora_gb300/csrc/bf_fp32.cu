@@ -185,16 +185,15 @@ int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint
   return HORA_OK;
 }
 
-// Exact FP32 rerank: one thread per candidate walks the dimensions in order
-// (bit-identical to the scan kernel and the reference's scalar loops).
 // Exact FP32 distance of each query's R candidate rows (reference op order:
-// one running sum over the dimensions in order).  One CTA per query; a warp
-// takes 32 candidates at a time and reads their rows 64 dimensions at a time
-// (two rows per coalesced 512-byte load) into a padded shared tile (row
-// stride 65 floats: conflict-free column reads); each lane then sums its own
-// row from the tile in dimension order.
-// One CTA per query with ceil(R / 32) warps (at most kRrMaxWarps), so that
-// R = 132 takes one round of five warps rather than two rounds of four.
+// one running sum over the dimensions in order, bit-identical to the scan
+// kernel and the reference's scalar loops).  One CTA per query with
+// ceil(R / 32) warps (at most kRrMaxWarps), so that R = 132 takes one round of
+// five warps rather than two rounds of four; a warp takes 32 candidates at a
+// time and reads their rows 64 dimensions at a time (two rows per coalesced
+// 512-byte load) into a padded shared tile (row stride 65 floats:
+// conflict-free column reads); each lane then sums its own row from the tile
+// in dimension order.
 constexpr int kRrMaxWarps = 8, kRrSlab = 64;
 template <int MT>
 __global__ void __launch_bounds__(kRrMaxWarps * 32) rerank_exact_kernel(

@@ -153,6 +153,26 @@ struct HostBuf {
   }
 };
 
+// An event created on first use and destroyed with its owner.
+struct EventBox {
+  cudaEvent_t ev = nullptr;
+  EventBox() = default;
+  EventBox(const EventBox &) = delete;
+  EventBox &operator=(const EventBox &) = delete;
+  ~EventBox() {
+    if (ev) cudaEventDestroy(ev);
+  }
+  int ensure() {
+    if (ev) return HORA_OK;
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      ev = nullptr;
+      return fail(HORA_ECUDA, "cudaEventCreate failed");
+    }
+    return HORA_OK;
+  }
+};
+
 struct DevBuf {
   void *ptr = nullptr;
   size_t bytes = 0;

@@ -71,8 +71,9 @@ int prepare_for_concurrent_search(hora_index *h);
 int ensure_norms(hora_index *h, cudaStream_t s);
 // Copies nq x dim queries (host or device) into ws.q with pitch h->ld, checks
 // finiteness and computes f32 norms when the metric needs them.  With
-// defer_check, the finiteness of device queries is copied to
-// ws.h_status without waiting; the caller reads it after its own sync.
+// defer_check, the queries (host or device) are checked on the device and the
+// flag is copied to ws.h_status behind ws.ev_status without waiting; the
+// caller reads it before it writes any result.
 int stage_queries(hora_index *h, const float *queries, int64_t nq, SearchWorkspace &ws,
                   cudaStream_t s, bool defer_check = false);
 

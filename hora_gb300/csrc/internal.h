@@ -83,9 +83,10 @@ struct SearchWorkspace {
   // learned nprobe
   DevBuf feats, pred, npq;
   std::vector<uint8_t> h_flags;
-  // the finiteness flag of device queries, read after the search's last sync
+  // the finiteness flag of the staged queries, read before the results are written
   DevBuf d_status;
   HostBuf h_status;
+  EventBox ev_status;
   bool status_pending = false;
 };
 
