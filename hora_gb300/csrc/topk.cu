@@ -466,6 +466,193 @@ __global__ void __launch_bounds__(kWmWarps * 32, 3) merge_warp_kernel(
   }
 }
 
+// k in (256, 4096]: the warp kernel's scheme with one CTA of 256 threads per
+// query.  Every key is read once; the distance words of up to 12,288 keys
+// stay in registers (48 per thread); the radix select runs on key - kmin
+// with an 11-bit first digit at the top of the key range, on the 32-bit words
+// while the selection stays within them (else on the full keys, re-read);
+// only the winners' full keys are read again.  Shared memory holds the
+// 2,048-bin histogram and the winners (sorted for a final list; otherwise
+// only the largest moves to k - 1).
+constexpr int kMbThreads = 256, kMbRegs = 48, kMbMaxK = 4096;
+
+template <bool SORTED>
+__global__ void __launch_bounds__(kMbThreads, 2) merge_block_kernel(
+    uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n,
+    uint8_t *ovf_flag, uint32_t *ovf_counter) {
+  extern __shared__ uint64_t mb_sel[];  // P >= k winners
+  __shared__ uint32_t hist[kSelBins];
+  __shared__ uint32_t red[3][kMbThreads / 32];
+  __shared__ int sc[8];  // [1] bin, [2] below, [3] taken, [4] remaining, [5] at bin
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t q = blockIdx.x;
+  uint32_t c = dense_n > 0 ? (uint32_t)dense_n : count[q];
+  if (c == 0) return;
+  const bool ovf = c > (uint32_t)cap;
+  if (ovf) c = cap;
+  const uint64_t *cq = cand + q * cap;
+  uint64_t *bq = best + q * k;
+  const int n = (int)c + k;  // <= kMbThreads * kMbRegs: the host checks
+  auto key_at = [&](int i) -> uint64_t { return i < (int)c ? cq[i] : bq[i - c]; };
+
+  // one read of every key: the distance words, live count and range
+  uint32_t hw[kMbRegs];
+#pragma unroll
+  for (int b = 0; b < kMbRegs; b += 8) {
+    uint64_t v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int i = (b + u) * kMbThreads + tid;
+      v[u] = i < n ? key_at(i) : kEmptyKey;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) hw[b + u] = (uint32_t)(v[u] >> 32);
+  }
+  int live = 0;
+  uint32_t hmin = 0xffffffffu, hmax = 0;
+#pragma unroll
+  for (int m = 0; m < kMbRegs; ++m) {
+    const bool ok = hw[m] != 0xffffffffu;
+    live += ok;
+    hmin = min(hmin, hw[m]);
+    hmax = max(hmax, ok ? hw[m] : 0u);
+  }
+  live = __reduce_add_sync(0xffffffffu, live);
+  hmin = __reduce_min_sync(0xffffffffu, hmin);
+  hmax = __reduce_max_sync(0xffffffffu, hmax);
+  if (lane == 0) {
+    red[0][warp] = (uint32_t)live;
+    red[1][warp] = hmin;
+    red[2][warp] = hmax;
+  }
+  for (int b = tid; b < kSelBins; b += kMbThreads) hist[b] = 0;
+  if (tid == 0) sc[3] = 0;
+  __syncthreads();
+  live = 0;
+  hmin = 0xffffffffu;
+  hmax = 0;
+#pragma unroll
+  for (int w = 0; w < kMbThreads / 32; ++w) {
+    live += (int)red[0][w];
+    hmin = min(hmin, red[1][w]);
+    hmax = max(hmax, red[2][w]);
+  }
+  const uint64_t kmin = (uint64_t)hmin << 32, kmax = ((uint64_t)hmax << 32) | 0xffffffffull;
+  const int want = live < k ? live : k;
+  uint64_t bound = kmax - kmin;
+  if (want > 0 && want < live) {
+    const uint64_t span = kmax - kmin;
+    int shift = 64 - __clzll((long long)span) - 11;
+    shift = shift < 0 ? 0 : shift;
+    uint64_t prefix = 0, mask = 0;
+    int rem = want;
+    for (;;) {
+      if (shift >= 32) {
+        const uint32_t mh = (uint32_t)(mask >> 32), ph = (uint32_t)(prefix >> 32);
+        const int sh = shift - 32;
+#pragma unroll
+        for (int m = 0; m < kMbRegs; ++m) {
+          const uint32_t dh = hw[m] - hmin;
+          if (hw[m] != 0xffffffffu && (dh & mh) == ph) atomicAdd(&hist[(dh >> sh) & (kSelBins - 1)], 1u);
+        }
+      } else {
+        for (int i = tid; i < n; i += kMbThreads) {
+          const uint64_t v = key_at(i);
+          const uint64_t d = v - kmin;
+          if (v != kEmptyKey && (d & mask) == prefix)
+            atomicAdd(&hist[(uint32_t)(d >> shift) & (kSelBins - 1)], 1u);
+        }
+      }
+      __syncthreads();
+      if (warp == 0) {
+        warp_find_bin(hist, kSelBins, (uint32_t)rem, sc + 1);
+        __syncwarp();
+        if (lane == 0) {
+          sc[4] = rem - sc[2];
+          sc[5] = (int)hist[sc[1]];
+        }
+      }
+      __syncthreads();
+      const int dd = sc[1], at = sc[5];
+      rem = sc[4];
+      prefix |= (uint64_t)dd << shift;
+      mask |= (uint64_t)(kSelBins - 1) << shift;
+      for (int b = tid; b < kSelBins; b += kMbThreads) hist[b] = 0;
+      __syncthreads();
+      if (at == rem || shift == 0) break;  // every key under this prefix is taken
+      shift = shift >= 11 ? shift - 11 : 0;
+    }
+    // the largest d under the prefix (d has no bits above the first digit)
+    bound = prefix | ((1ull << shift) - 1ull);
+  }
+  if (want > 0) {
+    const unsigned below = (1u << lane) - 1u;
+    if ((uint32_t)bound == 0xffffffffu) {
+      // d <= bound iff hi - hmin <= bound's high word
+      const uint32_t bh = (uint32_t)(bound >> 32);
+#pragma unroll
+      for (int m = 0; m < kMbRegs; ++m) {
+        const bool p = hw[m] != 0xffffffffu && hw[m] - hmin <= bh;
+        const unsigned pm = __ballot_sync(0xffffffffu, p);
+        if (pm) {
+          int base = 0;
+          if (lane == 0) base = atomicAdd(&sc[3], __popc(pm));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          const int slot = base + __popc(pm & below);
+          if (p && slot < want) mb_sel[slot] = key_at(m * kMbThreads + tid);
+        }
+      }
+    } else {
+      for (int i0 = 0; i0 < n; i0 += kMbThreads) {
+        const int i = i0 + tid;
+        const uint64_t v = i < n ? key_at(i) : kEmptyKey;
+        const bool p = v != kEmptyKey && v - kmin <= bound;
+        const unsigned pm = __ballot_sync(0xffffffffu, p);
+        if (pm) {
+          int base = 0;
+          if (lane == 0) base = atomicAdd(&sc[3], __popc(pm));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          const int slot = base + __popc(pm & below);
+          if (p && slot < want) mb_sel[slot] = v;
+        }
+      }
+    }
+    __syncthreads();
+    if (SORTED) {
+      int P = 1;
+      while (P < want) P <<= 1;
+      for (int i = want + tid; i < P; i += kMbThreads) mb_sel[i] = kEmptyKey;
+      __syncthreads();
+      block_bitonic_sort(mb_sel, P);
+    } else if (want == k && warp == 0) {
+      // the largest winner to slot k - 1
+      uint64_t m = 0;
+      int at = -1;
+      for (int i = lane; i < want; i += 32)
+        if (mb_sel[i] >= m) {
+          m = mb_sel[i];
+          at = i;
+        }
+      const uint64_t mx = warp_max_u64(m);
+      const unsigned who = __ballot_sync(0xffffffffu, m == mx && at >= 0);
+      const int src = __shfl_sync(0xffffffffu, at, __ffs(who) - 1);
+      if (lane == 0 && src != want - 1) {
+        mb_sel[src] = mb_sel[want - 1];
+        mb_sel[want - 1] = mx;
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < k; i += kMbThreads) bq[i] = i < want ? mb_sel[i] : kEmptyKey;
+  if (tid == 0) {
+    if (dense_n <= 0) count[q] = 0;
+    if (ovf) {
+      ovf_flag[q] = 1;
+      atomicAdd(ovf_counter, 1u);
+    }
+  }
+}
+
 int merge_smem_bytes(int k, int cap) {
   int P = 1;
   while (P < k + cap) P <<= 1;
@@ -494,6 +681,26 @@ int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *cou
     else
       merge_warp_kernel<false><<<grid, kWmWarps * 32, 0, s>>>(best, k, cand, count, cap, dense_n, nlist,
                                                                   ovf_flag, ovf_counter);
+    HORA_LAUNCHED();
+    return HORA_OK;
+  }
+  if (!qlist && k <= kMbMaxK && cmax + k <= kMbThreads * kMbRegs) {
+    int P = 1;
+    while (P < k) P <<= 1;
+    const int smem = P * 8;
+    static int mb_attr = 0;
+    if (mb_attr < smem && smem > 48 * 1024) {
+      HORA_CUDA_TRY(cudaFuncSetAttribute(merge_block_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      HORA_CUDA_TRY(cudaFuncSetAttribute(merge_block_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      mb_attr = smem;
+    }
+    ProfScope ps("topk_merge", s);
+    if (sorted)
+      merge_block_kernel<true><<<(unsigned)nlist, kMbThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
+                                                                      ovf_flag, ovf_counter);
+    else
+      merge_block_kernel<false><<<(unsigned)nlist, kMbThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
+                                                                       ovf_flag, ovf_counter);
     HORA_LAUNCHED();
     return HORA_OK;
   }
