@@ -277,6 +277,12 @@ def run_ivf(a, H, base, q, exact):
     out = {"workload": "IVFPQIndex 1Mx128 mixture, 1024 lists, 32x8-bit PQ, train 500k, "
                        f"{a.ivf_epochs} epochs, 10k queries, k=10, exact rerank of 100 ADC candidates",
            "build_s": build_s, "sweep": {str(k): v for k, v in sweep.items()}}
+    # per-kernel time of one nprobe-2 search (CUDA events on the library stream)
+    H._lib.profile_report()
+    H._lib.profile(True)
+    ix.search_batch(dq, 10, nprobe=2, ids_out=ids_d, dist_out=dist_d)
+    H._lib.profile(False)
+    out["kernels_nprobe2"] = {k: {"launches": v[0], "ms": v[1]} for k, v in H._lib.profile_report().items()}
     # the reference's CPU search (oracle port, ADC only) on the GPU-built index
     try:
         from oracle import oracle as O

@@ -776,9 +776,113 @@ __global__ void __launch_bounds__(kMergeThreads) rows_topk_kernel(const float *D
   for (int i = threadIdx.x; i < k; i += blockDim.x) out[r * k + i] = sk[i];
 }
 
+// The k smallest (distance, column) keys of each row, ascending, for rows of
+// up to 32 x kWmRegs columns and k <= 256: one warp per row, the merge
+// kernel's scheme with every key in registers (the distance word, and the
+// column implied by the register's place), one read of the row, a radix
+// select from the top of the row's key range and a warp sort of the winners.
+__global__ void __launch_bounds__(kWmWarps * 32) rows_select_warp_kernel(const float *D, int64_t rows,
+                                                                        int cols, int64_t ldd, int k,
+                                                                        uint64_t *out) {
+  __shared__ uint32_t hist_all[kWmWarps][256];
+  __shared__ uint64_t sel_all[kWmWarps][kWmMaxK];
+  __shared__ int dig_all[kWmWarps][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r = (int64_t)blockIdx.x * kWmWarps + warp;
+  if (r >= rows) return;
+  uint32_t *hist = hist_all[warp];
+  uint64_t *sel = sel_all[warp];
+  int *dig = dig_all[warp];
+  uint32_t hw[kWmRegs];
+#pragma unroll
+  for (int m = 0; m < kWmRegs; ++m) {
+    const int i = m * 32 + lane;
+    hw[m] = i < cols ? f2ord(D[r * ldd + i]) : 0xffffffffu;
+  }
+  int live = 0;
+  uint32_t hmin = 0xffffffffu, hmax = 0;
+#pragma unroll
+  for (int m = 0; m < kWmRegs; ++m) {
+    const bool ok = hw[m] != 0xffffffffu;
+    live += ok;
+    hmin = min(hmin, hw[m]);
+    hmax = max(hmax, ok ? hw[m] : 0u);
+  }
+  live = __reduce_add_sync(0xffffffffu, live);
+  hmin = __reduce_min_sync(0xffffffffu, hmin);
+  hmax = __reduce_max_sync(0xffffffffu, hmax);
+  const uint64_t kmin = (uint64_t)hmin << 32, kmax = ((uint64_t)hmax << 32) | 0xffffffffull;
+  const int want = live < k ? live : k;
+  uint64_t bound = kmax - kmin;
+  if (want > 0 && want < live) {
+    const uint64_t span = kmax - kmin;
+    int shift = 64 - __clzll((long long)span) - 8;
+    shift = shift < 0 ? 0 : shift;
+    uint64_t prefix = 0, mask = 0;
+    int rem = want;
+    for (;;) {
+      for (int b = lane; b < 256; b += 32) hist[b] = 0;
+      __syncwarp();
+      if (shift >= 32) {
+        const uint32_t mh = (uint32_t)(mask >> 32), ph = (uint32_t)(prefix >> 32);
+        const int sh = shift - 32;
+#pragma unroll
+        for (int m = 0; m < kWmRegs; ++m) {
+          const uint32_t dh = hw[m] - hmin;
+          if (hw[m] != 0xffffffffu && (dh & mh) == ph) atomicAdd(&hist[(dh >> sh) & 255u], 1u);
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < kWmRegs; ++m) {
+          const uint64_t d = ((((uint64_t)hw[m]) << 32) | (uint32_t)(m * 32 + lane)) - kmin;
+          if (hw[m] != 0xffffffffu && (d & mask) == prefix) atomicAdd(&hist[(uint32_t)(d >> shift) & 255u], 1u);
+        }
+      }
+      __syncwarp();
+      warp_find_digit(hist, (uint32_t)rem, dig);
+      __syncwarp();
+      const int dd = dig[0], at = (int)hist[dd];
+      rem -= dig[1];
+      prefix |= (uint64_t)dd << shift;
+      mask |= (uint64_t)0xff << shift;
+      __syncwarp();
+      if (at == rem || shift == 0) break;
+      shift = shift >= 8 ? shift - 8 : 0;
+    }
+    bound = prefix | ((1ull << shift) - 1ull);
+  }
+  if (want > 0) {
+    int taken = 0;
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int m = 0; m < kWmRegs; ++m) {
+      const uint64_t key = (((uint64_t)hw[m]) << 32) | (uint32_t)(m * 32 + lane);
+      const bool p = hw[m] != 0xffffffffu && key - kmin <= bound;
+      const unsigned pm = __ballot_sync(0xffffffffu, p);
+      const int slot = taken + __popc(pm & below);
+      if (p && slot < want) sel[slot] = key;
+      taken += __popc(pm);
+    }
+    int P = 1;
+    while (P < want) P <<= 1;
+    __syncwarp();
+    for (int i = want + lane; i < P; i += 32) sel[i] = kEmptyKey;
+    __syncwarp();
+    warp_bitonic_sort(sel, P);
+  }
+  for (int i = lane; i < k; i += 32) out[r * k + i] = i < want ? sel[i] : kEmptyKey;
+}
+
 int launch_rows_topk(const float *D, int64_t rows, int64_t cols, int64_t ldd, int k,
                      uint64_t *out, cudaStream_t s) {
   if (rows <= 0) return HORA_OK;
+  if (k <= kWmMaxK && cols <= 32 * kWmRegs) {
+    ProfScope ps("rows_topk", s);
+    rows_select_warp_kernel<<<(unsigned)ceil_div(rows, (int64_t)kWmWarps), kWmWarps * 32, 0, s>>>(
+        D, rows, (int)cols, ldd, k, out);
+    HORA_LAUNCHED();
+    return HORA_OK;
+  }
   int P = 1;
   while (P < cols || P < k) P <<= 1;
   if (P * 8 > 200 * 1024) return fail(HORA_ECAP, "rows_topk: too many columns");
