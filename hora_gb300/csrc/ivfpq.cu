@@ -595,47 +595,59 @@ __global__ void pair_scatter_kernel(const uint64_t *probes, int64_t nq, int pmax
   pslot[pos] = (uint32_t)j;
 }
 
-// CTA-wide selection of the k smallest of L 32-bit order keys held in smem:
-// radix select on 11/11/10-bit digits whose histogram updates are
-// aggregated per warp (one shared atomic per distinct digit and warp
-// instruction, so keys crowded into one digit do not serialise); ties at the
-// k-th key go to the lowest positions.  sel receives the k positions
+// CTA-wide selection of the k smallest of L 32-bit order keys held in smem.
+// The keys' range [kmin, kmax] comes first; the radix select then runs on
+// key - kmin with its first 11-bit digit at the top of that range (plain
+// shared atomics: the keys spread over the bins) and stops as soon as the
+// k-th key's bin is taken whole; otherwise it resolves the k-th key exactly
+// and ties at it go to the lowest positions.  sel receives the k positions
 // (unordered).  L and k are uniform, 0 < k < L.  hist: kSelBins u32, zero on
 // entry and on return; scratch: 48 ints.
 __device__ void cta_select_k(const uint32_t *keys, int L, int k, int *sel, uint32_t *hist,
                              int *scratch) {
-  // scratch: [0] remaining k, [1] digit, [2] below, [3] taken, [5] count at the k-th key,
-  // [8..8+nwarps) scan
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // scratch: [0] remaining k, [1] digit, [2] below, [3] taken, [5] count at the digit,
+  // [8..16) scan, [16..24) / [24..32) per-warp minima / maxima
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  uint32_t lo = 0xffffffffu, hi = 0;
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    const uint32_t v = keys[i];
+    lo = min(lo, v);
+    hi = max(hi, v);
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  if (lane == 0) {
+    scratch[16 + warp] = (int)lo;
+    scratch[24 + warp] = (int)hi;
+  }
   if (threadIdx.x == 0) {
     scratch[0] = k;
     scratch[3] = 0;
   }
   __syncthreads();
+  uint32_t kmin = 0xffffffffu, kmax = 0;
+  for (int x = 0; x < nwarp; ++x) {
+    kmin = min(kmin, (uint32_t)scratch[16 + x]);
+    kmax = max(kmax, (uint32_t)scratch[24 + x]);
+  }
+  int shift = 32 - __clz((int)(kmax - kmin)) - 11;  // __clz(0) = 32
+  shift = shift < 0 ? 0 : shift;
   uint32_t prefix = 0, mask = 0;
-  for (int pass = 0; pass < 3; ++pass) {
-    const int shift = pass == 0 ? 21 : pass == 1 ? 10 : 0;
-    const uint32_t dmask = pass == 2 ? 1023u : 2047u;
-    for (int i0 = 0; i0 < L; i0 += blockDim.x) {
-      const int i = i0 + threadIdx.x;
-      const uint32_t v = i < L ? keys[i] : 0u;
-      const bool p = i < L && (v & mask) == prefix;
-      const unsigned pm = __ballot_sync(0xffffffffu, p);
-      if (p) {
-        const uint32_t dig = (v >> shift) & dmask;
-        const unsigned peers = __match_any_sync(pm, dig);
-        if (lane == __ffs(peers) - 1) atomicAdd(&hist[dig], (uint32_t)__popc(peers));
-      }
+  bool whole = false;
+  for (;;) {
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+      const uint32_t d = keys[i] - kmin;
+      if ((d & mask) == prefix) atomicAdd(&hist[(d >> shift) & (kSelBins - 1)], 1u);
     }
     __syncthreads();
     if (warp == 0) {
-      warp_find_bin(hist, (int)dmask + 1, (uint32_t)scratch[0], scratch + 1);
+      warp_find_bin(hist, kSelBins, (uint32_t)scratch[0], scratch + 1);
       __syncwarp();
       const int d = scratch[1];
       const uint32_t at_d = hist[d];
       const int below = scratch[2];
       __syncwarp();
-      for (int b = lane; b <= (int)dmask; b += 32) hist[b] = 0;
+      for (int b = lane; b < kSelBins; b += 32) hist[b] = 0;
       if (lane == 0) {
         scratch[0] -= below;
         scratch[5] = (int)at_d;
@@ -643,8 +655,32 @@ __device__ void cta_select_k(const uint32_t *keys, int L, int k, int *sel, uint3
     }
     __syncthreads();
     prefix |= (uint32_t)scratch[1] << shift;
-    mask |= dmask << shift;
+    mask |= (uint32_t)(kSelBins - 1) << shift;
+    if (scratch[5] == scratch[0]) {  // every key in this bin is taken
+      whole = true;
+      break;
+    }
+    if (shift == 0) break;
+    shift = shift >= 11 ? shift - 11 : 0;
   }
+  if (whole) {
+    // exactly k keys lie at or below the bin's largest d
+    const uint32_t bound = prefix | ((1u << shift) - 1u);
+    for (int i0 = 0; i0 < L; i0 += blockDim.x) {
+      const int i = i0 + threadIdx.x;
+      const bool p = i < L && keys[i] - kmin <= bound;
+      const unsigned pm = __ballot_sync(0xffffffffu, p);
+      if (pm) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&scratch[3], __popc(pm));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (p) sel[base + __popc(pm & ((1u << lane) - 1u))] = i;
+      }
+    }
+    __syncthreads();
+    return;
+  }
+  prefix += kmin;  // the k-th key itself
   const uint32_t kth = prefix;
   const int need_eq = scratch[0];  // keys equal to kth that are taken (>= 1)
   const bool all_eq = scratch[5] == need_eq;
