@@ -840,7 +840,33 @@ __global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
       zq[t] = __fsub_rn(Q[q * ldq + t], centers[(int64_t)c * ldc + t]);
     __syncthreads();
     const float *book = books + (int64_t)c * M * K * DM;
-    if (mt == M_L2) {
+    if (DM == 4 && mt == M_L2) {
+      // 8 codewords' loads in flight per thread before any entry is computed
+      const float4 *b4 = reinterpret_cast<const float4 *>(book);
+      const int MK = M * K;
+      for (int e0 = threadIdx.x; e0 < MK; e0 += 8 * kAdcThreads) {
+        float4 cv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int e = e0 + u * kAdcThreads;
+          if (e < MK) cv[u] = __ldg(b4 + e);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int e = e0 + u * kAdcThreads;
+          if (e < MK) {
+            const int m = e >> kbits, len = sls[m];
+            const float *z = zq + sbs[m];
+            const float cw[4] = {cv[u].x, cv[u].y, cv[u].z, cv[u].w};
+            float acc = 0.0f;
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+              if (t < len) acc = dist_op<M_L2>(acc, z[t], cw[t]);
+            lut[e] = acc;
+          }
+        }
+      }
+    } else if (mt == M_L2) {
       for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
         const int m = e >> kbits;
         lut[e] = lut_entry<M_L2, DM>(book + (int64_t)e * DM, zq + sbs[m], sls[m]);
