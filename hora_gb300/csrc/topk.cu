@@ -493,12 +493,14 @@ __global__ void __launch_bounds__(kMbThreads, 2) merge_block_kernel(
   const uint64_t *cq = cand + q * cap;
   uint64_t *bq = best + q * k;
   const int n = (int)c + k;  // <= kMbThreads * kMbRegs: the host checks
+  const int nm = (n + kMbThreads - 1) / kMbThreads;  // register slots in use (uniform)
   auto key_at = [&](int i) -> uint64_t { return i < (int)c ? cq[i] : bq[i - c]; };
 
   // one read of every key: the distance words, live count and range
   uint32_t hw[kMbRegs];
 #pragma unroll
   for (int b = 0; b < kMbRegs; b += 8) {
+    if (b >= nm) break;
     uint64_t v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -512,6 +514,7 @@ __global__ void __launch_bounds__(kMbThreads, 2) merge_block_kernel(
   uint32_t hmin = 0xffffffffu, hmax = 0;
 #pragma unroll
   for (int m = 0; m < kMbRegs; ++m) {
+    if (m >= nm) break;
     const bool ok = hw[m] != 0xffffffffu;
     live += ok;
     hmin = min(hmin, hw[m]);
@@ -552,6 +555,7 @@ __global__ void __launch_bounds__(kMbThreads, 2) merge_block_kernel(
         const int sh = shift - 32;
 #pragma unroll
         for (int m = 0; m < kMbRegs; ++m) {
+          if (m >= nm) break;
           const uint32_t dh = hw[m] - hmin;
           if (hw[m] != 0xffffffffu && (dh & mh) == ph) atomicAdd(&hist[(dh >> sh) & (kSelBins - 1)], 1u);
         }
@@ -592,6 +596,7 @@ __global__ void __launch_bounds__(kMbThreads, 2) merge_block_kernel(
       const uint32_t bh = (uint32_t)(bound >> 32);
 #pragma unroll
       for (int m = 0; m < kMbRegs; ++m) {
+        if (m >= nm) break;
         const bool p = hw[m] != 0xffffffffu && hw[m] - hmin <= bh;
         const unsigned pm = __ballot_sync(0xffffffffu, p);
         if (pm) {
