@@ -313,6 +313,7 @@ __global__ void __launch_bounds__(kWmWarps * 32, 3) merge_warp_kernel(
   const int n = (int)c + k;
   auto key_at = [&](int i) -> uint64_t { return i < (int)c ? cq[i] : bq[i - c]; };
   const bool inreg = n <= 32 * kWmRegs;
+  const int nm = (n + 31) >> 5;  // register slots in use (uniform in the warp)
 
   // one read of every key: live count and the range of the high words (no
   // live key has the empty key's high word 0xffffffff, which is the largest)
@@ -322,6 +323,7 @@ __global__ void __launch_bounds__(kWmWarps * 32, 3) merge_warp_kernel(
   if (inreg) {
 #pragma unroll
     for (int b = 0; b < kWmRegs; b += 8) {
+      if (b >= nm) break;
       uint64_t v[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
@@ -333,6 +335,7 @@ __global__ void __launch_bounds__(kWmWarps * 32, 3) merge_warp_kernel(
     }
 #pragma unroll
     for (int m = 0; m < kWmRegs; ++m) {
+      if (m >= nm) break;
       const bool ok = hw[m] != 0xffffffffu;
       live += ok;
       hmin = min(hmin, hw[m]);
@@ -372,6 +375,7 @@ __global__ void __launch_bounds__(kWmWarps * 32, 3) merge_warp_kernel(
         if (inreg) {
 #pragma unroll
           for (int m = 0; m < kWmRegs; ++m) {
+            if (m >= nm) break;
             const uint32_t dh = hw[m] - hmin;
             if (hw[m] != 0xffffffffu && (dh & mh) == ph) atomicAdd(&hist[(dh >> sh) & 255u], 1u);
           }
@@ -413,6 +417,7 @@ __global__ void __launch_bounds__(kWmWarps * 32, 3) merge_warp_kernel(
       const uint32_t bh = (uint32_t)(bound >> 32);
 #pragma unroll
       for (int m = 0; m < kWmRegs; ++m) {
+        if (m >= nm) break;
         const bool p = hw[m] != 0xffffffffu && hw[m] - hmin <= bh;
         const unsigned pm = __ballot_sync(0xffffffffu, p);
         const int slot = taken + __popc(pm & below);
@@ -798,9 +803,11 @@ __global__ void __launch_bounds__(kWmWarps * 32) rows_select_warp_kernel(const f
   uint32_t *hist = hist_all[warp];
   uint64_t *sel = sel_all[warp];
   int *dig = dig_all[warp];
+  const int nm = (cols + 31) >> 5;  // register slots in use (uniform)
   uint32_t hw[kWmRegs];
 #pragma unroll
   for (int m = 0; m < kWmRegs; ++m) {
+    if (m >= nm) break;
     const int i = m * 32 + lane;
     hw[m] = i < cols ? f2ord(D[r * ldd + i]) : 0xffffffffu;
   }
@@ -808,6 +815,7 @@ __global__ void __launch_bounds__(kWmWarps * 32) rows_select_warp_kernel(const f
   uint32_t hmin = 0xffffffffu, hmax = 0;
 #pragma unroll
   for (int m = 0; m < kWmRegs; ++m) {
+    if (m >= nm) break;
     const bool ok = hw[m] != 0xffffffffu;
     live += ok;
     hmin = min(hmin, hw[m]);
@@ -833,12 +841,14 @@ __global__ void __launch_bounds__(kWmWarps * 32) rows_select_warp_kernel(const f
         const int sh = shift - 32;
 #pragma unroll
         for (int m = 0; m < kWmRegs; ++m) {
+          if (m >= nm) break;
           const uint32_t dh = hw[m] - hmin;
           if (hw[m] != 0xffffffffu && (dh & mh) == ph) atomicAdd(&hist[(dh >> sh) & 255u], 1u);
         }
       } else {
 #pragma unroll
         for (int m = 0; m < kWmRegs; ++m) {
+          if (m >= nm) break;
           const uint64_t d = ((((uint64_t)hw[m]) << 32) | (uint32_t)(m * 32 + lane)) - kmin;
           if (hw[m] != 0xffffffffu && (d & mask) == prefix) atomicAdd(&hist[(uint32_t)(d >> shift) & 255u], 1u);
         }
@@ -861,6 +871,7 @@ __global__ void __launch_bounds__(kWmWarps * 32) rows_select_warp_kernel(const f
     const unsigned below = (1u << lane) - 1u;
 #pragma unroll
     for (int m = 0; m < kWmRegs; ++m) {
+      if (m >= nm) break;
       const uint64_t key = (((uint64_t)hw[m]) << 32) | (uint32_t)(m * 32 + lane);
       const bool p = hw[m] != 0xffffffffu && key - kmin <= bound;
       const unsigned pm = __ballot_sync(0xffffffffu, p);
