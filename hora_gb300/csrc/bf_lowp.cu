@@ -155,6 +155,13 @@ __device__ __forceinline__ float drain_dist(uint32_t bits, float qa) {
   return !RAW ? a : MT == M_L2 ? fmaf(-2.0f, a, qa) : (MT == M_IP ? a : -a);
 }
 
+// One 32-byte store (four keys) to a 32-byte aligned address.
+__device__ __forceinline__ void st_global_32b(uint64_t *dst, const uint64_t (&k)[4]) {
+  asm volatile("st.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(dst), "l"(k[0]), "l"(k[1]), "l"(k[2]),
+               "l"(k[3])
+               : "memory");
+}
+
 // Appends the staged keys to the query's list: one atomic reserves the slots.
 __device__ __forceinline__ void flush_hits(const DrainCtx &c, int &nb) {
   uint32_t slot = atomicAdd(c.count + c.qid, (uint32_t)nb);
@@ -170,14 +177,15 @@ __device__ __forceinline__ void drain_mask(const uint32_t (&v)[32], uint32_t hit
   if constexpr (MODE == TILE_DENSE) {
     uint64_t *out = c.cand + c.qid * c.cap + (c.rt - c.r_begin);
     if (c.rt + 32 <= c.r_end) {
-      // a whole slice: 16-byte pair stores (cap is a multiple of 128 and a
-      // slice starts 32 rows into the chunk, so `out` is 16-byte aligned)
+      // a whole slice: 32-byte stores, one full sector each (cap is a
+      // multiple of 128 and a slice starts a multiple of 32 rows into the
+      // chunk, so `out` is 32-byte aligned)
 #pragma unroll
-      for (int j = 0; j < 32; j += 2) {
-        ulonglong2 kv;
-        kv.x = make_key(drain_dist<MT, MODE, RAW>(v[j], c.qa), (uint32_t)(c.rt + j));
-        kv.y = make_key(drain_dist<MT, MODE, RAW>(v[j + 1], c.qa), (uint32_t)(c.rt + j + 1));
-        *reinterpret_cast<ulonglong2 *>(out + j) = kv;
+      for (int j = 0; j < 32; j += 4) {
+        uint64_t kv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) kv[u] = make_key(drain_dist<MT, MODE, RAW>(v[j + u], c.qa), (uint32_t)(c.rt + j + u));
+        st_global_32b(out + j, kv);
       }
     } else {
 #pragma unroll
