@@ -77,6 +77,7 @@ struct LpParams {
   int cap;
   uint32_t *count;
   int *err;
+  int dense_hits;  // hit-dense launch: the warp-converged staging (stage_hits)
 };
 
 // BF16 Euclidean folds the row norm into the MMA: one extra K = 16 step
@@ -205,6 +206,58 @@ __device__ __forceinline__ void drain_mask(const uint32_t (&v)[32], uint32_t hit
       c.hb[nb * kLpEpiThreads] = make_key(d, (uint32_t)row);
       if (++nb == kLpHitBuf) flush_hits(c, nb);
     }
+  }
+}
+
+// A slice's hits in the BF16 filter drain, called by the whole warp
+// (converged).  Lanes whose staging column cannot take this slice's hits
+// flush it first, all together: one atomic round trip for the warp instead of
+// one per lane at different points of a divergent loop.  A lane with more
+// hits than the column holds reserves slots for the keys that pass the exact
+// key test and stores them directly (only accepted keys are counted, so an
+// overflow rescan still makes progress through runs of ties).  The staged loop itself
+// never flushes; a full column waits for the next slice or the end of the CTA.
+template <int MT>
+__device__ __forceinline__ void stage_hits(const uint32_t (&v)[32], uint32_t hits, const DrainCtx &c,
+                                           int &nb) {
+  const int nh = __popc(hits);
+  const bool big = nh > kLpHitBuf;
+  const bool must = !big && nb + nh > kLpHitBuf;
+  if (__any_sync(0xffffffffu, must)) {
+    if (must) flush_hits(c, nb);
+  }
+  if (__any_sync(0xffffffffu, big)) {
+    if (big) {
+      uint32_t acc = 0;
+      for (uint32_t h = hits; h;) {
+        const int j = __ffs(h) - 1;
+        h &= h - 1;
+        const int64_t row = c.rt + j;
+        const float d = drain_dist<MT, TILE_FILTER, true>(pick32(v, j), c.qa);
+        if (row < c.r_end && (d < c.tau_d || (d == c.tau_d && (uint32_t)row < c.tau_r))) acc |= 1u << j;
+      }
+      const int na = __popc(acc);
+      uint32_t slot = na ? atomicAdd(c.count + c.qid, (uint32_t)na) : 0u;
+      uint64_t *out = c.cand + c.qid * c.cap;
+      while (acc) {
+        const int j = __ffs(acc) - 1;
+        acc &= acc - 1;
+        const float d = drain_dist<MT, TILE_FILTER, true>(pick32(v, j), c.qa);
+        if (slot < (uint32_t)c.cap) out[slot] = make_key(d, (uint32_t)(c.rt + j));
+        ++slot;
+      }
+    }
+  }
+  if (big) return;
+  while (hits) {
+    const int j = __ffs(hits) - 1;
+    hits &= hits - 1;
+    const int64_t row = c.rt + j;
+    if (row >= c.r_end) continue;
+    const float d = drain_dist<MT, TILE_FILTER, true>(pick32(v, j), c.qa);
+    if (!(d < c.tau_d || (d == c.tau_d && (uint32_t)row < c.tau_r))) continue;
+    c.hb[nb * kLpEpiThreads] = make_key(d, (uint32_t)row);
+    ++nb;
   }
 }
 
@@ -391,14 +444,27 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         tc::mbar_arrive(acc_empty + b);
       }
       if (FAST) {
-        if (qid < 0) continue;
         if constexpr (MODE == TILE_DENSE) {
-          drain_mask<MT, MODE, true>(v, 0xffffffffu, c, nb);
+          if (qid >= 0) drain_mask<MT, MODE, true>(v, 0xffffffffu, c, nb);
         } else {
           // the slice's extreme decides whether any column can hit; the
-          // hit mask is built only then
+          // hit mask is built only then (padded query rows never hit)
           const float ext = slice_extreme<MT == M_IP>(v);
-          if (MT == M_IP ? ext <= thr : ext >= thr) {
+          const bool maybe = qid >= 0 && (MT == M_IP ? ext <= thr : ext >= thr);
+          if (p.dense_hits) {
+            // many hits per slice: flushes converged across the warp
+            if (__any_sync(0xffffffffu, maybe)) {
+              uint32_t hits = 0;
+              if (maybe) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                  const float a = __uint_as_float(v[j]);
+                  hits |= (uint32_t)(MT == M_IP ? a <= thr : a >= thr) << j;
+                }
+              }
+              stage_hits<MT>(v, hits, c, nb);
+            }
+          } else if (maybe) {
             uint32_t hits = 0;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
@@ -759,6 +825,9 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     c = std::min<int64_t>(round_up(c, kLpBN), std::min<int64_t>(n - done, max_chunk));
     p.r_begin = done;
     p.r_end = done + c;
+    // expected hits per drain thread and CTA, R x (rows per CTA / 4) / done:
+    // from about 20 on, warp-converged flushes beat per-lane ones
+    p.dense_hits = (double)R * (kLpBN * kLpTilesPerCta / 4) / (double)done >= 20.0;
     HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, ta, L, p, s));
     HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s, false));
     done += c;
@@ -804,6 +873,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     LpParams r = p;
     r.nq = nl;
     r.qmap = ws.qlist.as<int>();
+    r.dense_hits = 0;
     for (int64_t lo = 0; lo < n; lo += max_chunk) {
       r.r_begin = lo;
       r.r_end = std::min<int64_t>(n, lo + max_chunk);
