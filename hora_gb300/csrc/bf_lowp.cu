@@ -817,11 +817,12 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   int64_t done = c0;
   const int64_t max_chunk = (int64_t)60000 * kLpBN * kLpTilesPerCta;
   while (done < n) {
-    // each chunk at most 1.5x the rows scanned so far: a hit costs the drain
-    // more than the merge a smaller chunk adds (measured on 1M x 128, R = 132)
+    // each chunk at most 1.5x the rows scanned so far and at least 2,048
+    // rows: a hit costs the drain more than the merge a smaller chunk adds
+    // (measured on 1M x 128, R = 132)
     double grow = std::min((double)cap / (4.0 * R), 1.5);
     int64_t c = (int64_t)((double)done * std::max(grow, 1.0));
-    c = std::max<int64_t>(c, (int64_t)4096);
+    c = std::max<int64_t>(c, (int64_t)2048);
     c = std::min<int64_t>(round_up(c, kLpBN), std::min<int64_t>(n - done, max_chunk));
     p.r_begin = done;
     p.r_end = done + c;
