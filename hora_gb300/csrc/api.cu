@@ -104,26 +104,37 @@ int stage_queries(hora_index *h, const float *queries, int64_t nq, SearchWorkspa
   if (!dev && !defer_check && !host_all_finite(queries, nq * (int64_t)h->dim))
     return fail(HORA_ENAN, "invalid float element");
   HORA_TRY(ws.q.reserve(sizeof(float) * nq * h->ld));
-  if (h->ld != h->dim) HORA_CUDA_TRY(cudaMemsetAsync(ws.q.ptr, 0, sizeof(float) * nq * h->ld, s));
-  HORA_CUDA_TRY(cudaMemcpy2DAsync(ws.q.ptr, h->ld * 4, queries, h->dim * 4, h->dim * 4, nq,
-                                  cudaMemcpyDefault, s));
-  if (defer_check) {
+  // host queries come over in one pitched copy and are staged in place;
+  // device queries are read where they are
+  if (!dev)
+    HORA_CUDA_TRY(cudaMemcpy2DAsync(ws.q.ptr, h->ld * 4, queries, h->dim * 4, h->dim * 4, nq,
+                                    cudaMemcpyHostToDevice, s));
+  float *qn = nullptr;
+  double *qsq = nullptr;
+  if (h->metric == M_COS || h->precision != HORA_PREC_FP32) {
+    HORA_TRY(ws.qnorm.reserve(sizeof(float) * nq + sizeof(double) * nq + 16));
+    qn = ws.qnorm.as<float>();
+    qsq = reinterpret_cast<double *>(ws.qnorm.as<char>() + round_up(sizeof(float) * nq, 16));
+  }
+  uint32_t *flag = nullptr;
+  if (defer_check || dev) {
     HORA_TRY(ws.d_status.reserve(sizeof(uint32_t)));
+    flag = ws.d_status.as<uint32_t>();
+    HORA_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(uint32_t), s));
+  }
+  HORA_TRY(launch_stage_rows(dev ? queries : ws.q.as<float>(), dev ? h->dim : h->ld, nq, h->dim, h->ld,
+                             ws.q.as<float>(), flag, qn, qsq, s));
+  if (defer_check) {
     HORA_TRY(ws.h_status.reserve(sizeof(uint32_t)));
     HORA_TRY(ws.ev_status.ensure());
-    HORA_CUDA_TRY(cudaMemsetAsync(ws.d_status.ptr, 0, sizeof(uint32_t), s));
-    HORA_TRY(launch_check_finite(ws.q.as<float>(), nq, h->ld, h->dim, ws.d_status.as<uint32_t>(), s));
-    HORA_CUDA_TRY(cudaMemcpyAsync(ws.h_status.ptr, ws.d_status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaMemcpyAsync(ws.h_status.ptr, flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     HORA_CUDA_TRY(cudaEventRecord(ws.ev_status.ev, s));
     ws.status_pending = true;
   } else if (dev) {
-    HORA_TRY(check_device_finite(ws.q.as<float>(), nq, h->ld, h->dim, ws.tmp, s));
-  }
-  if (h->metric == M_COS || h->precision != HORA_PREC_FP32) {
-    HORA_TRY(ws.qnorm.reserve(sizeof(float) * nq + sizeof(double) * nq + 16));
-    float *qn = ws.qnorm.as<float>();
-    double *qsq = reinterpret_cast<double *>(ws.qnorm.as<char>() + round_up(sizeof(float) * nq, 16));
-    HORA_TRY(launch_row_norms(ws.q.as<float>(), nq, h->ld, h->dim, qn, qsq, s));
+    uint32_t bad = 0;
+    HORA_CUDA_TRY(cudaMemcpyAsync(&bad, flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+    if (bad) return fail(HORA_ENAN, "invalid float element");
   }
   return HORA_OK;
 }

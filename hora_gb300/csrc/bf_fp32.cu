@@ -162,6 +162,39 @@ int launch_row_norms(const float *X, int64_t n, int64_t ld, int64_t dim, float *
   return HORA_OK;
 }
 
+// Query staging in one pass: each thread copies its row from src (pitch
+// lds) to dst (pitch ld, zero padding; src may alias dst), flags a NaN / Inf
+// element and computes the norms in the same order as row_norms_kernel.
+__global__ void stage_rows_kernel(const float *src, int64_t lds, int64_t n, int64_t dim, int64_t ld,
+                                  float *dst, uint32_t *flag, float *nf, double *sq) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const float *x = src + r * lds;
+  float *y = dst + r * ld;
+  float s = 0.0f;
+  double s64 = 0.0;
+  bool bad = false;
+  for (int64_t t = 0; t < dim; ++t) {
+    const float v = x[t];
+    y[t] = v;
+    bad |= !isfinite(v);
+    s = __fadd_rn(s, __fmul_rn(v, v));
+    s64 += (double)v * (double)v;
+  }
+  for (int64_t t = dim; t < ld; ++t) y[t] = 0.0f;
+  if (bad && flag) atomicOr(flag, 1u);
+  if (nf) nf[r] = __fsqrt_rn(s);
+  if (sq) sq[r] = s64;
+}
+
+int launch_stage_rows(const float *src, int64_t lds, int64_t n, int64_t dim, int64_t ld, float *dst,
+                      uint32_t *flag, float *nf, double *sq, cudaStream_t s) {
+  if (n <= 0) return HORA_OK;
+  stage_rows_kernel<<<ceil_div(n, 128), 128, 0, s>>>(src, lds, n, dim, ld, dst, flag, nf, sq);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
 __global__ void check_finite_kernel(const float *X, int64_t n, int64_t ld, int64_t dim,
                                     uint32_t *flag) {
   int64_t total = n * dim;

@@ -39,6 +39,11 @@ struct TileParams {
 };
 
 int launch_dist_tile(int metric, int mode, const TileParams &p, cudaStream_t s);
+// Copies n rows (src pitch lds, may alias dst) to dst (pitch ld, zero
+// padding), raises *flag on a NaN / Inf element and writes the row norms
+// (f32 and f64 squares, either may be null), in one pass.
+int launch_stage_rows(const float *src, int64_t lds, int64_t n, int64_t dim, int64_t ld, float *dst,
+                      uint32_t *flag, float *nf, double *sq, cudaStream_t s);
 int launch_row_norms(const float *X, int64_t n, int64_t ld, int64_t dim, float *norm_f32,
                      double *sq_f64, cudaStream_t s);
 int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint32_t *flag,
