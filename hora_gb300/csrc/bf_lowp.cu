@@ -51,14 +51,19 @@ constexpr int kLpMaxStages = 8;
 constexpr int kLpHitBuf = 8;
 constexpr int kLpHitBytes = kLpHitBuf * kLpEpiThreads * 8;
 
+// The low-precision base is kept as the shared-memory image of each 256-row
+// base tile, tile after tile: its K blocks (256 rows x 128 bytes each, the
+// 16-byte chunks of row r permuted by chunk ^ (r % 8): the 128-byte swizzle
+// the MMA descriptors read), then for BF16 Euclidean the two 8-column halves
+// of the norm block (256 rows x 16 bytes each, unswizzled).  One bulk copy
+// moves a whole tile into a ring stage; rows past n are zero.
 struct LowpState {
   int prec = 0, metric = 0;
   int64_t n = 0, Dp = 0;
-  DevBuf base;     // n x Dp (bf16 or e4m3); unit rows for BF16 cosine
+  DevBuf tiles;    // ceil(n / 256) x tile_bytes
+  int64_t tile_bytes = 0;
   DevBuf xsq;      // n f32 exact squared norms
   DevBuf xscale;   // n f32 (e4m3 per-row scale)
-  DevBuf normblk;  // BF16 Euclidean: n x 16 bf16, -|x|^2/2 in three parts
-  CUtensorMap tmap_b, tmap_n;
 };
 
 void lowp_state_free(LowpState *p) { delete p; }
@@ -66,6 +71,7 @@ void lowp_state_free(LowpState *p) { delete p; }
 struct LpParams {
   int64_t nq;
   const int *qmap;
+  const uint8_t *tiles;  // the base's tile image (see LowpState)
   int64_t r_begin, r_end;
   int nkb;        // 128-byte K blocks per row (1 or 2)
   int stages;     // base-tile ring depth
@@ -263,9 +269,7 @@ __device__ __forceinline__ void stage_hits(const uint32_t (&v)[32], uint32_t hit
 
 template <int PREC, int MT, int MODE>
 __global__ void __launch_bounds__(kLpThreads, 1)
-    lowp_tile_kernel(const __grid_constant__ CUtensorMap tmap_a,
-                     const __grid_constant__ CUtensorMap tmap_b,
-                     const __grid_constant__ CUtensorMap tmap_n, LpParams p) {
+    lowp_tile_kernel(const __grid_constant__ CUtensorMap tmap_a, LpParams p) {
   constexpr bool FOLD = PREC == HORA_PREC_BF16 && MT == M_L2;
   extern __shared__ __align__(1024) uint8_t smraw[];
   uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
@@ -321,24 +325,21 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     // ---------------- TMA producer ----------------
     if (tc::elect_one()) {
       tc::prefetch_tmap(&tmap_a);
-      tc::prefetch_tmap(&tmap_b);
-      if (FOLD) tc::prefetch_tmap(&tmap_n);
       const int kb_elems = PREC == HORA_PREC_BF16 ? 64 : 128;
       tc::mbar_arrive_expect_tx(a_full, nkb * a_kb_bytes);
       for (int kb = 0; kb < nkb; ++kb) tc::tma_load_2d(sA + kb * a_kb_bytes, &tmap_a, a_full, kb * kb_elems, (int)q0);
+      // base tiles: one bulk copy per K block (and one for the norm block)
+      // from the tile image, whose bytes are the stage's layout
+      const uint8_t *img = p.tiles + (row0 / kLpBN) * (int64_t)stage_bytes;
       for (int t = 0; t < T; ++t) {
         const int s = t % S, j = t / S;
         if (j > 0 && !tc::mbar_wait(empty + s, (j - 1) & 1, abort)) break;
         tc::mbar_arrive_expect_tx(full + s, stage_bytes);
-        const int y = (int)(row0 + (int64_t)t * kLpBN);
         uint8_t *st = sB + (size_t)s * stage_bytes;
+        const uint8_t *src = img + (int64_t)t * stage_bytes;
         for (int kb = 0; kb < nkb; ++kb)
-          tc::tma_load_2d(st + kb * b_kb_bytes, &tmap_b, full + s, kb * kb_elems, y);
-        if (FOLD) {
-          uint8_t *sn = st + nkb * b_kb_bytes;
-          tc::tma_load_2d(sn, &tmap_n, full + s, 0, y);
-          tc::tma_load_2d(sn + kNormHalfB, &tmap_n, full + s, 8, y);
-        }
+          tc::bulk_load(st + kb * b_kb_bytes, src + kb * b_kb_bytes, b_kb_bytes, full + s);
+        if (FOLD) tc::bulk_load(st + nkb * b_kb_bytes, src + nkb * b_kb_bytes, kNormBytesB, full + s);
       }
     }
   } else if (warp == 1) {
@@ -609,22 +610,6 @@ static int make_tmap(CUtensorMap *m, const void *ptr, int prec, int64_t Dp, int6
   return HORA_OK;
 }
 
-// The norm block: rows x 16 bf16 (32-byte rows), box 8 columns x 256 rows,
-// no swizzle (lands as the unswizzled K-major core-matrix layout).
-static int make_tmap_norm(CUtensorMap *m, const void *ptr, int64_t rows) {
-  EncodeTiledFn enc;
-  HORA_TRY(encode_fn(&enc));
-  cuuint64_t dims[2] = {16, (cuuint64_t)std::max<int64_t>(rows, 1)};
-  cuuint64_t strides[1] = {32};
-  cuuint32_t box[2] = {8, (cuuint32_t)kLpBN};
-  cuuint32_t es[2] = {1, 1};
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides,
-                   box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return fail(HORA_ECUDA, "cuTensorMapEncodeTiled (norm) failed: " + std::to_string((int)r));
-  return HORA_OK;
-}
-
 static int lp_smem_bytes(int nkb, int stages, bool fold) {
   return 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) +
          stages * (nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0)) + 32 * 8 + kLpHitBytes;
@@ -639,8 +624,7 @@ static int lp_stages(int nkb, bool fold) {
 }
 
 template <int PREC, int MT, int MODE>
-static int launch_lp3(const CUtensorMap &ta, const CUtensorMap &tb, const CUtensorMap &tn,
-                      const LpParams &p, cudaStream_t s) {
+static int launch_lp3(const CUtensorMap &ta, const LpParams &p, cudaStream_t s) {
   const int smem = lp_smem_bytes(p.nkb, p.stages, PREC == HORA_PREC_BF16 && MT == M_L2);
   static int attr = 0;
   if (attr < smem) {
@@ -652,28 +636,54 @@ static int launch_lp3(const CUtensorMap &ta, const CUtensorMap &tb, const CUtens
   dim3 grid((unsigned)ceil_div(p.nq, kLpBM), (unsigned)ceil_div(rows, (int64_t)kLpBN * kLpTilesPerCta));
   if (grid.x == 0 || grid.y == 0) return HORA_OK;
   ProfScope ps(PREC == HORA_PREC_BF16 ? "bf16_tc_scan" : "fp8_tc_scan", s);
-  lowp_tile_kernel<PREC, MT, MODE><<<grid, kLpThreads, smem, s>>>(ta, tb, tn, p);
+  lowp_tile_kernel<PREC, MT, MODE><<<grid, kLpThreads, smem, s>>>(ta, p);
   HORA_LAUNCHED();
   return HORA_OK;
 }
 
 template <int PREC>
-static int launch_lp2(int metric, int mode, const CUtensorMap &ta, const CUtensorMap &tb,
-                      const CUtensorMap &tn, const LpParams &p, cudaStream_t s) {
+static int launch_lp2(int metric, int mode, const CUtensorMap &ta, const LpParams &p, cudaStream_t s) {
   const bool dense = mode == TILE_DENSE;
   switch (metric) {
-    case M_L2: return dense ? launch_lp3<PREC, M_L2, TILE_DENSE>(ta, tb, tn, p, s) : launch_lp3<PREC, M_L2, TILE_FILTER>(ta, tb, tn, p, s);
-    case M_IP: return dense ? launch_lp3<PREC, M_IP, TILE_DENSE>(ta, tb, tn, p, s) : launch_lp3<PREC, M_IP, TILE_FILTER>(ta, tb, tn, p, s);
-    case M_COS: return dense ? launch_lp3<PREC, M_COS, TILE_DENSE>(ta, tb, tn, p, s) : launch_lp3<PREC, M_COS, TILE_FILTER>(ta, tb, tn, p, s);
+    case M_L2: return dense ? launch_lp3<PREC, M_L2, TILE_DENSE>(ta, p, s) : launch_lp3<PREC, M_L2, TILE_FILTER>(ta, p, s);
+    case M_IP: return dense ? launch_lp3<PREC, M_IP, TILE_DENSE>(ta, p, s) : launch_lp3<PREC, M_IP, TILE_FILTER>(ta, p, s);
+    case M_COS: return dense ? launch_lp3<PREC, M_COS, TILE_DENSE>(ta, p, s) : launch_lp3<PREC, M_COS, TILE_FILTER>(ta, p, s);
   }
   return fail(HORA_EMETRIC, "no tensor-core form for this metric");
 }
 
 static int launch_lp(int prec, int metric, int mode, const CUtensorMap &ta, const LowpState &L,
                      const LpParams &p, cudaStream_t s) {
-  const CUtensorMap &tn = L.normblk.ptr ? L.tmap_n : L.tmap_b;  // unused unless BF16 Euclidean
-  return prec == HORA_PREC_BF16 ? launch_lp2<HORA_PREC_BF16>(metric, mode, ta, L.tmap_b, tn, p, s)
-                                : launch_lp2<HORA_PREC_FP8>(metric, mode, ta, L.tmap_b, tn, p, s);
+  LpParams q = p;
+  q.tiles = L.tiles.as<uint8_t>();
+  return prec == HORA_PREC_BF16 ? launch_lp2<HORA_PREC_BF16>(metric, mode, ta, q, s)
+                                : launch_lp2<HORA_PREC_FP8>(metric, mode, ta, q, s);
+}
+
+// The tile image from a row-major copy (n x row_bytes) and, for BF16
+// Euclidean, the n x 32-byte norm block: one thread per 16-byte chunk.
+__global__ void tile_image_kernel(const uint8_t *rows, int64_t n, int64_t row_bytes, int nkb,
+                                  const uint8_t *norm, int64_t tile_bytes, int64_t ntiles, uint8_t *out) {
+  const int64_t per_tile = (int64_t)kLpBN * (nkb * 8 + (norm ? 2 : 0));
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntiles * per_tile) return;
+  const int64_t t = i / per_tile;
+  const int64_t w = i % per_tile;
+  uint8_t *tile = out + t * tile_bytes;
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (w < (int64_t)kLpBN * nkb * 8) {
+    const int kb = (int)(w / (kLpBN * 8));
+    const int r = (int)((w / 8) % kLpBN), c = (int)(w % 8);
+    const int64_t row = t * kLpBN + r;
+    if (row < n) v = *reinterpret_cast<const uint4 *>(rows + row * row_bytes + kb * 128 + c * 16);
+    *reinterpret_cast<uint4 *>(tile + kb * (kLpBN * 128) + r * 128 + ((c ^ (r & 7)) * 16)) = v;
+  } else {
+    const int64_t u = w - (int64_t)kLpBN * nkb * 8;
+    const int half = (int)(u / kLpBN), r = (int)(u % kLpBN);
+    const int64_t row = t * kLpBN + r;
+    if (row < n) v = *reinterpret_cast<const uint4 *>(norm + row * 32 + half * 16);
+    *reinterpret_cast<uint4 *>(tile + nkb * (kLpBN * 128) + half * (kLpBN * 16) + r * 16) = v;
+  }
 }
 
 // Low-precision copy of the base (and its exact squared norms / scales),
@@ -689,31 +699,41 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
   st->n = h->n;
   st->Dp = Dp;
   const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
-  HORA_TRY(st->base.reserve(std::max<int64_t>(h->n, 1) * Dp * esz));
+  const int nkb = (int)(Dp / kbe);
+  const bool fold = prec == HORA_PREC_BF16 && h->metric == M_L2;
+  st->tile_bytes = (int64_t)nkb * kLpBN * 128 + (fold ? (int64_t)kNormBytesB : 0);
+  const int64_t ntiles = std::max<int64_t>(ceil_div(h->n, kLpBN), 1);
+  DevBuf rows, normblk;  // row-major staging, freed once the image is built
+  HORA_TRY(rows.reserve(std::max<int64_t>(h->n, 1) * Dp * esz));
+  HORA_TRY(st->tiles.reserve(ntiles * st->tile_bytes));
   HORA_TRY(st->xsq.reserve(sizeof(float) * std::max<int64_t>(h->n, 1)));
   {
     ProfScope ps("lowp_convert", s);
     if (prec == HORA_PREC_BF16) {
       to_bf16_kernel<<<ceil_div(h->n * Dp, 256), 256, 0, s>>>(
           h->base.as<float>(), h->n, h->ld, h->dim, Dp,
-          h->metric == M_COS ? h->xsq64.as<double>() : nullptr, st->base.as<__nv_bfloat16>());
-      if (h->metric == M_L2) {
+          h->metric == M_COS ? h->xsq64.as<double>() : nullptr, rows.as<__nv_bfloat16>());
+      if (fold) {
         HORA_LAUNCHED();
-        HORA_TRY(st->normblk.reserve(std::max<int64_t>(h->n, 1) * 16 * 2));
+        HORA_TRY(normblk.reserve(std::max<int64_t>(h->n, 1) * 16 * 2));
         norm_block_kernel<<<ceil_div(h->n, 256), 256, 0, s>>>(h->xsq64.as<double>(), h->n,
-                                                              st->normblk.as<__nv_bfloat16>());
+                                                              normblk.as<__nv_bfloat16>());
       }
     } else {
       HORA_TRY(st->xscale.reserve(sizeof(float) * std::max<int64_t>(h->n, 1)));
       to_e4m3_kernel<<<ceil_div(h->n, 8), 256, 0, s>>>(h->base.as<float>(), h->n, h->ld, h->dim, Dp,
-                                                       st->base.as<uint8_t>(), st->xscale.as<float>());
+                                                       rows.as<uint8_t>(), st->xscale.as<float>());
     }
     HORA_LAUNCHED();
     f64_to_f32_kernel<<<ceil_div(h->n, 256), 256, 0, s>>>(h->xsq64.as<double>(), h->n, st->xsq.as<float>());
     HORA_LAUNCHED();
+    const int64_t chunks = ntiles * kLpBN * (nkb * 8 + (fold ? 2 : 0));
+    tile_image_kernel<<<ceil_div(chunks, 256), 256, 0, s>>>(rows.as<uint8_t>(), h->n, Dp * esz, nkb,
+                                                            fold ? normblk.as<uint8_t>() : nullptr,
+                                                            st->tile_bytes, ntiles, st->tiles.as<uint8_t>());
+    HORA_LAUNCHED();
   }
-  HORA_TRY(make_tmap(&st->tmap_b, st->base.ptr, prec, Dp, h->n, kLpBN));
-  if (st->normblk.ptr) HORA_TRY(make_tmap_norm(&st->tmap_n, st->normblk.ptr, h->n));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));  // the staging buffers are freed on return
   h->lowp = std::move(st);
   return HORA_OK;
 }
