@@ -45,6 +45,7 @@ constexpr int kLpEpiThreads = 512;   // warps 2..17
 constexpr int kLpTilesPerCta = 16;   // 4,096 rows per CTA
 constexpr int kLpSlices = kLpBN / 4 / 32;  // 32-column slices per drain warp and tile
 constexpr int kLpMaxStages = 8;
+constexpr int kLpBarSlots = 48;  // u64 slots for the barriers, TMEM address and abort flag
 // Filter-mode hits are staged per drain thread in shared memory and
 // appended to the query's global list kLpHitBuf at a time (one atomic per
 // flush instead of one per hit, off the per-tile critical path).
@@ -280,7 +281,13 @@ __global__ void __launch_bounds__(kLpThreads, 1)
   uint8_t *sAn = sm + nkb * a_kb_bytes;  // FOLD: the (1,1,1,0...) block
   uint8_t *sB = sAn + (FOLD ? 4096 : 0);
   uint64_t *bars = reinterpret_cast<uint64_t *>(sB + S * stage_bytes);
-  uint64_t *full = bars, *empty = bars + kLpMaxStages, *a_full = bars + 2 * kLpMaxStages;
+  // each ring stage in two halves with their own barriers: K block 0, then
+  // the other K blocks and the norm block (when there are any), so the MMA
+  // starts on a tile's first half while its second half is still arriving,
+  // and a half is refilled as soon as its own MMAs are done
+  uint64_t *full = bars, *empty = bars + kLpMaxStages;
+  uint64_t *full2 = bars + 2 * kLpMaxStages, *empty2 = bars + 3 * kLpMaxStages;
+  uint64_t *a_full = bars + 4 * kLpMaxStages;
   uint64_t *acc_full = a_full + 1, *acc_empty = acc_full + kLpNB, *done = acc_empty + kLpNB;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
   volatile int *abort = reinterpret_cast<volatile int *>(done + 2);
@@ -295,6 +302,8 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     for (int s = 0; s < S; ++s) {
       tc::mbar_init(full + s, 1);
       tc::mbar_init(empty + s, 1);
+      tc::mbar_init(full2 + s, 1);
+      tc::mbar_init(empty2 + s, 1);
     }
     tc::mbar_init(a_full, 1);
     for (int b = 0; b < kLpNB; ++b) {
@@ -328,18 +337,22 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       const int kb_elems = PREC == HORA_PREC_BF16 ? 64 : 128;
       tc::mbar_arrive_expect_tx(a_full, nkb * a_kb_bytes);
       for (int kb = 0; kb < nkb; ++kb) tc::tma_load_2d(sA + kb * a_kb_bytes, &tmap_a, a_full, kb * kb_elems, (int)q0);
-      // base tiles: one bulk copy per K block (and one for the norm block)
-      // from the tile image, whose bytes are the stage's layout
+      // base tiles: bulk copies from the tile image, whose bytes are the
+      // stage's layout; the first half (K block 0) and the rest separately
       const uint8_t *img = p.tiles + (row0 / kLpBN) * (int64_t)stage_bytes;
+      const uint32_t rest = stage_bytes - b_kb_bytes;
       for (int t = 0; t < T; ++t) {
         const int s = t % S, j = t / S;
-        if (j > 0 && !tc::mbar_wait(empty + s, (j - 1) & 1, abort)) break;
-        tc::mbar_arrive_expect_tx(full + s, stage_bytes);
         uint8_t *st = sB + (size_t)s * stage_bytes;
         const uint8_t *src = img + (int64_t)t * stage_bytes;
-        for (int kb = 0; kb < nkb; ++kb)
-          tc::bulk_load(st + kb * b_kb_bytes, src + kb * b_kb_bytes, b_kb_bytes, full + s);
-        if (FOLD) tc::bulk_load(st + nkb * b_kb_bytes, src + nkb * b_kb_bytes, kNormBytesB, full + s);
+        if (j > 0 && !tc::mbar_wait(empty + s, (j - 1) & 1, abort)) break;
+        tc::mbar_arrive_expect_tx(full + s, b_kb_bytes);
+        tc::bulk_load(st, src, b_kb_bytes, full + s);
+        if (rest) {
+          if (j > 0 && !tc::mbar_wait(empty2 + s, (j - 1) & 1, abort)) break;
+          tc::mbar_arrive_expect_tx(full2 + s, rest);
+          tc::bulk_load(st + b_kb_bytes, src + b_kb_bytes, rest, full2 + s);
+        }
       }
     }
   } else if (warp == 1) {
@@ -347,6 +360,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     if (tc::elect_one()) {
       constexpr uint32_t idesc = tc::idesc_f32acc(PREC == HORA_PREC_BF16 ? 1u : 0u, kLpBM, kLpBN);
       bool ok = tc::mbar_wait(a_full, 0, abort);
+      const bool rest = nkb > 1 || FOLD;  // a second half exists
       for (int t = 0; ok && t < T; ++t) {
         const int s = t % S, j = t / S, b = t % kLpNB, jb = t / kLpNB;
         if (!tc::mbar_wait(full + s, j & 1, abort)) break;
@@ -354,7 +368,17 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         tc::fence_after_sync();
         const uint32_t d = tmem + (uint32_t)(b * kLpBN);
         uint8_t *st = sB + (size_t)s * stage_bytes;
+        bool ok2 = true;
         for (int kb = 0; kb < nkb; ++kb) {
+          if (kb == 1) {
+            // K block 0 read: its half of the stage may be refilled
+            tc::mma_commit(empty + s);
+            if (!tc::mbar_wait(full2 + s, j & 1, abort)) {
+              ok2 = false;
+              break;
+            }
+            tc::fence_after_sync();
+          }
           const uint32_t a0 = tc::smem_u32(sA + kb * a_kb_bytes);
           const uint32_t b0 = tc::smem_u32(st + kb * b_kb_bytes);
 #pragma unroll
@@ -368,12 +392,18 @@ __global__ void __launch_bounds__(kLpThreads, 1)
               tc::mma_e4m3(d, ad, bd, idesc, acc);
           }
         }
+        if (!ok2) break;
         if (FOLD) {
+          if (nkb == 1) {
+            tc::mma_commit(empty + s);
+            if (!tc::mbar_wait(full2 + s, j & 1, abort)) break;
+            tc::fence_after_sync();
+          }
           const uint64_t ad = tc::sdesc_kmajor_none(tc::smem_u32(sAn), kNormHalfA, 128);
           const uint64_t bd = tc::sdesc_kmajor_none(tc::smem_u32(st + nkb * b_kb_bytes), kNormHalfB, 128);
           tc::mma_bf16(d, ad, bd, idesc, 1u);
         }
-        tc::mma_commit(empty + s);
+        tc::mma_commit(rest ? empty2 + s : empty + s);
         tc::mma_commit(acc_full + b);
       }
       // all MMAs of this thread complete before TMEM is released
@@ -413,7 +443,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       const float slack = 1e-6f * (fabsf(qa) + fabsf(tau_d)) + 1e-30f;
       thr = MT == M_L2 ? 0.5f * (qa - tau_d) - slack : (MT == M_IP ? tau_d + slack : -tau_d - slack);
     }
-    uint64_t *hbuf = reinterpret_cast<uint64_t *>(bars + 32);
+    uint64_t *hbuf = reinterpret_cast<uint64_t *>(bars + kLpBarSlots);
     DrainCtx c{p.cand, p.count, hbuf + (threadIdx.x - 64), qid, 0, p.r_begin, p.r_end, p.cap, qa, tau_d, tau_r};
     int nb = 0;  // keys staged in this thread's column
     for (int t = 0; t < T; ++t) {
@@ -612,13 +642,13 @@ static int make_tmap(CUtensorMap *m, const void *ptr, int prec, int64_t Dp, int6
 
 static int lp_smem_bytes(int nkb, int stages, bool fold) {
   return 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) +
-         stages * (nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0)) + 32 * 8 + kLpHitBytes;
+         stages * (nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0)) + kLpBarSlots * 8 + kLpHitBytes;
 }
 
 // Ring depth: as many base tiles as fit in ~220 KB of shared memory beside
 // the query tile and the hit staging.
 static int lp_stages(int nkb, bool fold) {
-  const int fixed = 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) + 32 * 8 + kLpHitBytes;
+  const int fixed = 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) + kLpBarSlots * 8 + kLpHitBytes;
   const int stage = nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0);
   return std::max(2, std::min(kLpMaxStages, (220 * 1024 - fixed) / stage));
 }
