@@ -42,7 +42,11 @@ constexpr int kLpBN = 256;           // base rows per tile (accumulator columns,
 constexpr int kLpNB = 2;             // TMEM accumulator buffers (2 x 256 columns)
 constexpr int kLpThreads = 576;      // 18 warps
 constexpr int kLpEpiThreads = 512;   // warps 2..17
-constexpr int kLpTilesPerCta = 16;   // 4,096 rows per CTA
+// Base tiles per CTA: 32 (8,192 rows) amortises the CTA prologue (measured
+// best of 16-64 at 10k queries); a launch with few query blocks takes 16 or
+// 8 so that it still spreads over every SM (see lp_tiles_per_cta).
+constexpr int kLpTilesPerCta = 32;
+constexpr int kLpMinTilesPerCta = 8;
 constexpr int kLpSlices = kLpBN / 4 / 32;  // 32-column slices per drain warp and tile
 constexpr int kLpMaxStages = 8;
 constexpr int kLpBarSlots = 48;  // u64 slots for the barriers, TMEM address and abort flag
@@ -85,6 +89,7 @@ struct LpParams {
   uint32_t *count;
   int *err;
   int dense_hits;  // hit-dense launch: the warp-converged staging (stage_hits)
+  int tpc;         // base tiles per CTA (lp_tiles_per_cta)
 };
 
 // BF16 Euclidean folds the row norm into the MMA: one extra K = 16 step
@@ -294,9 +299,9 @@ __global__ void __launch_bounds__(kLpThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t q0 = (int64_t)blockIdx.x * kLpBM;
-  const int64_t row0 = p.r_begin + (int64_t)blockIdx.y * kLpBN * kLpTilesPerCta;
+  const int64_t row0 = p.r_begin + (int64_t)blockIdx.y * kLpBN * p.tpc;
   const int64_t rows_here = p.r_end - row0;
-  const int T = (int)std::min<int64_t>(kLpTilesPerCta, (rows_here + kLpBN - 1) / kLpBN);
+  const int T = (int)std::min<int64_t>(p.tpc, (rows_here + kLpBN - 1) / kLpBN);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -653,6 +658,15 @@ static int lp_stages(int nkb, bool fold) {
   return std::max(2, std::min(kLpMaxStages, (220 * 1024 - fixed) / stage));
 }
 
+// The largest tiles-per-CTA of 32 / 16 / 8 whose grid still holds two
+// waves of CTAs (one CTA per SM), else 8.
+static int lp_tiles_per_cta(int64_t nq, int64_t rows) {
+  const int64_t qb = ceil_div(nq, kLpBM);
+  for (int tpc = kLpTilesPerCta; tpc > kLpMinTilesPerCta; tpc >>= 1)
+    if (qb * ceil_div(rows, (int64_t)kLpBN * tpc) >= 2 * 152) return tpc;
+  return kLpMinTilesPerCta;
+}
+
 template <int PREC, int MT, int MODE>
 static int launch_lp3(const CUtensorMap &ta, const LpParams &p, cudaStream_t s) {
   const int smem = lp_smem_bytes(p.nkb, p.stages, PREC == HORA_PREC_BF16 && MT == M_L2);
@@ -663,7 +677,7 @@ static int launch_lp3(const CUtensorMap &ta, const LpParams &p, cudaStream_t s) 
     attr = smem;
   }
   const int64_t rows = p.r_end - p.r_begin;
-  dim3 grid((unsigned)ceil_div(p.nq, kLpBM), (unsigned)ceil_div(rows, (int64_t)kLpBN * kLpTilesPerCta));
+  dim3 grid((unsigned)ceil_div(p.nq, kLpBM), (unsigned)ceil_div(rows, (int64_t)kLpBN * p.tpc));
   if (grid.x == 0 || grid.y == 0) return HORA_OK;
   ProfScope ps(PREC == HORA_PREC_BF16 ? "bf16_tc_scan" : "fp8_tc_scan", s);
   lowp_tile_kernel<PREC, MT, MODE><<<grid, kLpThreads, smem, s>>>(ta, p);
@@ -861,11 +875,12 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   int64_t c0 = std::min<int64_t>(n, std::min<int64_t>(cap, round_up(std::max(2 * R, 1024), kLpBN)));
   p.r_begin = 0;
   p.r_end = c0;
+  p.tpc = lp_tiles_per_cta(nq, c0);
   HORA_TRY(launch_lp(prec, h->metric, TILE_DENSE, ta, L, p, s));
   // bestR is an intermediate list: only its R-th key (the threshold) needs its place
   HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, (int)c0, nullptr, nq, flags, ovc, s, false));
   int64_t done = c0;
-  const int64_t max_chunk = (int64_t)60000 * kLpBN * kLpTilesPerCta;
+  const int64_t max_chunk = (int64_t)60000 * kLpBN * kLpMinTilesPerCta;
   while (done < n) {
     // each chunk at most 1.5x the rows scanned so far and at least 2,048
     // rows: a hit costs the drain more than the merge a smaller chunk adds
@@ -878,7 +893,8 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     p.r_end = done + c;
     // expected hits per drain thread and CTA, R x (rows per CTA / 4) / done:
     // from about 20 on, warp-converged flushes beat per-lane ones
-    p.dense_hits = (double)R * (kLpBN * kLpTilesPerCta / 4) / (double)done >= 20.0;
+    p.tpc = lp_tiles_per_cta(nq, c);
+    p.dense_hits = (double)R * (kLpBN * p.tpc / 4) / (double)done >= 20.0;
     HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, ta, L, p, s));
     HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s, false));
     done += c;
@@ -928,6 +944,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     for (int64_t lo = 0; lo < n; lo += max_chunk) {
       r.r_begin = lo;
       r.r_end = std::min<int64_t>(n, lo + max_chunk);
+      r.tpc = lp_tiles_per_cta(nl, r.r_end - r.r_begin);
       HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, tg, L, r, s));
       HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, ws.qlist.as<int>(), nl, flags, ovc, s));
     }
