@@ -524,6 +524,7 @@ int hora_idx_info(const hora_index *h, char *buf, uint64_t cap) {
                                              h->xsq64.bytes + ivf_device_bytes(h));
   s += ",\"last_search_ms\":" + std::to_string(h->last_ms.load());
   s += ",\"last_overflow_rescans\":" + std::to_string(h->last_retries.load());
+  s += ",\"last_threshold_probe\":" + std::to_string(h->last_probe.load());
   if (h->kind != HORA_INDEX_BRUTE_FORCE) {
     std::string iv;
     ivf_info(h, iv);
@@ -663,6 +664,7 @@ int hora_set_option(hora_index *h, int key, double v) {
       if (v < 0 || v > 4096) return fail(HORA_ECAP, "ivf rerank must be in [0, 4096]");
       h->ivf_rerank = (int)v;
       return HORA_OK;
+    case HORA_OPT_BF_PROBE: h->bf_probe = v != 0; return HORA_OK;
   }
   return fail(HORA_EINVAL, "unknown option");
 }
@@ -681,6 +683,7 @@ int hora_get_option(const hora_index *h, int key, double *out) {
     case HORA_OPT_NPROBE_MAX: *out = h->nprobe_max; return HORA_OK;
     case HORA_OPT_IVF_RERANK: *out = h->ivf_rerank; return HORA_OK;
     case HORA_OPT_NPROBE_PHASE1: *out = h->nprobe_phase1; return HORA_OK;
+    case HORA_OPT_BF_PROBE: *out = h->bf_probe; return HORA_OK;
   }
   return fail(HORA_EINVAL, "unknown option");
 }

@@ -29,6 +29,7 @@
 #include <cuda_fp8.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cstring>
 
 #include "dist_tile.cuh"
@@ -69,6 +70,14 @@ struct LowpState {
   int64_t tile_bytes = 0;
   DevBuf xsq;      // n f32 exact squared norms
   DevBuf xscale;   // n f32 (e4m3 per-row scale)
+  // BF16 Euclidean on at least kProbeMinRows rows: pivot clusters of the base
+  // (see ensure_pivots), built on first use
+  int pc = 0;      // pivots (0: not built)
+  DevBuf centers;  // pc x ld f32
+  DevBuf coff;     // pc + 1 int64 member offsets
+  DevBuf cmem;     // n uint32 member rows, cluster after cluster, ascending
+  DevBuf xsqmax;   // 1 f32: the largest squared row norm
+  DevBuf ctiles;   // the pivots' BF16 tile image (same layout as tiles)
 };
 
 void lowp_state_free(LowpState *p) { delete p; }
@@ -90,6 +99,7 @@ struct LpParams {
   int *err;
   int dense_hits;  // hit-dense launch: the warp-converged staging (stage_hits)
   int tpc;         // base tiles per CTA (lp_tiles_per_cta)
+  const float *tau0;  // per query starting distance threshold (filter mode), or null
 };
 
 // BF16 Euclidean folds the row norm into the MMA: one extra K = 16 step
@@ -436,6 +446,14 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         tau_d = key_dist(tk);
         tau_r = key_row(tk);
       }
+      if (p.tau0) {
+        // a probed threshold: every row at or below it is kept
+        const float t0 = p.tau0[qid];
+        if (t0 < tau_d) {
+          tau_d = t0;
+          tau_r = 0xffffffffu;
+        }
+      }
     }
     // BF16: the accumulator is the distance up to a per-query affine map
     // (Euclidean: qsq - 2 acc with the norm folded in; DotProduct: acc;
@@ -603,6 +621,266 @@ __global__ void gather_rows_u8_kernel(const uint8_t *src, int64_t row_bytes, con
   if (r >= n) return;
   const uint8_t *s = src + (int64_t)rows[r] * row_bytes;
   for (int64_t t = threadIdx.x; t < row_bytes; t += blockDim.x) dst[r * row_bytes + t] = s[t];
+}
+
+// ---- starting thresholds from pivot clusters (BF16 Euclidean) ---------------------------
+// With a threshold that starts at the R-th key of the rows scanned so far,
+// the chunked schedule keeps about R x ln(n / first chunk) rows per query
+// (~1,500 on 1M rows, R = 132), and the drain's hit handling is the largest
+// cost of the scan after the MMAs.  A base of at least kProbeMinRows rows
+// therefore keeps ~n / 1,024 pivot clusters (a few Lloyd steps from evenly
+// spaced rows).  Before the scan every query goes to its nearest pivot and
+// is scored against up to kProbeMaxMembers rows of that cluster with the
+// scan's own arithmetic (BF16 operands, exact products, f32 sums, the
+// folded norm).  Its starting threshold is the R-th of those distances plus
+// a bound on what the different summation order can change; one filter pass
+// over the base then keeps every row at or below it.  A query that kept at
+// least R rows has its R-best set complete: R rows at or below the
+// threshold put its R-th key there, and every key up to that one was kept.
+// A query that kept fewer (the bound did not hold, or its cluster had fewer
+// than R members) is answered again by the chunked schedule.
+constexpr int64_t kProbeRowsPerPivot = 1024;
+constexpr int64_t kProbeMinRows = 65536;
+constexpr int kProbeMaxMembers = 1024;  // members a query is scored against
+constexpr int kProbeMaxR = 256;         // widest R-best list the probe serves
+constexpr int kProbeMinCluster = 256;   // smaller clusters are dissolved at the end
+constexpr int kProbeReseed = 128;       // Lloyd steps re-seed clusters below this
+constexpr int kProbeLloyd = 6;
+constexpr int kProbeQ = 32;       // queries per pass of a probe CTA
+constexpr int kProbeRows = 128;   // member rows per shared-memory tile
+constexpr int kProbePitch = 132;  // f32 pitch of a staged row (spreads the banks)
+constexpr int kProbeSmem = (kProbeQ + kProbeRows) * kProbePitch * 4 + kProbeMaxMembers * 8;
+
+__device__ __forceinline__ void bf16x8_to_f32(const uint4 &v, float *out) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    out[2 * i] = __uint_as_float(w[i] << 16);
+    out[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+  }
+}
+
+// One CTA per pivot: the pivot's queries (32 at a time) against its first
+// kProbeMaxMembers member rows, read from the tile image.  Thread (qg, rg)
+// of the 8 x 32 layout scores queries qg + 8i against rows rg + 32j, the
+// products summed over ascending dimensions with one f32 FMA each, then the
+// folded norm added: dist = qsq - 2 (sum + (-|x|^2 / 2)).
+__global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, int64_t tile_bytes,
+                                                         const float *xsq, const int64_t *coff,
+                                                         const uint32_t *cmem, const __nv_bfloat16 *lq,
+                                                         int64_t Dp, const float *qsq, const int64_t *qoff,
+                                                         const uint32_t *qmem, const int *item_off, int C,
+                                                         float *pdist) {
+  extern __shared__ __align__(16) float psm[];
+  float *qs = psm;                           // kProbeQ x kProbePitch
+  float *xs = qs + kProbeQ * kProbePitch;    // kProbeRows x kProbePitch
+  float *xh = xs + kProbeRows * kProbePitch;                       // per member: -|x|^2 / 2
+  uint32_t *ids = reinterpret_cast<uint32_t *>(xh + kProbeMaxMembers);  // per member: its row
+  // work item blockIdx.x: batch (item - item_off[c]) of pivot c's queries
+  const int b = blockIdx.x;
+  if (b >= item_off[C]) return;
+  int lo = 0, hi = C;  // the last c with item_off[c] <= b
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (item_off[mid] <= b) lo = mid; else hi = mid;
+  }
+  const int c = lo;
+  const int64_t q_lo = qoff[c], nqc = qoff[c + 1] - q_lo;
+  const int64_t m_lo = coff[c];
+  const int L = (int)(coff[c + 1] - m_lo < kProbeMaxMembers ? coff[c + 1] - m_lo : kProbeMaxMembers);
+  const int t = threadIdx.x, qg = t & 7, rg = t >> 3;
+  const int D = (int)Dp, nch = D / 8;
+  {
+    const int64_t qb = (int64_t)(b - item_off[c]) * kProbeQ;
+    const int nb = (int)(nqc - qb < kProbeQ ? nqc - qb : kProbeQ);
+    const int ni = (nb + 7) >> 3;  // query slots in use per thread (CTA-uniform)
+    for (int j = t; j < L; j += 256) {
+      const uint32_t r = cmem[m_lo + j];
+      ids[j] = r;
+      xh[j] = -0.5f * xsq[r];
+    }
+    for (int i = t; i < kProbeQ * nch; i += 256) {
+      const int qi = i / nch, ch = i % nch;
+      float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (qi < nb) {
+        const uint32_t qid = qmem[q_lo + qb + qi];
+        bf16x8_to_f32(*reinterpret_cast<const uint4 *>(lq + (int64_t)qid * Dp + ch * 8), f);
+      }
+      float4 *dst = reinterpret_cast<float4 *>(qs + qi * kProbePitch + ch * 8);
+      dst[0] = make_float4(f[0], f[1], f[2], f[3]);
+      dst[1] = make_float4(f[4], f[5], f[6], f[7]);
+    }
+    for (int mt = 0; mt < L; mt += kProbeRows) {
+      __syncthreads();  // queries staged / the previous tile consumed
+      // the tile's 16-byte chunks: every load issued before the first store
+      uint4 buf[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = t + 256 * u, j = i / nch, ch = i % nch;
+        buf[u] = make_uint4(0u, 0u, 0u, 0u);
+        if (i < kProbeRows * nch && mt + j < L) {
+          const uint32_t r = ids[mt + j];
+          const int rr = (int)(r % kLpBN), kb = ch >> 3, cc = ch & 7;
+          buf[u] = *reinterpret_cast<const uint4 *>(tiles + (int64_t)(r / kLpBN) * tile_bytes + kb * (kLpBN * 128) +
+                                                    rr * 128 + ((cc ^ (rr & 7)) * 16));
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = t + 256 * u, j = i / nch, ch = i % nch;
+        if (i < kProbeRows * nch) {
+          float f[8];
+          bf16x8_to_f32(buf[u], f);
+          float4 *dst = reinterpret_cast<float4 *>(xs + j * kProbePitch + ch * 8);
+          dst[0] = make_float4(f[0], f[1], f[2], f[3]);
+          dst[1] = make_float4(f[4], f[5], f[6], f[7]);
+        }
+      }
+      __syncthreads();
+      float acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+#pragma unroll 2
+      for (int d = 0; d < D; d += 4) {
+        float4 xv[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) xv[j] = *reinterpret_cast<const float4 *>(xs + (rg + 32 * j) * kProbePitch + d);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          if (i < ni) {
+            const float4 qv = *reinterpret_cast<const float4 *>(qs + (qg + 8 * i) * kProbePitch + d);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              acc[i][j] = fmaf(qv.x, xv[j].x, acc[i][j]);
+              acc[i][j] = fmaf(qv.y, xv[j].y, acc[i][j]);
+              acc[i][j] = fmaf(qv.z, xv[j].z, acc[i][j]);
+              acc[i][j] = fmaf(qv.w, xv[j].w, acc[i][j]);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int qi = qg + 8 * i;
+        if (i >= ni || qi >= nb) continue;
+        const uint32_t qid = qmem[q_lo + qb + qi];
+        const float qa = qsq[qid];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int m = mt + rg + 32 * j;
+          if (m < L) pdist[(int64_t)qid * kProbeMaxMembers + m] = fmaf(-2.0f, acc[i][j] + xh[m], qa);
+        }
+      }
+    }
+  }
+}
+
+// One warp per query: the R-th smallest probe distance by a 32-step bitwise
+// descent over the ordered encoding, plus the summation-order bound
+// 1e-4 (|q|^2 + max |x|^2).  Both sums add the same exact BF16 products
+// (<= |q||x| + |x|^2 / 2 in magnitude, <= |q|^2 / 2 + max|x|^2) in f32; each
+// is within 144 x 2^-24 of that magnitude, so the distances (2 x the sum)
+// differ by less than 3.5e-5 of it.  A cluster with fewer than R members
+// gives -FLT_MAX: the scan keeps nothing and the query is rescheduled.
+__global__ void probe_select_kernel(const uint64_t *pkeys, const int64_t *coff, const float *pdist,
+                                    const float *qsq, const float *xsqmax, int64_t nq, int R, float *tau) {
+  const int64_t q = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  const uint32_t c = key_row(pkeys[q]);
+  const int L = (int)(coff[c + 1] - coff[c] < kProbeMaxMembers ? coff[c + 1] - coff[c] : kProbeMaxMembers);
+  if (L < R) {
+    if (lane == 0) tau[q] = -FLT_MAX;
+    return;
+  }
+  uint32_t v[kProbeMaxMembers / 32];
+#pragma unroll
+  for (int i = 0; i < kProbeMaxMembers / 32; ++i) {
+    const int m = lane + 32 * i;
+    v[i] = m < L ? f2ord(pdist[q * kProbeMaxMembers + m]) : 0xffffffffu;
+  }
+  // the largest a with fewer than R values below it is the R-th smallest
+  uint32_t a = 0;
+  for (int b = 31; b >= 0; --b) {
+    const uint32_t tt = a | (1u << b);
+    int cnt = 0;
+#pragma unroll
+    for (int i = 0; i < kProbeMaxMembers / 32; ++i) cnt += v[i] < tt;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (cnt < R) a = tt;
+  }
+  if (lane == 0) tau[q] = ord2f(a) + 1e-4f * (qsq[q] + *xsqmax);
+}
+
+// Probe work items: pivot c owns ceil(queries / kProbeQ) of them, from
+// item_off[c] (C + 1 offsets; one CTA of 1,024 threads, C <= 4,096).
+__global__ void probe_items_kernel(const int64_t *qoff, int C, int *item_off) {
+  __shared__ int part[1024];
+  const int t = threadIdx.x, per = (C + 1023) / 1024;
+  const int lo = min(C, t * per), hi = min(C, lo + per);
+  int s = 0;
+  for (int c = lo; c < hi; ++c) s += (int)((qoff[c + 1] - qoff[c] + kProbeQ - 1) / kProbeQ);
+  part[t] = s;
+  __syncthreads();
+  if (t == 0) {
+    int run = 0;
+    for (int i = 0; i < 1024; ++i) {
+      const int v = part[i];
+      part[i] = run;
+      run += v;
+    }
+    item_off[C] = run;
+  }
+  __syncthreads();
+  int run = part[t];
+  for (int c = lo; c < hi; ++c) {
+    item_off[c] = run;
+    run += (int)((qoff[c + 1] - qoff[c] + kProbeQ - 1) / kProbeQ);
+  }
+}
+
+// Re-seeds centre dst[i] with base row cmem[src[i]] (all ld columns).
+__global__ void reseed_kernel(const float *X, int64_t ld, const uint32_t *cmem, const int64_t *src,
+                              const int *dst, int m, float *centers) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m * ld) return;
+  const int j = (int)(i / ld);
+  centers[(int64_t)dst[j] * ld + (i % ld)] = X[(int64_t)cmem[src[j]] * ld + (i % ld)];
+}
+
+// Queries whose R-best list is still short after the probed pass, appended
+// to list (count in *n).
+__global__ void short_lists_kernel(const uint64_t *best, int R, int64_t nq, int *n, int *list) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq && best[q * R + (R - 1)] == kEmptyKey) list[atomicAdd(n, 1)] = (int)q;
+}
+
+// Empties the R-best lists of the listed queries.
+__global__ void clear_lists_kernel(uint64_t *best, int R, const int *list, int64_t nl) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nl * R) best[(int64_t)list[i / R] * R + (i % R)] = kEmptyKey;
+}
+
+// The largest of n non-negative floats (as ordered bits) into *out.
+__global__ void max_nonneg_kernel(const float *x, int64_t n, unsigned *out) {
+  float m = 0.0f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, x[i]);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// Pivots of clusters below kProbeMinCluster members are moved out of reach
+// so that the final assignment spreads their rows over the others.
+__global__ void dissolve_small_kernel(float *centers, int64_t ld, int64_t dim, const int64_t *counts, int C) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)C * dim) return;
+  const int c = (int)(i / dim);
+  if (counts[c] < kProbeMinCluster) centers[(int64_t)c * ld + (i % dim)] = 1e15f;
 }
 
 // ---- host ------------------------------------------------------------------------------
@@ -782,10 +1060,165 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
   return HORA_OK;
 }
 
+static bool probe_eligible(const hora_index *h) {
+  return h->bf_probe && h->precision == HORA_PREC_BF16 && h->metric == M_L2 && h->n >= kProbeMinRows;
+}
+
+// Pivot clusters of the base (exact FP32 nearest-pivot assignment): evenly
+// spaced rows, then kProbeLloyd Lloyd steps in which a cluster below
+// kProbeReseed members is re-seeded with a member of one of the largest
+// clusters (so that clusters which absorbed a whole group of rows without a
+// pivot of their own get split), then clusters below kProbeMinCluster
+// members dissolved into their neighbours by one more assignment.  Built
+// once per low-precision state, with the pivots' own BF16 tile image for the
+// queries' assignment.
+static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
+  if (L.pc > 0) return HORA_OK;
+  const int64_t n = h->n, ld = (int64_t)h->ld;
+  const int C = (int)std::min<int64_t>(4096, std::max<int64_t>(16, n / kProbeRowsPerPivot));
+  DevBuf keys, blk, cnt, plan;
+  HORA_TRY(L.centers.reserve(sizeof(float) * C * ld));
+  HORA_TRY(L.coff.reserve(sizeof(int64_t) * (C + 1)));
+  HORA_TRY(L.cmem.reserve(sizeof(uint32_t) * n));
+  HORA_TRY(L.xsqmax.reserve(sizeof(float)));
+  HORA_TRY(keys.reserve(sizeof(uint64_t) * n));
+  HORA_TRY(plan.reserve((sizeof(int64_t) + sizeof(int)) * C));
+  std::vector<int64_t> h_cnt(C), h_off(C + 1), h_src;
+  std::vector<int> h_dst;
+  ProfScope ps("probe_pivots", s);
+  const int64_t step = n / C;
+  HORA_CUDA_TRY(cudaMemcpy2DAsync(L.centers.ptr, sizeof(float) * ld, h->base.ptr, sizeof(float) * ld * step,
+                                  sizeof(float) * ld, C, cudaMemcpyDeviceToDevice, s));
+  for (int it = 0; it <= kProbeLloyd + 1; ++it) {
+    TileParams p;
+    p.Q = h->base.as<float>();
+    p.ldq = ld;
+    p.nq = n;
+    p.X = L.centers.as<float>();
+    p.ldx = ld;
+    p.r_begin = 0;
+    p.r_end = C;
+    p.ld = ld;
+    p.out_key = keys.as<uint64_t>();
+    HORA_TRY(launch_dist_tile(M_L2, TILE_ARGMIN, p, s));
+    HORA_TRY(sort_labels(keys.as<uint64_t>(), nullptr, n, C, blk, cnt, L.coff.as<int64_t>(),
+                         L.cmem.as<uint32_t>(), s));
+    if (it == kProbeLloyd + 1) break;
+    if (it == kProbeLloyd) {
+      dissolve_small_kernel<<<ceil_div((int64_t)C * h->dim, 256), 256, 0, s>>>(L.centers.as<float>(), ld, h->dim,
+                                                                              cnt.as<int64_t>(), C);
+      HORA_LAUNCHED();
+      continue;
+    }
+    HORA_TRY(launch_center_sum(h->base.as<float>(), ld, L.cmem.as<uint32_t>(), L.coff.as<int64_t>(), C, h->dim, 0,
+                               0.0f, L.centers.as<float>(), s));
+    // re-seed the small clusters from the largest ones (host plan)
+    HORA_CUDA_TRY(cudaMemcpyAsync(h_cnt.data(), cnt.ptr, sizeof(int64_t) * C, cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaMemcpyAsync(h_off.data(), L.coff.ptr, sizeof(int64_t) * (C + 1), cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<int> order(C);
+    for (int c = 0; c < C; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return h_cnt[x] > h_cnt[y]; });
+    h_src.clear();
+    h_dst.clear();
+    int big = 0;
+    for (int c = 0; c < C; ++c) {
+      if (h_cnt[c] >= kProbeReseed) continue;
+      const int from = order[big % C];
+      if (h_cnt[from] < 4 * kProbeReseed) break;  // nothing large enough to split
+      // a member a third of the way into the donor's list (row order)
+      h_src.push_back(h_off[from] + h_cnt[from] / 3 + (big / C));
+      h_dst.push_back(c);
+      ++big;
+    }
+    if (!h_dst.empty()) {
+      const int m = (int)h_dst.size();
+      int64_t *d_src = plan.as<int64_t>();
+      int *d_dst = reinterpret_cast<int *>(d_src + C);
+      HORA_CUDA_TRY(cudaMemcpyAsync(d_src, h_src.data(), sizeof(int64_t) * m, cudaMemcpyHostToDevice, s));
+      HORA_CUDA_TRY(cudaMemcpyAsync(d_dst, h_dst.data(), sizeof(int) * m, cudaMemcpyHostToDevice, s));
+      reseed_kernel<<<ceil_div((int64_t)m * ld, 256), 256, 0, s>>>(h->base.as<float>(), ld, L.cmem.as<uint32_t>(),
+                                                                  d_src, d_dst, m, L.centers.as<float>());
+      HORA_LAUNCHED();
+      HORA_CUDA_TRY(cudaStreamSynchronize(s));  // the host plan is reused next step
+    }
+  }
+  HORA_CUDA_TRY(cudaMemsetAsync(L.xsqmax.ptr, 0, sizeof(float), s));
+  max_nonneg_kernel<<<152, 256, 0, s>>>(L.xsq.as<float>(), n, L.xsqmax.as<unsigned>());
+  HORA_LAUNCHED();
+  // the pivots' tile image (BF16 rows and folded norms, like the base's)
+  const int64_t Dp = L.Dp;
+  const int nkb = (int)(Dp / 64);
+  const int64_t ctiles = ceil_div((int64_t)C, (int64_t)kLpBN);
+  DevBuf crow, cnorm, csq;
+  HORA_TRY(crow.reserve(sizeof(__nv_bfloat16) * C * Dp));
+  HORA_TRY(cnorm.reserve(sizeof(__nv_bfloat16) * C * 16));
+  HORA_TRY(csq.reserve(sizeof(double) * C));
+  HORA_TRY(L.ctiles.reserve(ctiles * L.tile_bytes));
+  HORA_TRY(launch_row_norms(L.centers.as<float>(), C, ld, h->dim, nullptr, csq.as<double>(), s));
+  to_bf16_kernel<<<ceil_div((int64_t)C * Dp, 256), 256, 0, s>>>(L.centers.as<float>(), C, ld, h->dim, Dp, nullptr,
+                                                                crow.as<__nv_bfloat16>());
+  HORA_LAUNCHED();
+  norm_block_kernel<<<ceil_div((int64_t)C, 256), 256, 0, s>>>(csq.as<double>(), C, cnorm.as<__nv_bfloat16>());
+  HORA_LAUNCHED();
+  tile_image_kernel<<<ceil_div(ctiles * kLpBN * (nkb * 8 + 2), 256), 256, 0, s>>>(
+      crow.as<uint8_t>(), C, Dp * 2, nkb, cnorm.as<uint8_t>(), L.tile_bytes, ctiles, L.ctiles.as<uint8_t>());
+  HORA_LAUNCHED();
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));  // the temporaries are freed on return
+  L.pc = C;
+  return HORA_OK;
+}
+
+// Starting thresholds of nq staged queries (ws.q f32, ws.lq BF16 under the
+// tensor map ta, ws.lqsq) into ws.ptau.  lp carries the search's scan
+// parameters; its candidate lists take the pivot scores (C <= cap).
+static int probe_thresholds(hora_index *h, LowpState &L, int64_t nq, int R, int64_t Dp, SearchWorkspace &ws,
+                            const CUtensorMap &ta, const LpParams &lp, cudaStream_t s) {
+  const int C = L.pc;
+  HORA_TRY(ws.pkeys.reserve(sizeof(uint64_t) * nq));
+  HORA_TRY(ws.poff.reserve(sizeof(int64_t) * (C + 1) + sizeof(int) * (C + 1)));
+  HORA_TRY(ws.pmem.reserve(sizeof(uint32_t) * nq));
+  HORA_TRY(ws.pdist.reserve(sizeof(float) * nq * kProbeMaxMembers));
+  HORA_TRY(ws.ptau.reserve(sizeof(float) * nq));
+  int64_t *qoff = ws.poff.as<int64_t>();
+  int *item_off = reinterpret_cast<int *>(qoff + C + 1);
+  // nearest pivot: the tensor-core scan over the pivots in dense mode, then the best key
+  LpParams a = lp;
+  a.tiles = L.ctiles.as<uint8_t>();
+  a.r_begin = 0;
+  a.r_end = C;
+  a.tpc = lp_tiles_per_cta(nq, C);
+  a.tau0 = nullptr;
+  a.dense_hits = 0;
+  HORA_TRY(launch_lp2<HORA_PREC_BF16>(M_L2, TILE_DENSE, ta, a, s));
+  HORA_CUDA_TRY(cudaMemsetAsync(ws.pkeys.ptr, 0xff, sizeof(uint64_t) * nq, s));
+  HORA_TRY(launch_merge_topk(ws.pkeys.as<uint64_t>(), 1, a.cand, a.count, a.cap, C, nullptr, nq, nullptr, nullptr, s));
+  HORA_TRY(sort_labels(ws.pkeys.as<uint64_t>(), nullptr, nq, C, ws.pblk, ws.pcnt, qoff, ws.pmem.as<uint32_t>(), s));
+  HORA_CUDA_TRY(cudaFuncSetAttribute(probe_dist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kProbeSmem));
+  {
+    ProfScope ps("probe_scores", s);
+    probe_items_kernel<<<1, 1024, 0, s>>>(qoff, C, item_off);
+    HORA_LAUNCHED();
+    probe_dist_kernel<<<(unsigned)(C + ceil_div(nq, (int64_t)kProbeQ)), 256, kProbeSmem, s>>>(
+      L.tiles.as<uint8_t>(), L.tile_bytes, L.xsq.as<float>(), L.coff.as<int64_t>(), L.cmem.as<uint32_t>(),
+      ws.lq.as<__nv_bfloat16>(), Dp, ws.lqsq.as<float>(), qoff, ws.pmem.as<uint32_t>(), item_off, C,
+      ws.pdist.as<float>());
+    HORA_LAUNCHED();
+  }
+  ProfScope ps("probe_select", s);
+  probe_select_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(
+      ws.pkeys.as<uint64_t>(), L.coff.as<int64_t>(), ws.pdist.as<float>(), ws.lqsq.as<float>(),
+      L.xsqmax.as<float>(), nq, R, ws.ptau.as<float>());
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
 int lowp_prepare(hora_index *h, cudaStream_t s) {
   const int64_t kbe = h->precision == HORA_PREC_BF16 ? 64 : 128;
   if (round_up((int64_t)h->dim, kbe) / kbe > 2) return HORA_OK;  // exact path answers
-  return ensure_lowp(h, h->precision, s);
+  HORA_TRY(ensure_lowp(h, h->precision, s));
+  if (probe_eligible(h)) HORA_TRY(ensure_pivots(h, *h->lowp, s));
+  return HORA_OK;
 }
 
 int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
@@ -872,36 +1305,75 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   p.count = count;
   p.err = ws.lerr.as<int>();
   const int64_t n = h->n;
-  int64_t c0 = std::min<int64_t>(n, std::min<int64_t>(cap, round_up(std::max(2 * R, 1024), kLpBN)));
-  p.r_begin = 0;
-  p.r_end = c0;
-  p.tpc = lp_tiles_per_cta(nq, c0);
-  HORA_TRY(launch_lp(prec, h->metric, TILE_DENSE, ta, L, p, s));
-  // bestR is an intermediate list: only its R-th key (the threshold) needs its place
-  HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, (int)c0, nullptr, nq, flags, ovc, s, false));
-  int64_t done = c0;
   const int64_t max_chunk = (int64_t)60000 * kLpBN * kLpMinTilesPerCta;
-  while (done < n) {
-    // each chunk at most 1.5x the rows scanned so far and at least 2,048
-    // rows: a hit costs the drain more than the merge a smaller chunk adds
-    // (measured on 1M x 128, R = 132)
-    double grow = std::min((double)cap / (4.0 * R), 1.5);
-    int64_t c = (int64_t)((double)done * std::max(grow, 1.0));
-    c = std::max<int64_t>(c, (int64_t)2048);
-    c = std::min<int64_t>(round_up(c, kLpBN), std::min<int64_t>(n - done, max_chunk));
-    p.r_begin = done;
-    p.r_end = done + c;
-    // expected hits per drain thread and CTA, R x (rows per CTA / 4) / done:
-    // from about 20 on, warp-converged flushes beat per-lane ones
-    p.tpc = lp_tiles_per_cta(nq, c);
-    p.dense_hits = (double)R * (kLpBN * p.tpc / 4) / (double)done >= 20.0;
-    HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, ta, L, p, s));
-    HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s, false));
-    done += c;
+  // The chunked schedule for nl queries (list slots through qlist, or all;
+  // tm = their query tiles): a dense first chunk, then filter chunks against
+  // each query's R-th key so far.
+  auto chunked = [&](const CUtensorMap &tm, int64_t nl, const int *qlist) -> int {
+    LpParams c = p;
+    c.nq = nl;
+    c.qmap = qlist;
+    c.tau0 = nullptr;
+    c.dense_hits = 0;
+    const int64_t c0 = std::min<int64_t>(n, std::min<int64_t>(cap, round_up(std::max(2 * R, 1024), kLpBN)));
+    c.r_begin = 0;
+    c.r_end = c0;
+    c.tpc = lp_tiles_per_cta(nl, c0);
+    HORA_TRY(launch_lp(prec, h->metric, TILE_DENSE, tm, L, c, s));
+    // bestR is an intermediate list: only its R-th key (the threshold) needs its place
+    HORA_TRY(launch_merge_topk(bestR, R, c.cand, count, cap, (int)c0, qlist, nl, flags, ovc, s, false));
+    int64_t done = c0;
+    while (done < n) {
+      // each chunk at most 1.5x the rows scanned so far and at least 2,048
+      // rows: a hit costs the drain more than the merge a smaller chunk adds
+      // (measured on 1M x 128, R = 132)
+      double grow = std::min((double)cap / (4.0 * R), 1.5);
+      int64_t w = (int64_t)((double)done * std::max(grow, 1.0));
+      w = std::max<int64_t>(w, (int64_t)2048);
+      w = std::min<int64_t>(round_up(w, kLpBN), std::min<int64_t>(n - done, max_chunk));
+      c.r_begin = done;
+      c.r_end = done + w;
+      // expected hits per drain thread and CTA, R x (rows per CTA / 4) / done:
+      // from about 20 on, warp-converged flushes beat per-lane ones
+      c.tpc = lp_tiles_per_cta(nl, w);
+      c.dense_hits = (double)R * (kLpBN * c.tpc / 4) / (double)done >= 20.0;
+      HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, tm, L, c, s));
+      HORA_TRY(launch_merge_topk(bestR, R, c.cand, count, cap, 0, qlist, nl, flags, ovc, s, false));
+      done += w;
+    }
+    return HORA_OK;
+  };
+  // gathered query tiles of the nl queries listed in ws.qlist
+  auto gather = [&](int64_t nl, CUtensorMap *tg) -> int {
+    HORA_TRY(ws.lqgather.reserve(nl * Dp * esz));
+    gather_rows_u8_kernel<<<(unsigned)nl, 128, 0, s>>>(ws.lq.as<uint8_t>(), Dp * esz, ws.qlist.as<int>(), nl,
+                                                       ws.lqgather.as<uint8_t>());
+    HORA_LAUNCHED();
+    return make_tmap(tg, ws.lqgather.ptr, prec, Dp, nl, kLpBM);
+  };
+  int *lerr = ws.lerr.as<int>();  // [0] a pipeline wait timed out, [1] short lists after the probed pass
+  const bool probe = probe_eligible(h) && R <= kProbeMaxR;
+  if (probe) {
+    // one filter pass from the probed thresholds
+    HORA_TRY(ensure_pivots(h, L, s));
+    HORA_TRY(probe_thresholds(h, L, nq, R, Dp, ws, ta, p, s));
+    p.tau0 = ws.ptau.as<float>();
+    p.dense_hits = 0;
+    for (int64_t lo = 0; lo < n; lo += max_chunk) {
+      p.r_begin = lo;
+      p.r_end = std::min<int64_t>(n, lo + max_chunk);
+      p.tpc = lp_tiles_per_cta(nq, p.r_end - p.r_begin);
+      HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, ta, L, p, s));
+      HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s, false));
+    }
+    short_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(bestR, R, nq, lerr + 1, ws.qlist.as<int>());
+    HORA_LAUNCHED();
+  } else {
+    HORA_TRY(chunked(ta, nq, nullptr));
   }
   // exact FP32 rerank of the R candidates, then the k best; launched before
-  // the host learns whether a candidate list overflowed (rare), so the
-  // stream runs on without a round trip, and redone after the rescans
+  // the host learns whether a candidate list overflowed or came out short
+  // (rare), so the stream runs on without a round trip, and redone after
   HORA_TRY(ws.tmp.reserve(sizeof(uint64_t) * nq * R));
   auto finish = [&]() -> int {
     HORA_TRY(launch_rerank_exact(h->metric, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim,
@@ -911,13 +1383,33 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     return launch_merge_topk(d_best, k, ws.tmp.as<uint64_t>(), nullptr, R, R, nullptr, nq, flags, ovc, s);
   };
   HORA_TRY(finish());
-  // overflow rescans over gathered query rows
   uint32_t h_ovc = 0;
-  int errflag = 0;
-  HORA_CUDA_TRY(cudaMemcpyAsync(&h_ovc, ovc, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  HORA_CUDA_TRY(cudaMemcpyAsync(&errflag, ws.lerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-  HORA_CUDA_TRY(cudaStreamSynchronize(s));
-  if (errflag) return fail(HORA_ETIMEDOUT, "tensor-core scan: a pipeline wait timed out");
+  int hs[2] = {0, 0};
+  auto status = [&]() -> int {
+    HORA_CUDA_TRY(cudaMemcpyAsync(&h_ovc, ovc, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaMemcpyAsync(hs, lerr, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hs[0]) return fail(HORA_ETIMEDOUT, "tensor-core scan: a pipeline wait timed out");
+    return HORA_OK;
+  };
+  HORA_TRY(status());
+  h->last_probe = probe ? 1 : 0;
+  bool redo = false;
+  if (hs[1] > 0) {
+    // lists the probed pass left short: the chunked schedule answers them
+    h->last_probe = 2;
+    const int64_t nl = hs[1];
+    clear_lists_kernel<<<(unsigned)ceil_div(nl * R, 256), 256, 0, s>>>(bestR, R, ws.qlist.as<int>(), nl);
+    HORA_LAUNCHED();
+    CUtensorMap tg;
+    HORA_TRY(gather(nl, &tg));
+    HORA_TRY(chunked(tg, nl, ws.qlist.as<int>()));
+    HORA_TRY(status());
+    redo = true;
+  }
+  // overflow rescans over gathered query rows, against the R-th key of the
+  // list so far (for a probed list that key is already at or below its
+  // starting threshold)
   int rounds = 0;
   while (h_ovc > 0) {
     if (++rounds > 64) return fail(HORA_ECUDA, "candidate overflow did not converge");
@@ -931,15 +1423,12 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     HORA_CUDA_TRY(cudaMemcpyAsync(ws.qlist.ptr, list.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, s));
     HORA_CUDA_TRY(cudaMemsetAsync(flags, 0, nq, s));
     HORA_CUDA_TRY(cudaMemsetAsync(ovc, 0, sizeof(uint32_t), s));
-    HORA_TRY(ws.lqgather.reserve(nl * Dp * esz));
-    gather_rows_u8_kernel<<<(unsigned)nl, 128, 0, s>>>(ws.lq.as<uint8_t>(), Dp * esz, ws.qlist.as<int>(), nl,
-                                                       ws.lqgather.as<uint8_t>());
-    HORA_LAUNCHED();
     CUtensorMap tg;
-    HORA_TRY(make_tmap(&tg, ws.lqgather.ptr, prec, Dp, nl, kLpBM));
+    HORA_TRY(gather(nl, &tg));
     LpParams r = p;
     r.nq = nl;
     r.qmap = ws.qlist.as<int>();
+    r.tau0 = nullptr;
     r.dense_hits = 0;
     for (int64_t lo = 0; lo < n; lo += max_chunk) {
       r.r_begin = lo;
@@ -948,11 +1437,11 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
       HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, tg, L, r, s));
       HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, ws.qlist.as<int>(), nl, flags, ovc, s));
     }
-    HORA_CUDA_TRY(cudaMemcpyAsync(&h_ovc, ovc, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+    HORA_TRY(status());
+    redo = true;
   }
   h->last_retries = rounds;
-  if (rounds > 0) HORA_TRY(finish());
+  if (redo) HORA_TRY(finish());
   return HORA_OK;
 }
 

@@ -47,6 +47,7 @@ struct hora_index {
   int nprobe_max = 0;
   int ivf_rerank = 0;
   int nprobe_phase1 = 4;
+  int bf_probe = 1;
 
   cudaStream_t stream = nullptr;
   std::mutex mu;
@@ -56,6 +57,8 @@ struct hora_index {
   std::unique_ptr<hora::NprobeModel, hora::NprobeDeleter> nprobe;
   // last search diagnostics (written by whichever search finished last)
   std::atomic<int> last_retries{0};
+  // BF16 starting-threshold probe: 0 not used, 1 answered, 2 fell back to the chunked schedule
+  std::atomic<int> last_probe{0};
   std::atomic<double> last_ms{0.0};
 };
 

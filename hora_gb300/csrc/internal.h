@@ -85,6 +85,9 @@ struct SearchWorkspace {
   DevBuf coarse, probes, pair_cnt, pair_off, pair_q, pair_c, pair_slot, ivf_cand, best_r, tmp_keys;
   // low-precision scoring
   DevBuf lq, lqsq, lqscale, lqgather, lerr;
+  // BF16 starting thresholds: query -> pivot keys, queries bucketed by pivot,
+  // probe distances (queries x members), thresholds
+  DevBuf pkeys, poff, pmem, pblk, pcnt, pdist, ptau;
   // learned nprobe
   DevBuf feats, pred, npq;
   std::vector<uint8_t> h_flags;

@@ -51,6 +51,7 @@ class Option(enum.IntEnum):
     NPROBE_MAX = 9
     IVF_RERANK = 10
     NPROBE_PHASE1 = 11
+    BF_PROBE = 12
 
 
 @dataclass

@@ -120,8 +120,12 @@ typedef enum {
   HORA_OPT_NPROBE_MAX = 9,     /* learned nprobe: upper clamp */
   HORA_OPT_IVF_RERANK = 10,    /* IVF-PQ: exact FP32 rerank of this many ADC
                                   candidates (0 = off, reference behaviour) */
-  HORA_OPT_NPROBE_PHASE1 = 11  /* learned nprobe: lists probed before the model
+  HORA_OPT_NPROBE_PHASE1 = 11, /* learned nprobe: lists probed before the model
                                   reads its features (default 4; fixed at training) */
+  HORA_OPT_BF_PROBE = 12       /* BF16 Euclidean brute force on >= 65,536 rows:
+                                  start each query's scan from a threshold probed
+                                  in its nearest pivot cluster (default 1; 0 =
+                                  chunked schedule only; same results either way) */
 } hora_option;
 
 typedef struct hora_index hora_index;
