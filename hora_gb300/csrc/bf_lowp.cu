@@ -660,8 +660,25 @@ __device__ __forceinline__ void bf16x8_to_f32(const uint4 &v, float *out) {
   }
 }
 
-// One CTA per pivot: the pivot's queries (32 at a time) against its first
-// kProbeMaxMembers member rows, read from the tile image.  Thread (qg, rg)
+// The 16-byte chunks of member rows mt.. (kProbeRows of them) that thread t
+// stages: chunk i = t + 256 u is row i / nch, chunk i % nch.
+__device__ __forceinline__ void probe_load_tile(uint4 (&buf)[8], const uint32_t *ids, int mt, int L, int nch, int t,
+                                                const uint8_t *tiles, int64_t tile_bytes) {
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int i = t + 256 * u, j = i / nch, ch = i % nch;
+    buf[u] = make_uint4(0u, 0u, 0u, 0u);
+    if (i < kProbeRows * nch && mt + j < L) {
+      const uint32_t r = ids[mt + j];
+      const int rr = (int)(r % kLpBN), kb = ch >> 3, cc = ch & 7;
+      buf[u] = *reinterpret_cast<const uint4 *>(tiles + (int64_t)(r / kLpBN) * tile_bytes + kb * (kLpBN * 128) +
+                                                rr * 128 + ((cc ^ (rr & 7)) * 16));
+    }
+  }
+}
+
+// One CTA per work item: up to kProbeQ of one pivot's queries against its
+// first kProbeMaxMembers member rows, read from the tile image.  Thread (qg, rg)
 // of the 8 x 32 layout scores queries qg + 8i against rows rg + 32j, the
 // products summed over ascending dimensions with one f32 FMA each, then the
 // folded norm added: dist = qsq - 2 (sum + (-|x|^2 / 2)).
@@ -710,21 +727,13 @@ __global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, i
       dst[0] = make_float4(f[0], f[1], f[2], f[3]);
       dst[1] = make_float4(f[4], f[5], f[6], f[7]);
     }
+    __syncthreads();  // member rows and queries staged
+    // a tile's 16-byte chunks in registers: the next tile's loads are in
+    // flight while the current one is scored
+    uint4 buf[8];
+    probe_load_tile(buf, ids, 0, L, nch, t, tiles, tile_bytes);
     for (int mt = 0; mt < L; mt += kProbeRows) {
-      __syncthreads();  // queries staged / the previous tile consumed
-      // the tile's 16-byte chunks: every load issued before the first store
-      uint4 buf[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int i = t + 256 * u, j = i / nch, ch = i % nch;
-        buf[u] = make_uint4(0u, 0u, 0u, 0u);
-        if (i < kProbeRows * nch && mt + j < L) {
-          const uint32_t r = ids[mt + j];
-          const int rr = (int)(r % kLpBN), kb = ch >> 3, cc = ch & 7;
-          buf[u] = *reinterpret_cast<const uint4 *>(tiles + (int64_t)(r / kLpBN) * tile_bytes + kb * (kLpBN * 128) +
-                                                    rr * 128 + ((cc ^ (rr & 7)) * 16));
-        }
-      }
+      if (mt > 0) __syncthreads();  // the previous tile consumed
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int i = t + 256 * u, j = i / nch, ch = i % nch;
@@ -737,6 +746,7 @@ __global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, i
         }
       }
       __syncthreads();
+      if (mt + kProbeRows < L) probe_load_tile(buf, ids, mt + kProbeRows, L, nch, t, tiles, tile_bytes);
       float acc[4][4];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
@@ -801,9 +811,12 @@ __global__ void probe_select_kernel(const uint64_t *pkeys, const int64_t *coff, 
     const int m = lane + 32 * i;
     v[i] = m < L ? f2ord(pdist[q * kProbeMaxMembers + m]) : 0xffffffffu;
   }
-  // the largest a with fewer than R values below it is the R-th smallest
+  // the largest a with fewer than R values below it is the R-th smallest;
+  // the descent stops kSelectSkip bits short and rounds up (an upper bound
+  // within 2^-(23 - kSelectSkip) of the value, which is all a threshold needs)
+  constexpr int kSelectSkip = 12;
   uint32_t a = 0;
-  for (int b = 31; b >= 0; --b) {
+  for (int b = 31; b >= kSelectSkip; --b) {
     const uint32_t tt = a | (1u << b);
     int cnt = 0;
 #pragma unroll
@@ -812,7 +825,7 @@ __global__ void probe_select_kernel(const uint64_t *pkeys, const int64_t *coff, 
     for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     if (cnt < R) a = tt;
   }
-  if (lane == 0) tau[q] = ord2f(a) + 1e-4f * (qsq[q] + *xsqmax);
+  if (lane == 0) tau[q] = ord2f(a | ((1u << kSelectSkip) - 1)) + 1e-4f * (qsq[q] + *xsqmax);
 }
 
 // Probe work items: pivot c owns ceil(queries / kProbeQ) of them, from
@@ -1175,11 +1188,15 @@ static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
 static int probe_thresholds(hora_index *h, LowpState &L, int64_t nq, int R, int64_t Dp, SearchWorkspace &ws,
                             const CUtensorMap &ta, const LpParams &lp, cudaStream_t s) {
   const int C = L.pc;
-  HORA_TRY(ws.pkeys.reserve(sizeof(uint64_t) * nq));
+  // sized for a power of two of at least 1,024 queries: a serving slot whose
+  // batches vary reallocates (and with that waits for the device) rarely
+  int64_t nres = 1024;
+  while (nres < nq) nres <<= 1;
+  HORA_TRY(ws.pkeys.reserve(sizeof(uint64_t) * nres));
   HORA_TRY(ws.poff.reserve(sizeof(int64_t) * (C + 1) + sizeof(int) * (C + 1)));
-  HORA_TRY(ws.pmem.reserve(sizeof(uint32_t) * nq));
-  HORA_TRY(ws.pdist.reserve(sizeof(float) * nq * kProbeMaxMembers));
-  HORA_TRY(ws.ptau.reserve(sizeof(float) * nq));
+  HORA_TRY(ws.pmem.reserve(sizeof(uint32_t) * nres));
+  HORA_TRY(ws.pdist.reserve(sizeof(float) * nres * kProbeMaxMembers));
+  HORA_TRY(ws.ptau.reserve(sizeof(float) * nres));
   int64_t *qoff = ws.poff.as<int64_t>();
   int *item_off = reinterpret_cast<int *>(qoff + C + 1);
   // nearest pivot: the tensor-core scan over the pivots in dense mode, then the best key
