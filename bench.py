@@ -149,9 +149,10 @@ class Clocks:
 
 
 # DRAM traffic of the BF16 scan in one step of the headline form (1M x 128,
-# 10k queries, R = 132: 9 launches), from one ncu capture of
-# dram__bytes_read.sum + dram__bytes_write.sum: 323.1 MB read + 38.6 MB written.
-SCAN_TRAFFIC_BYTES_PER_STEP = 361.7e6
+# 10k queries, R = 132: the pivot pass and the probed pass over the base),
+# from one ncu capture of dram__bytes_read.sum + dram__bytes_write.sum:
+# 295.1 MB read + 37.3 MB written.
+SCAN_TRAFFIC_BYTES_PER_STEP = 332.4e6
 
 
 def peaks() -> dict:

@@ -2,12 +2,12 @@
 
     python -m hora_gb300.workloads ivfpq [--queries N] [--epochs E] [--nprobe P]
                                          [--n ROWS] [--lists C]
-    python -m hora_gb300.workloads bf [--queries N] [--precision fp32|bf16|fp8]
+    python -m hora_gb300.workloads bf [--queries N] [--precision fp32|bf16|fp8] [--rerank R]
 
 ivfpq: IVFPQIndex over the 1M x 128 Gaussian mixture, 1,024 lists, 32 x
 8-bit PQ trained on the first 500k items, then one search of N queries with
 an exact rerank of 100 ADC candidates.  bf: BruteForceIndex over the same
-data, one search of N queries, k = 100.
+data, one search of N queries, k = 100 (R candidates reranked, 0 = auto).
 """
 from __future__ import annotations
 
@@ -39,7 +39,7 @@ def ivfpq(queries: int = 1024, epochs: int = 25, nprobe: int = 16, n: int = 1_00
     return {"build_s": build_s, "search_ms": json.loads(ix.idx_info())["last_search_ms"]}
 
 
-def bf(queries: int = 1024, precision: str = "bf16", n: int = 1_000_000):
+def bf(queries: int = 1024, precision: str = "bf16", n: int = 1_000_000, rerank: int = 0):
     import torch
 
     import hora_gb300 as H
@@ -50,6 +50,7 @@ def bf(queries: int = 1024, precision: str = "bf16", n: int = 1_000_000):
     ix.madd(torch.from_numpy(X).cuda(), None)
     ix.build(H.Metric.Euclidean)
     ix.set_option(H.Option.PRECISION, {"fp32": 0, "bf16": 1, "fp8": 2}[precision])
+    ix.set_option(H.Option.RERANK, rerank)
     ids, d = ix.search_batch(q, 100)
     return {"search_ms": json.loads(ix.idx_info())["last_search_ms"]}
 
@@ -63,11 +64,12 @@ def main():
     ap.add_argument("--precision", default="bf16")
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--lists", type=int, default=1024)
+    ap.add_argument("--rerank", type=int, default=0)
     a = ap.parse_args()
     if a.workload == "ivfpq":
         print(json.dumps(ivfpq(a.queries, a.epochs, a.nprobe, a.n, a.lists)))
     else:
-        print(json.dumps(bf(a.queries, a.precision)))
+        print(json.dumps(bf(a.queries, a.precision, a.n, a.rerank)))
 
 
 if __name__ == "__main__":
