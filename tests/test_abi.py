@@ -21,6 +21,18 @@ def test_library_exports_header_symbols(hora):
     assert not [n for n in names if n not in _lib.SIGNATURES]
 
 
+def test_option_keys_match_header(hora):
+    """The Python Option enum carries every hora_option key of the header
+    with the same value."""
+    import re
+    from hora_gb300 import _lib
+    txt = open(_lib.HEADER).read()
+    body = txt[txt.index("HORA_OPT_PRECISION"):txt.index("} hora_option;")]
+    keys = {m.group(1): int(m.group(2)) for m in re.finditer(r"HORA_OPT_([A-Z0-9_]+)\s*=\s*(\d+)", body)}
+    assert len(keys) >= 12
+    assert keys == {o.name: int(o.value) for o in hora.Option}
+
+
 def test_version_and_error_string(hora):
     L = hora.lib()
     assert b"sm_103a" in L.hora_version()
