@@ -1073,6 +1073,11 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
   return HORA_OK;
 }
 
+// Pivots of an n-row base: ~n / kProbeRowsPerPivot, 16 to 4,096.
+static int probe_pivot_count(int64_t n) {
+  return (int)std::min<int64_t>(4096, std::max<int64_t>(16, n / kProbeRowsPerPivot));
+}
+
 static bool probe_eligible(const hora_index *h) {
   return h->bf_probe && h->precision == HORA_PREC_BF16 && h->metric == M_L2 && h->n >= kProbeMinRows;
 }
@@ -1088,7 +1093,7 @@ static bool probe_eligible(const hora_index *h) {
 static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
   if (L.pc > 0) return HORA_OK;
   const int64_t n = h->n, ld = (int64_t)h->ld;
-  const int C = (int)std::min<int64_t>(4096, std::max<int64_t>(16, n / kProbeRowsPerPivot));
+  const int C = probe_pivot_count(n);
   DevBuf keys, blk, cnt, plan;
   HORA_TRY(L.centers.reserve(sizeof(float) * C * ld));
   HORA_TRY(L.coff.reserve(sizeof(int64_t) * (C + 1)));
@@ -1369,7 +1374,8 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     return make_tmap(tg, ws.lqgather.ptr, prec, Dp, nl, kLpBM);
   };
   int *lerr = ws.lerr.as<int>();  // [0] a pipeline wait timed out, [1] short lists after the probed pass
-  const bool probe = probe_eligible(h) && R <= kProbeMaxR;
+  // the pivot pass writes one key per pivot into each query's candidate list
+  const bool probe = probe_eligible(h) && R <= kProbeMaxR && probe_pivot_count(n) <= cap;
   if (probe) {
     // one filter pass from the probed thresholds
     HORA_TRY(ensure_pivots(h, L, s));

@@ -85,3 +85,21 @@ def test_probe_overflow_with_duplicates(hora, oracle, gpu):
     np.testing.assert_array_equal(d1, d0)
     assert ids1[3].tolist() == rows[:50].tolist()
     assert d1[3, 0] == oracle.metric(q[3], base[rows[0]], 3)
+
+
+def test_small_candidate_capacity_keeps_chunked(hora, gpu):
+    """The pivot pass writes one key per pivot into each query's candidate
+    list: with a capacity below the pivot count (410 pivots for 420,000 rows
+    against 384 slots) the probe stays off; with the default it is on, and
+    both answers agree."""
+    from hora_gb300 import synth
+    base = synth.mixture(420_000, 16, 256, stream=43)
+    q = synth.mixture(300, 16, 256, stream=44)
+    ix = build(hora, base, 132)
+    ids1, d1, info1 = run(hora, ix, q, 20, 1)
+    assert info1["last_threshold_probe"] == 1
+    ix.set_option(hora.Option.CAND_CAP, 256)
+    ids2, d2, info2 = run(hora, ix, q, 20, 1)
+    assert info2["last_threshold_probe"] == 0
+    np.testing.assert_array_equal(ids1, ids2)
+    np.testing.assert_array_equal(d1, d2)
