@@ -46,6 +46,12 @@ def args_parse():
                     help="scoring forms: fp32, bf16, fp8, optionally with an explicit rerank "
                          "width (bf16r132 = BF16 scoring + exact rerank of 132 candidates)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="queries in the CPU baseline sample")
+    ap.add_argument("--cpu-shipped-sample", type=int, default=48,
+                    help="queries in the one-at-a-time single-thread CPU sample")
+    ap.add_argument("--ivf-profile", action="store_true",
+                    help="only build the IVF-PQ index of the IVF section and run one search of "
+                         "--nq queries at --nprobe (a small case for ncu captures)")
+    ap.add_argument("--nprobe", type=int, default=2)
     ap.add_argument("--small", action="store_true", help="tiny workload for a quick check")
     ap.add_argument("--nq", type=int, default=0, help="override the number of queries (profiling)")
     ap.add_argument("--no-ivf", action="store_true", help="skip the IVF-PQ section")
@@ -199,6 +205,24 @@ def cpu_sample_qps(base, q, k, n_sample, threads):
     O.bf_search(base, qs, k, O.EUCLIDEAN, threads=threads)
     dt = time.perf_counter() - t0
     return n_sample / dt, dt
+
+
+def cpu_as_shipped(base, q, k, n_sample):
+    """The reference as its own benchmark drives it (examples/src/ann_bench.rs
+    195-218): one query at a time on one thread, each search timed on its own
+    and the latencies summed; queries/s = queries / summed latency."""
+    from oracle import oracle as O
+    O.build()
+    lat = []
+    for i in range(n_sample):
+        t0 = time.perf_counter()
+        O.bf_search(base, q[i:i + 1], k, O.EUCLIDEAN, threads=1)
+        lat.append(time.perf_counter() - t0)
+    tot = sum(lat)
+    return {"value": n_sample / tot, "unit": "queries/s", "cores": 1, "kind": "port",
+            "sample": f"{n_sample} queries one at a time on one thread against the full "
+                      f"{base.shape[0]}x{base.shape[1]} base, k={k}, latency sum {tot:.1f} s",
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3)}
 
 
 # ---- the reference's CPU-runnable case ---------------------------------------------
@@ -491,6 +515,27 @@ def run_ssg(H, ix, base, cpu_bf_qps):
     return out
 
 
+def run_ivf_profile(a, H, base, q):
+    """The IVF section's index (1M x 128, 1,024 lists, 32 x 8-bit PQ trained on
+    the first 500k items, exact rerank of 100) and one search of the given
+    queries at --nprobe."""
+    import torch
+    params = H.IVFPQParams(n_sub=32, sub_bits=8, n_kmeans_center=1024, search_n_center=a.nprobe,
+                           train_epoch=a.ivf_epochs)
+    ix = H.IVFPQIndex(DIM, params)
+    ix.set_option(H.Option.TRAIN_SIZE, min(500_000, base.shape[0]))
+    ix.madd(torch.from_numpy(base).cuda(), None)
+    t0 = time.perf_counter()
+    ix.build(H.Metric.Euclidean)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    ix.set_option(H.Option.IVF_RERANK, 100)
+    ix.search_batch(q, 10)
+    print(json.dumps({"workload": "IVF-PQ profile case", "queries": q.shape[0], "nprobe": a.nprobe,
+                      "build_s": build_s, "search_ms": json.loads(ix.idx_info())["last_search_ms"]}),
+          flush=True)
+
+
 # ---- our implementation ------------------------------------------------------------
 def run_ours(a, dist: Dist):
     import torch
@@ -501,6 +546,9 @@ def run_ours(a, dist: Dist):
     torch.cuda.set_device(dist.local)
     B.build()
     base, q = make_data(a.small, a.nq)
+    if a.ivf_profile:
+        run_ivf_profile(a, H, base, q)
+        return
     n, nq = base.shape[0], q.shape[0]
     ix = H.BruteForceIndex(DIM)
     ix.madd(torch.from_numpy(base).cuda(), None)
@@ -644,7 +692,8 @@ def run_ours(a, dist: Dist):
         qps_cpu, dt = cpu_sample_qps(base, q, K, ns, threads)
         cpu = {"value": qps_cpu, "unit": "queries/s", "cores": threads, "kind": "port",
                "sample": f"{ns} of the 10k queries against the full 1Mx128 base, k=100, "
-                         f"{threads} threads, {dt:.1f} s"}
+                         f"{threads} threads, {dt:.1f} s",
+               "as_shipped": cpu_as_shipped(base, q, K, 4 if a.small else a.cpu_shipped_sample)}
 
     if dist.rank == 0:
         line = {

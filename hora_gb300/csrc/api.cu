@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -35,15 +36,44 @@ int fail(int code, const std::string &msg) {
   return code;
 }
 
-bool is_device_ptr(const void *p) {
-  if (!p) return false;
+int pointer_kind(const void *p) {
+  if (!p) return PTR_HOST;
   cudaPointerAttributes a;
   cudaError_t e = cudaPointerGetAttributes(&a, p);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return PTR_HOST;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return PTR_DEVICE;
+  if (a.type != cudaMemoryTypeDevice) return PTR_HOST;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return PTR_FOREIGN;
+  }
+  return a.device == dev ? PTR_DEVICE : PTR_FOREIGN;
+}
+
+bool is_device_ptr(const void *p) { return pointer_kind(p) == PTR_DEVICE; }
+
+int check_not_foreign(const void *p, const char *what) {
+  if (p && pointer_kind(p) == PTR_FOREIGN)
+    return fail(HORA_EINVAL, std::string(what) + " is memory of another device");
+  return HORA_OK;
+}
+
+int ensure_smem_attr(const void *kernel, int bytes) {
+  if (bytes <= 48 * 1024) return HORA_OK;
+  int dev = 0;
+  HORA_CUDA_TRY(cudaGetDevice(&dev));
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, int> have;
+  std::lock_guard<std::mutex> g(mu);
+  int &cur = have[{kernel, dev}];
+  if (cur >= bytes) return HORA_OK;
+  HORA_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  cur = bytes;
+  return HORA_OK;
 }
 
 const char *metric_name(int m) {
@@ -333,6 +363,8 @@ int hora_add(hora_index *h, const float *vecs, const uint64_t *ids, uint64_t n) 
   if (!h) return fail(HORA_EINVAL, "null index");
   if (n == 0) return HORA_OK;
   if (!vecs) return fail(HORA_EINVAL, "null vectors");
+  HORA_TRY(check_not_foreign(vecs, "vectors"));
+  HORA_TRY(check_not_foreign(ids, "ids"));
   std::lock_guard<std::mutex> g(h->mu);
   return add_rows(h, vecs, ids, n);
 }
@@ -376,10 +408,9 @@ namespace hora {
 int search_core(hora_index *h, SearchWorkspace &ws, cudaStream_t s, const float *queries,
                 uint64_t nq, uint64_t k, uint64_t nprobe, uint64_t *ids_out, float *dist_out,
                 float *vecs_out) {
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0, s);
+  HORA_TRY(ws.ev_t0.ensure(true));
+  HORA_TRY(ws.ev_t1.ensure(true));
+  HORA_CUDA_TRY(cudaEventRecord(ws.ev_t0.ev, s));
   int64_t total = (int64_t)(nq * k);
   // the queries' finiteness is checked on the device and read only before
   // the results are written: no host scan of the queries and no host round
@@ -432,14 +463,16 @@ int search_core(hora_index *h, SearchWorkspace &ws, cudaStream_t s, const float 
                  ? fail(HORA_ECUDA, "D2H vecs") : HORA_OK;
     }
   }
-  cudaEventRecord(e1, s);
+  cudaError_t re = cudaEventRecord(ws.ev_t1.ev, s);
   cudaError_t se = cudaStreamSynchronize(s);
   if (rc == HORA_OK && se != cudaSuccess) rc = fail(HORA_ECUDA, cudaGetErrorString(se));
   float ms = 0;
-  if (cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) h->last_ms = ms;
-  cudaGetLastError();
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  if (re == cudaSuccess && cudaEventElapsedTime(&ms, ws.ev_t0.ev, ws.ev_t1.ev) == cudaSuccess)
+    h->last_ms = ms;
+  // an error left by a launch or a copy that no status above reported
+  cudaError_t le = cudaGetLastError();
+  if (rc == HORA_OK && re != cudaSuccess) rc = fail(HORA_ECUDA, cudaGetErrorString(re));
+  if (rc == HORA_OK && le != cudaSuccess) rc = fail(HORA_ECUDA, cudaGetErrorString(le));
   return rc;
 }
 }  // namespace hora
@@ -453,6 +486,10 @@ static int search_common(hora_index *h, const float *queries, uint64_t nq, uint6
   if (!queries || (!ids_out && !dist_out && !vecs_out)) return fail(HORA_EINVAL, "null buffer");
   if (k == 0) return fail(HORA_EINVAL, "k must be positive");
   if (k > 4096) return fail(HORA_ECAP, "k must be <= 4096");
+  HORA_TRY(check_not_foreign(queries, "queries"));
+  HORA_TRY(check_not_foreign(ids_out, "ids_out"));
+  HORA_TRY(check_not_foreign(dist_out, "dist_out"));
+  HORA_TRY(check_not_foreign(vecs_out, "vecs_out"));
   std::lock_guard<std::mutex> g(h->mu);
   if (!h->built || h->metric == M_UNKNOWN) return fail(HORA_ENOTBUILT, "unknown method");
   return search_core(h, h->ws, h->stream, queries, nq, k, nprobe, ids_out, dist_out, vecs_out);
@@ -657,7 +694,7 @@ int hora_set_option(hora_index *h, int key, double v) {
     case HORA_OPT_NPROBE_MARGIN: h->nprobe_margin = v; return HORA_OK;
     case HORA_OPT_NPROBE_MAX: h->nprobe_max = (int)(v < 0 ? 0 : v); return HORA_OK;
     case HORA_OPT_NPROBE_PHASE1:
-      if (v < 1 || v > 64) return fail(HORA_ECAP, "phase-1 probes must be in [1, 64]");
+      if (v < 0 || v > 64) return fail(HORA_ECAP, "phase-1 probes must be in [0, 64]");
       h->nprobe_phase1 = (int)v;
       return HORA_OK;
     case HORA_OPT_IVF_RERANK:

@@ -98,12 +98,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) dist_tile_kernel(TileParams p
 
 template <int MT, int MODE>
 static int launch_one(const TileParams &p, cudaStream_t s) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    HORA_CUDA_TRY(cudaFuncSetAttribute(dist_tile_kernel<MT, MODE>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem));
-    attr_set = true;
-  }
+  HORA_SMEM_ATTR((dist_tile_kernel<MT, MODE>), kTileSmem);
   dim3 grid(ceil_div(p.nq, kTileQ), 1);
   if (MODE != TILE_ARGMIN) grid.y = ceil_div(p.r_end - p.r_begin, kTileN);
   if (grid.x == 0 || grid.y == 0) return HORA_OK;
@@ -299,14 +294,10 @@ int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, 
   // the warps' tiles and the query row in dynamic shared memory
   const size_t qb = sizeof(float) * ((size_t)nw * 32 * (kRrSlab + 1) + (size_t)ld);
   if (qb > 200 * 1024) return fail(HORA_EINVAL, "rerank: dimension too large");
-  static size_t attr = 48 * 1024;
-  if (qb > attr) {
-    HORA_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel<M_L2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qb));
-    HORA_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel<M_L1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qb));
-    HORA_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel<M_IP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qb));
-    HORA_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel<M_COS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qb));
-    attr = qb;
-  }
+  HORA_SMEM_ATTR(rerank_exact_kernel<M_L2>, qb);
+  HORA_SMEM_ATTR(rerank_exact_kernel<M_L1>, qb);
+  HORA_SMEM_ATTR(rerank_exact_kernel<M_IP>, qb);
+  HORA_SMEM_ATTR(rerank_exact_kernel<M_COS>, qb);
   switch (metric) {
     case M_L2: rerank_exact_kernel<M_L2><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
     case M_L1: rerank_exact_kernel<M_L1><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;

@@ -961,12 +961,7 @@ static int lp_tiles_per_cta(int64_t nq, int64_t rows) {
 template <int PREC, int MT, int MODE>
 static int launch_lp3(const CUtensorMap &ta, const LpParams &p, cudaStream_t s) {
   const int smem = lp_smem_bytes(p.nkb, p.stages, PREC == HORA_PREC_BF16 && MT == M_L2);
-  static int attr = 0;
-  if (attr < smem) {
-    HORA_CUDA_TRY(cudaFuncSetAttribute(lowp_tile_kernel<PREC, MT, MODE>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr = smem;
-  }
+  HORA_SMEM_ATTR((lowp_tile_kernel<PREC, MT, MODE>), smem);
   const int64_t rows = p.r_end - p.r_begin;
   dim3 grid((unsigned)ceil_div(p.nq, kLpBM), (unsigned)ceil_div(rows, (int64_t)kLpBN * p.tpc));
   if (grid.x == 0 || grid.y == 0) return HORA_OK;
@@ -1216,7 +1211,7 @@ static int probe_thresholds(hora_index *h, LowpState &L, int64_t nq, int R, int6
   HORA_CUDA_TRY(cudaMemsetAsync(ws.pkeys.ptr, 0xff, sizeof(uint64_t) * nq, s));
   HORA_TRY(launch_merge_topk(ws.pkeys.as<uint64_t>(), 1, a.cand, a.count, a.cap, C, nullptr, nq, nullptr, nullptr, s));
   HORA_TRY(sort_labels(ws.pkeys.as<uint64_t>(), nullptr, nq, C, ws.pblk, ws.pcnt, qoff, ws.pmem.as<uint32_t>(), s));
-  HORA_CUDA_TRY(cudaFuncSetAttribute(probe_dist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kProbeSmem));
+  HORA_SMEM_ATTR(probe_dist_kernel, kProbeSmem);
   {
     ProfScope ps("probe_scores", s);
     probe_items_kernel<<<1, 1024, 0, s>>>(qoff, C, item_off);

@@ -162,9 +162,9 @@ struct EventBox {
   ~EventBox() {
     if (ev) cudaEventDestroy(ev);
   }
-  int ensure() {
+  int ensure(bool timing = false) {
     if (ev) return HORA_OK;
-    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+    if (cudaEventCreateWithFlags(&ev, timing ? cudaEventDefault : cudaEventDisableTiming) != cudaSuccess) {
       cudaGetLastError();
       ev = nullptr;
       return fail(HORA_ECUDA, "cudaEventCreate failed");
@@ -212,7 +212,24 @@ struct DevBuf {
   T *as() const { return reinterpret_cast<T *>(ptr); }
 };
 
-// True when p is device (or managed) memory visible to the current device.
+// Where a caller's buffer lives.  PTR_HOST: host memory (pageable or
+// page-locked), copied by the library.  PTR_DEVICE: memory the current
+// device's kernels may read and write in place (its own allocations or
+// managed memory).  PTR_FOREIGN: device memory of another device, which
+// the library's kernels must not touch (without peer access that faults).
+enum PtrKind : int { PTR_FOREIGN = -1, PTR_HOST = 0, PTR_DEVICE = 1 };
+int pointer_kind(const void *p);
+// pointer_kind(p) == PTR_DEVICE
 bool is_device_ptr(const void *p);
+// HORA_EINVAL when p is memory of another device (null passes).
+int check_not_foreign(const void *p, const char *what);
+
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device.  The attribute belongs to each device's context, so it is
+// tracked per (kernel, device): a process-wide flag would leave every device
+// after the first without it.
+int ensure_smem_attr(const void *kernel, int bytes);
+#define HORA_SMEM_ATTR(kernel, bytes) \
+  HORA_TRY(::hora::ensure_smem_attr(reinterpret_cast<const void *>(kernel), (int)(bytes)))
 
 }  // namespace hora

@@ -105,6 +105,9 @@ uint64_t *ivf_merge_buffer(SearchWorkspace &ws, int64_t nq, int R, uint64_t *d_b
 // learned nprobe (nprobe_mlp.cu)
 int ivf_search_learned(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
                        cudaStream_t s);
+// JSON of the trained nprobe model (phase-1 probes, calibrated margin and
+// its held-out recall / mean nprobe), "null" without a model
+std::string nprobe_model_info(const hora_index *h);
 int ivf_layout(const hora_index *h, uint64_t *n_list, uint64_t *n_sub, uint64_t *sub_bits,
                uint64_t *dmax);
 int ivf_export(const hora_index *h, float *centers, int64_t *offsets, int64_t *items,

@@ -96,6 +96,8 @@ struct SearchWorkspace {
   HostBuf h_status;
   EventBox ev_status;
   bool status_pending = false;
+  // the search's own start / end events (timed), created once per workspace
+  EventBox ev_t0, ev_t1;
 };
 
 struct BaseView {

@@ -939,10 +939,8 @@ int sort_labels(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
   HORA_TRY(blk.reserve(sizeof(uint32_t) * nb * C));
   HORA_TRY(counts.reserve(sizeof(int64_t) * C));
   int smem = C * 4;
-  if (smem > 48 * 1024) {
-    HORA_CUDA_TRY(cudaFuncSetAttribute(label_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    HORA_CUDA_TRY(cudaFuncSetAttribute(label_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  }
+  HORA_SMEM_ATTR(label_hist_kernel, smem);
+  HORA_SMEM_ATTR(label_scatter_kernel, smem);
   {
     ProfScope ps("ivf_sort", s);
     label_hist_kernel<<<(unsigned)nb, 256, smem, s>>>(keys, labels, n, C, blk.as<uint32_t>());
@@ -970,7 +968,7 @@ static int launch_pq_kmeans(IvfState &v, const float *Z, int64_t npos, const int
                             int epochs, uint64_t seed, int accum, uint8_t *asg, uint32_t *mem, int *status,
                             cudaStream_t s) {
   int smem = (int)(v.K * DM * 4 + 8 + v.K * 8 + 3 * v.K * 4 + 16);
-  HORA_CUDA_TRY(cudaFuncSetAttribute(pq_kmeans_kernel<DM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  HORA_SMEM_ATTR(pq_kmeans_kernel<DM>, smem);
   ProfScope ps("pq_kmeans", s);
   pq_kmeans_kernel<DM><<<(unsigned)(v.n_list * v.n_sub), 256, smem, s>>>(
       Z, npos, toff, (int)v.n_sub, (int)v.K, v.sub_len_d.as<int>(), epochs, seed, accum, v.pq_metric, asg, mem,
@@ -1264,7 +1262,7 @@ static int launch_adc_vb(IvfState &v, SearchWorkspace &ws, const float *Q, int64
                 2 * sizeof(uint32_t) * (kAdcChunk + kk) + sizeof(int) * kk + sizeof(int) * 48 +
                 2 * sizeof(int) * v.n_sub;
   if (smem > 200 * 1024) return fail(HORA_ECAP, "IVF-PQ: LUT too large for shared memory");
-  HORA_CUDA_TRY(cudaFuncSetAttribute(adc_scan_kernel<DM, VB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  HORA_SMEM_ATTR((adc_scan_kernel<DM, VB>), smem);
   unsigned grid = (unsigned)ceil_div(npairs, per);
   if (grid == 0) return HORA_OK;
   ProfScope ps("adc_scan", s);
@@ -1543,7 +1541,8 @@ int ivf_info(const hora_index *h, std::string &out) {
   out = "{\"n_list\":" + std::to_string(v.n_list) + ",\"n_sub\":" + std::to_string(v.n_sub) +
         ",\"sub_bits\":" + std::to_string(v.sub_bits) + ",\"max_list\":" + std::to_string(v.max_list) +
         ",\"empty_lists\":" + std::to_string(empty) + ",\"search_n_center\":" +
-        std::to_string(h->ivf.search_n_center) + ",\"rerank\":" + std::to_string(h->ivf_rerank) + "}";
+        std::to_string(h->ivf.search_n_center) + ",\"rerank\":" + std::to_string(h->ivf_rerank) +
+        ",\"nprobe_model\":" + nprobe_model_info(h) + "}";
   return HORA_OK;
 }
 

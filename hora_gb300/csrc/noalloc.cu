@@ -11,10 +11,16 @@
 //
 // Limits: at most kNaMaxQueries queries and k <= kNaMaxK per call; dim a
 // multiple of 4 with 16-byte aligned rows; Euclidean, Manhattan or
-// DotProduct (cosine would need per-row norms of the whole base).
+// DotProduct (cosine would need per-row norms of the whole base).  Every
+// buffer must be memory of the current device (or managed memory).  A NaN or
+// Inf element in the queries or the base is HORA_ENAN, as hora_search and
+// hora_add report it (the reference panics, src/core/node.rs:158-166); the
+// flag is read before any result is written.
 // All calls share the array and it keeps the previous call's contents, so
 // this code clears what must start at zero on every call, and two calls that
-// overlap on the GPU (different streams or threads) race on it.
+// overlap on the GPU (different streams or threads) race on it.  A call is
+// synchronous: it waits on its stream and returns once the results are in
+// the caller's buffers.
 //
 // The first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (the host-side name is only a stand-in for it) and
@@ -37,7 +43,7 @@ struct NaScratch {
   uint32_t count[kNaMaxQueries];
   int qlist[kNaMaxQueries];
   uint8_t flags[kNaMaxQueries];
-  uint32_t ovf_counter[4];
+  uint32_t ovf_counter[4];  // [0] overflowed queries, [1] non-finite input element
   uint32_t nlist[4];
 };
 
@@ -98,7 +104,7 @@ extern "C" int hora_bf_search_noalloc(const float *base, uint64_t n, uint64_t di
     return fail(HORA_EINVAL, "noalloc search: base and queries must be 16-byte aligned");
   if (!is_device_ptr(base) || !is_device_ptr(queries) || !is_device_ptr(ids_out) ||
       !is_device_ptr(dist_out))
-    return fail(HORA_EINVAL, "noalloc search: all buffers must be device memory");
+    return fail(HORA_EINVAL, "noalloc search: all buffers must be memory of the current device");
   NaScratch *sc = nullptr;
   HORA_TRY(noalloc_scratch(&sc));
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -108,6 +114,9 @@ extern "C" int hora_bf_search_noalloc(const float *base, uint64_t n, uint64_t di
   HORA_CUDA_TRY(cudaMemsetAsync(sc->count, 0, sizeof(uint32_t) * Q, s));
   HORA_CUDA_TRY(cudaMemsetAsync(sc->flags, 0, Q, s));
   HORA_CUDA_TRY(cudaMemsetAsync(sc->ovf_counter, 0, sizeof(sc->ovf_counter), s));
+  const int64_t N = (int64_t)n;
+  HORA_TRY(launch_check_finite(queries, Q, (int64_t)dim, (int64_t)dim, &sc->ovf_counter[1], s));
+  HORA_TRY(launch_check_finite(base, N, (int64_t)dim, (int64_t)dim, &sc->ovf_counter[1], s));
 
   TileParams p;
   p.Q = queries;
@@ -121,7 +130,6 @@ extern "C" int hora_bf_search_noalloc(const float *base, uint64_t n, uint64_t di
   p.cand = sc->cand;
   p.cap = kNaCap;
   p.count = sc->count;
-  const int64_t N = (int64_t)n;
   const int64_t c0 = N < kNaCap ? N : kNaCap;
   p.r_begin = 0;
   p.r_end = c0;
@@ -144,10 +152,13 @@ extern "C" int hora_bf_search_noalloc(const float *base, uint64_t n, uint64_t di
                                sc->ovf_counter, s));
     done += c;
   }
-  // rescan queries whose candidates overflowed, with their tightened bound
-  uint32_t ovc = 0;
-  HORA_CUDA_TRY(cudaMemcpyAsync(&ovc, sc->ovf_counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  // the input check, then a rescan of the queries whose candidates
+  // overflowed, with their tightened bound
+  uint32_t st[2] = {0, 0};
+  HORA_CUDA_TRY(cudaMemcpyAsync(st, sc->ovf_counter, sizeof(st), cudaMemcpyDeviceToHost, s));
   HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (st[1]) return fail(HORA_ENAN, "invalid float element");
+  uint32_t ovc = st[0];
   for (int round = 0; ovc > 0; ++round) {
     if (round >= 64) return fail(HORA_ECUDA, "noalloc search: overflow rescan did not converge");
     HORA_CUDA_TRY(cudaMemsetAsync(sc->nlist, 0, sizeof(sc->nlist), s));

@@ -2,19 +2,26 @@
 // counterpart; the reference always probes search_n_center lists,
 // src/index/pq_idx.rs:424).
 //
-// Search with the model: probe the 4 nearest lists, read 40 features (the 32
-// smallest coarse distances and 8 summaries of the running top-10 after the 4
-// probes, all relative to the nearest coarse distance), predict
-// log2(nprobe) with an MLP 40 -> 64 -> 64 -> 1 (ReLU, FP32 weights), probe the
-// remaining lists of each query, merge, rerank.  Fixed-nprobe search stays
-// the fallback (option off, or no model).
+// Search with the model: probe the p1 nearest lists (p1 = HORA_OPT_NPROBE_
+// PHASE1, 0..64; 4 as the configuration states it, 0 or 1 when the probes
+// themselves are the cost to save), read 40 features (the 32 smallest coarse
+// distances and 8 summaries of the running top-10 after the p1 probes, all
+// relative to the nearest coarse distance; with p1 = 0 the top-10 summaries
+// fall back to coarse distances), predict log2(nprobe) with an MLP
+// 40 -> 64 -> 64 -> 1 (ReLU, FP32 weights), probe the remaining lists of
+// each query, merge, rerank.  Fixed-nprobe search stays the fallback (option
+// off, or no model).
 //
 // Training (hora_ivfpq_train_nprobe): labels come from the method itself —
 // for each training query the smallest nprobe in 1, 2, 4, ... max whose
-// top-10 reaches the recall target against exact brute force — and the MLP
-// is fitted on the GPU with this file's forward / backward / Adam kernels
-// (asymmetric squared error: under-predicting nprobe costs recall and is
-// weighted more).  The same kernels serve the gradient check against the
+// top-10 reaches the recall target against exact brute force (with k = 10 a
+// per-query recall of 0.95 means all ten) — and the MLP is fitted on the GPU
+// with this file's forward / backward / Adam kernels (asymmetric squared
+// error: under-predicting nprobe costs recall and is weighted more).  The
+// last tenth of the training queries is held out: on it the model's margin
+// (added to the predicted log2 nprobe) is calibrated as the smallest that
+// keeps the held-out recall@10 at or above the target, judged by the same
+// exact brute force.  The same kernels serve the gradient check against the
 // oracle (hora_mlp_loss_grad).
 #include <algorithm>
 #include <cmath>
@@ -39,6 +46,12 @@ struct NprobeModel {
   int pmax = 128;
   int p1 = 4;  // lists probed before the features are read
   double final_loss = 0;
+  // calibration on the held-out training queries
+  double margin = 0;        // added to the predicted log2 nprobe
+  double target = 0;        // recall@10 the margin was calibrated for
+  double cal_recall = -1;   // held-out recall@10 at that margin
+  double cal_nprobe = 0;    // held-out mean nprobe at that margin
+  int64_t cal_queries = 0;
 };
 
 void nprobe_model_free(NprobeModel *p) { delete p; }
@@ -202,11 +215,7 @@ static int mlp_step(const float *P, int f, int h1, int h2, const float *X, const
   HORA_TRY(gpart.reserve(sizeof(float) * (size_t)G * np));
   HORA_TRY(lpart.reserve(sizeof(float) * G));
   const int smem = mlp_smem(f, h1, h2);
-  static int attr = 0;
-  if (smem > attr) {
-    HORA_CUDA_TRY(cudaFuncSetAttribute(mlp_fwd_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr = smem;
-  }
+  HORA_SMEM_ATTR(mlp_fwd_bwd_kernel, smem);
   {
     ProfScope ps("mlp_fwd_bwd", s);
     mlp_fwd_bwd_kernel<<<G, kMlpBatch, smem, s>>>(P, f, h1, h2, X, Y, idx, n, n, alpha,
@@ -280,11 +289,13 @@ __global__ void fill_u32_kernel(uint32_t *a, int64_t n, uint32_t v) {
   if (i < n) a[i] = v;
 }
 
-// per-query recall@10 of result keys vs exact keys -> label update
+// per-query recall@10 of result keys vs exact keys -> label update; the hit
+// count at every grid nprobe is kept for the margin calibration
 __global__ void label_kernel(const uint64_t *res, int kr, const uint64_t *exact, int ke, int64_t nq,
-                             float target, float log2p, float *label, uint8_t *done) {
+                             float target, float log2p, float *label, uint8_t *done, uint8_t *hits,
+                             int gi, int ng) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq || done[q]) return;
+  if (q >= nq) return;
   int hit = 0, tot = 0;
   for (int i = 0; i < ke; ++i) {
     uint64_t e = exact[q * ke + i];
@@ -296,6 +307,8 @@ __global__ void label_kernel(const uint64_t *res, int kr, const uint64_t *exact,
         break;
       }
   }
+  hits[q * ng + gi] = (uint8_t)(tot == 0 ? ke : hit);
+  if (done[q]) return;
   if (tot == 0 || (float)hit >= target * (float)tot - 1e-6f) {
     label[q] = log2p;
     done[q] = 1;
@@ -306,13 +319,15 @@ __global__ void label_kernel(const uint64_t *res, int kr, const uint64_t *exact,
 static int learned_nprobe_per_query(hora_index *h, int64_t nq, int R, uint64_t *M, SearchWorkspace &ws,
                                     int pw, DevBuf &np_q, cudaStream_t s) {
   NprobeModel &md = *h->nprobe;
-  // phase 1: the 4 nearest lists
+  // phase 1: the p1 nearest lists (none when p1 = 0)
   HORA_TRY(np_q.reserve(sizeof(uint32_t) * std::max<int64_t>(nq, 1)));
   const int p1 = std::min(md.p1, pw);
-  fill_u32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(np_q.as<uint32_t>(), nq, (uint32_t)p1);
-  HORA_LAUNCHED();
   HORA_CUDA_TRY(cudaMemsetAsync(M, 0xff, sizeof(uint64_t) * nq * R, s));
-  HORA_TRY(ivf_adc_merge(h, nq, pw, 0, np_q.as<uint32_t>(), R, M, ws, s));
+  if (p1 > 0) {
+    fill_u32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(np_q.as<uint32_t>(), nq, (uint32_t)p1);
+    HORA_LAUNCHED();
+    HORA_TRY(ivf_adc_merge(h, nq, pw, 0, np_q.as<uint32_t>(), R, M, ws, s));
+  }
   // features -> MLP -> nprobe
   HORA_TRY(ws.feats.reserve(sizeof(float) * nq * kF));
   HORA_TRY(ws.pred.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
@@ -324,8 +339,10 @@ static int learned_nprobe_per_query(hora_index *h, int64_t nq, int R, uint64_t *
   HORA_TRY(mlp_forward(md.params.as<float>(), md.f, md.h1, md.h2, ws.feats.as<float>(), nq,
                        md.mean.as<float>(), md.inv_std.as<float>(), ws.pred.as<float>(), s));
   const int hi = std::min(pw, h->nprobe_max > 0 ? h->nprobe_max : md.pmax);
-  predict_nprobe_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(ws.pred.as<float>(), nq, (float)h->nprobe_margin,
-                                                          1, hi, np_q.as<uint32_t>());
+  predict_nprobe_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(ws.pred.as<float>(), nq,
+                                                          (float)(md.margin + h->nprobe_margin),
+                                                          std::max(1, p1), std::max(hi, p1),
+                                                          np_q.as<uint32_t>());
   HORA_LAUNCHED();
   return HORA_OK;
 }
@@ -334,6 +351,18 @@ static int learned_width(hora_index *h) {
   const int C = (int)h->ivf.n_kmeans_center;
   int pm = h->nprobe_max > 0 ? h->nprobe_max : h->nprobe->pmax;
   return std::min(C, std::max(32, pm));
+}
+
+std::string nprobe_model_info(const hora_index *h) {
+  if (!h->nprobe) return "null";
+  const NprobeModel &m = *h->nprobe;
+  char buf[320];
+  std::snprintf(buf, sizeof(buf),
+                "{\"phase1\":%d,\"pmax\":%d,\"final_loss\":%.6g,\"target\":%.6g,\"margin\":%.6g,"
+                "\"heldout_queries\":%lld,\"heldout_recall\":%.6g,\"heldout_mean_nprobe\":%.6g}",
+                m.p1, m.pmax, m.final_loss, m.target, m.margin, (long long)m.cal_queries, m.cal_recall,
+                m.cal_nprobe);
+  return buf;
 }
 
 int ivf_search_learned(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
@@ -457,6 +486,8 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
   if (!h || !train_queries) return fail(HORA_EINVAL, "null argument");
   if (h->kind != HORA_INDEX_IVFPQ || !h->ivfs) return fail(HORA_ENOTBUILT, "IVF-PQ index not built");
   if (n_train < kMlpBatch) return fail(HORA_EINVAL, "need at least 128 training queries");
+  if (!(recall_target > 0.0 && recall_target <= 1.0)) return fail(HORA_EINVAL, "recall target must be in (0, 1]");
+  HORA_TRY(check_not_foreign(train_queries, "train_queries"));
   std::lock_guard<std::mutex> g(h->mu);
   cudaStream_t s = h->stream;
   SearchWorkspace &ws = h->ws;
@@ -464,16 +495,21 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
   const int pm = (int)std::min<uint64_t>(std::max<uint64_t>(max_nprobe, 1), (uint64_t)C);
   const int pw = std::min(C, std::max(32, pm));
   const int kk = 10;
-  const int p1 = h->nprobe_phase1;
+  const int p1 = std::min(h->nprobe_phase1, pw);
   const int R = ivf_rerank_width(h, kk);
   std::vector<int> grid;
   for (int p = 1; p < pm; p *= 2) grid.push_back(p);
   grid.push_back(pm);
+  const int ng = (int)grid.size();
   const int64_t N = (int64_t)n_train;
-  DevBuf feats, labels, done, exact, res, M, npq;
+  // the last tenth is held out for the margin calibration
+  const int64_t n_cal = N >= 2048 ? N / 10 : 0;
+  const int64_t N_fit = N - n_cal;
+  DevBuf feats, labels, done, hits, exact, res, M, npq;
   HORA_TRY(feats.reserve(4 * N * kF));
   HORA_TRY(labels.reserve(4 * N));
   HORA_TRY(done.reserve(N));
+  HORA_TRY(hits.reserve((size_t)N * ng));
   const int64_t chunk = 8192;
   HORA_TRY(exact.reserve(8 * chunk * kk));
   HORA_TRY(res.reserve(8 * chunk * kk));
@@ -498,41 +534,48 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
     int retries = 0;
     HORA_TRY(bf_topk_exact(bv, h->metric, ws.q.as<float>(), ws.qnorm.as<float>(), nq, kk, h->cand_cap,
                            ws, exact.as<uint64_t>(), s, &retries));
-    // labels: smallest grid nprobe whose top-10 reaches the target
-    for (int p : grid) {
+    // labels: smallest grid nprobe whose top-10 reaches the target; hits at every grid nprobe
+    for (int gi = 0; gi < ng; ++gi) {
+      const int p = grid[gi];
       HORA_TRY(ivf_search_keys(h, nq, kk, p, nullptr, ws, res.as<uint64_t>(), s));
       label_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(res.as<uint64_t>(), kk, exact.as<uint64_t>(), kk, nq,
                                                      (float)recall_target, std::log2((float)p),
-                                                     labels.as<float>() + lo, done.as<uint8_t>() + lo);
+                                                     labels.as<float>() + lo, done.as<uint8_t>() + lo,
+                                                     hits.as<uint8_t>() + lo * ng, gi, ng);
       HORA_LAUNCHED();
     }
-    // features after the first 4 probes
+    // features after the first p1 probes
     HORA_TRY(ivf_probe(h, nq, pw, ws, s));
-    fill_u32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(npq.as<uint32_t>(), nq, (uint32_t)std::min(p1, pw));
-    HORA_LAUNCHED();
     HORA_CUDA_TRY(cudaMemsetAsync(M.ptr, 0xff, 8 * nq * R, s));
-    HORA_TRY(ivf_adc_merge(h, nq, pw, 0, npq.as<uint32_t>(), R, M.as<uint64_t>(), ws, s));
+    if (p1 > 0) {
+      fill_u32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(npq.as<uint32_t>(), nq, (uint32_t)p1);
+      HORA_LAUNCHED();
+      HORA_TRY(ivf_adc_merge(h, nq, pw, 0, npq.as<uint32_t>(), R, M.as<uint64_t>(), ws, s));
+    }
     nprobe_features_kernel<<<ceil_div(nq, 128), 128, 0, s>>>(ivf_probe_keys(ws), pw, M.as<uint64_t>(), R, nq,
                                                              feats.as<float>() + lo * kF);
     HORA_LAUNCHED();
   }
   h->learned_nprobe = saved_learned;
-  // feature standardisation (statistics on the host, applied in the forward)
+  // feature standardisation over the fitted queries (statistics on the
+  // host, applied in the forward)
   std::vector<float> hf(N * kF), hl(N);
+  std::vector<uint8_t> hh((size_t)N * ng);
   HORA_CUDA_TRY(cudaMemcpyAsync(hf.data(), feats.ptr, 4 * N * kF, cudaMemcpyDeviceToHost, s));
   HORA_CUDA_TRY(cudaMemcpyAsync(hl.data(), labels.ptr, 4 * N, cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaMemcpyAsync(hh.data(), hits.ptr, (size_t)N * ng, cudaMemcpyDeviceToHost, s));
   HORA_CUDA_TRY(cudaStreamSynchronize(s));
   std::vector<float> mean(kF, 0.0f), inv(kF, 1.0f);
   for (int t = 0; t < kF; ++t) {
     double m = 0, v = 0;
-    for (int64_t i = 0; i < N; ++i) m += hf[i * kF + t];
-    m /= N;
-    for (int64_t i = 0; i < N; ++i) v += (hf[i * kF + t] - m) * (hf[i * kF + t] - m);
-    v /= N;
+    for (int64_t i = 0; i < N_fit; ++i) m += hf[i * kF + t];
+    m /= N_fit;
+    for (int64_t i = 0; i < N_fit; ++i) v += (hf[i * kF + t] - m) * (hf[i * kF + t] - m);
+    v /= N_fit;
     mean[t] = (float)m;
     inv[t] = (float)(1.0 / std::sqrt(v + 1e-6));
   }
-  // standardised copy for training
+  // standardised copy (all queries: the held-out ones are predicted from it)
   for (int64_t i = 0; i < N; ++i)
     for (int t = 0; t < kF; ++t) hf[i * kF + t] = (hf[i * kF + t] - mean[t]) * inv[t];
   HORA_CUDA_TRY(cudaMemcpyAsync(feats.ptr, hf.data(), 4 * N * kF, cudaMemcpyHostToDevice, s));
@@ -550,11 +593,11 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
   fill(kH1 * kF + kH1, kH1, kH2 * kH1);
   fill(kH1 * kF + kH1 + kH2 * kH1 + kH2, kH2, kH2);
   double lab_mean = 0, lab_max = 0;
-  for (float l : hl) {
-    lab_mean += l;
-    lab_max = std::max<double>(lab_max, l);
+  for (int64_t i = 0; i < N_fit; ++i) {
+    lab_mean += hl[i];
+    lab_max = std::max<double>(lab_max, hl[i]);
   }
-  lab_mean /= N;
+  lab_mean /= N_fit;
   P[np - 1] = (float)lab_mean;  // output bias starts at the mean label
   HORA_TRY(md->params.reserve(4 * np));
   HORA_TRY(md->mean.reserve(4 * kF));
@@ -565,40 +608,79 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
   DevBuf mom, var, gp, lp, perm;
   HORA_TRY(mom.reserve(4 * np));
   HORA_TRY(var.reserve(4 * np));
-  HORA_TRY(perm.reserve(4 * N));
+  HORA_TRY(perm.reserve(4 * N_fit));
   HORA_CUDA_TRY(cudaMemsetAsync(mom.ptr, 0, 4 * np, s));
   HORA_CUDA_TRY(cudaMemsetAsync(var.ptr, 0, 4 * np, s));
   const int64_t step_n = 4096;
   const float alpha = 3.0f;  // under-predicting nprobe loses recall
-  std::vector<int> order(N);
+  std::vector<int> order(N_fit);
   std::iota(order.begin(), order.end(), 0);
   int step = 0;
   for (uint64_t ep = 0; ep < epochs; ++ep) {
     std::shuffle(order.begin(), order.end(), rng);
-    HORA_CUDA_TRY(cudaMemcpyAsync(perm.ptr, order.data(), 4 * N, cudaMemcpyHostToDevice, s));
+    HORA_CUDA_TRY(cudaMemcpyAsync(perm.ptr, order.data(), 4 * N_fit, cudaMemcpyHostToDevice, s));
     HORA_CUDA_TRY(cudaStreamSynchronize(s));
     const float lr = 3e-3f * (ep + 1 < epochs ? 1.0f : 0.3f);
-    for (int64_t b = 0; b + step_n <= N || (b == 0 && N < step_n); b += step_n) {
-      const int64_t nb = std::min(step_n, N - b);
+    for (int64_t b = 0; b + step_n <= N_fit || (b == 0 && N_fit < step_n); b += step_n) {
+      const int64_t nb = std::min(step_n, N_fit - b);
       ++step;
       HORA_TRY(mlp_step(md->params.as<float>(), kF, kH1, kH2, feats.as<float>(), labels.as<float>(),
                         perm.as<int>() + b, nb, alpha, gp, lp, nullptr, mom.as<float>(), var.as<float>(),
                         step, lr, md->params.as<float>(), s));
     }
   }
-  // final loss over the whole training set
-  HORA_TRY(mlp_step(md->params.as<float>(), kF, kH1, kH2, feats.as<float>(), labels.as<float>(), nullptr, N,
-                    alpha, gp, lp, nullptr, nullptr, nullptr, 0, 0.0f, nullptr, s));
-  const int Gc = ceil_div(N, kMlpBatch);
+  // final loss over the fitted queries
+  HORA_TRY(mlp_step(md->params.as<float>(), kF, kH1, kH2, feats.as<float>(), labels.as<float>(), nullptr,
+                    N_fit, alpha, gp, lp, nullptr, nullptr, nullptr, 0, 0.0f, nullptr, s));
+  const int Gc = ceil_div(N_fit, kMlpBatch);
   std::vector<float> l(Gc);
   HORA_CUDA_TRY(cudaMemcpyAsync(l.data(), lp.ptr, 4 * Gc, cudaMemcpyDeviceToHost, s));
   HORA_CUDA_TRY(cudaStreamSynchronize(s));
   double loss = 0;
   for (float v : l) loss += v;
-  loss /= N;
+  loss /= N_fit;
   md->pmax = pm;
   md->p1 = p1;
   md->final_loss = loss;
+  md->target = recall_target;
+  // margin calibration on the held-out queries: per margin on a 1/32 grid,
+  // each query's nprobe as the search computes it, and its recall taken from
+  // the hits measured at the largest grid nprobe not above that (nprobe 3 is
+  // scored as 2); the smallest margin whose held-out recall@10 reaches the
+  // target wins
+  if (n_cal > 0) {
+    DevBuf pred;
+    HORA_TRY(pred.reserve(4 * n_cal));
+    HORA_TRY(mlp_forward(md->params.as<float>(), kF, kH1, kH2, feats.as<float>() + N_fit * kF, n_cal, nullptr,
+                         nullptr, pred.as<float>(), s));
+    std::vector<float> hp(n_cal);
+    HORA_CUDA_TRY(cudaMemcpyAsync(hp.data(), pred.ptr, 4 * n_cal, cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+    const int hi = std::min(pw, h->nprobe_max > 0 ? h->nprobe_max : pm);
+    const int lo = std::max(1, p1);
+    bool found = false;
+    for (int mi = -160; mi <= 160 && !found; ++mi) {
+      const float m = (float)mi / 32.0f;
+      double hit = 0, probes = 0;
+      for (int64_t i = 0; i < n_cal; ++i) {
+        float e = std::min(hp[i] + m, 20.0f);
+        int p = (int)std::ceil(std::exp2(e) - 1e-4f);
+        p = std::min(std::max(p, lo), std::max(hi, lo));
+        int gi = 0;
+        while (gi + 1 < ng && grid[gi + 1] <= p) ++gi;
+        hit += hh[(size_t)(N_fit + i) * ng + gi];
+        probes += p;
+      }
+      const double rec = hit / (10.0 * (double)n_cal);
+      if (rec >= recall_target || mi == 160) {
+        md->margin = m;
+        md->cal_recall = rec;
+        md->cal_nprobe = probes / (double)n_cal;
+        found = true;
+      }
+    }
+    md->cal_queries = n_cal;
+  }
   h->nprobe = std::move(md);
   if (stats_out) {
     stats_out[0] = loss;

@@ -673,14 +673,8 @@ int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *cou
                       int dense_n, const int *qlist, int64_t nlist, uint8_t *ovf_flag,
                       uint32_t *ovf_counter, cudaStream_t s, bool sorted) {
   if (nlist <= 0) return HORA_OK;
-  static bool attr = false;
-  if (!attr) {
-    HORA_CUDA_TRY(cudaFuncSetAttribute(merge_topk_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    HORA_CUDA_TRY(cudaFuncSetAttribute(merge_select_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
-  }
+  HORA_SMEM_ATTR(merge_topk_kernel, 200 * 1024);
+  HORA_SMEM_ATTR(merge_select_kernel, 200 * 1024);
   const int cmax = dense_n > 0 ? dense_n : cap;
   if (!qlist && k <= kWmMaxK) {
     ProfScope ps("topk_merge", s);
@@ -698,12 +692,8 @@ int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *cou
     int P = 1;
     while (P < k) P <<= 1;
     const int smem = P * 8;
-    static int mb_attr = 0;
-    if (mb_attr < smem && smem > 48 * 1024) {
-      HORA_CUDA_TRY(cudaFuncSetAttribute(merge_block_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      HORA_CUDA_TRY(cudaFuncSetAttribute(merge_block_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      mb_attr = smem;
-    }
+    HORA_SMEM_ATTR(merge_block_kernel<true>, smem);
+    HORA_SMEM_ATTR(merge_block_kernel<false>, smem);
     ProfScope ps("topk_merge", s);
     if (sorted)
       merge_block_kernel<true><<<(unsigned)nlist, kMbThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
@@ -902,12 +892,7 @@ int launch_rows_topk(const float *D, int64_t rows, int64_t cols, int64_t ldd, in
   int P = 1;
   while (P < cols || P < k) P <<= 1;
   if (P * 8 > 200 * 1024) return fail(HORA_ECAP, "rows_topk: too many columns");
-  static bool attr = false;
-  if (!attr) {
-    HORA_CUDA_TRY(cudaFuncSetAttribute(rows_topk_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
-  }
+  HORA_SMEM_ATTR(rows_topk_kernel, 200 * 1024);
   ProfScope ps("rows_topk", s);
   rows_topk_kernel<<<(unsigned)rows, kMergeThreads, P * 8, s>>>(D, cols, ldd, k, P, out);
   HORA_LAUNCHED();

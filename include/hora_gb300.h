@@ -18,8 +18,9 @@
  *    across this ABI).
  *  - Vector arguments are row-major n x dim float32.  A pointer may be host
  *    memory or device memory of the current CUDA device; the library detects
- *    which and copies only host buffers.  The caller owns all buffers, the
- *    library owns the handle and its device memory.
+ *    which and copies only host buffers (memory of another device is
+ *    HORA_EINVAL).  The caller owns all buffers, the library owns the handle
+ *    and its device memory.
  *  - Search results are nq x k, ascending distance ("smaller means closer",
  *    src/core/metrics.rs:55,78).  When fewer than k items exist the tail
  *    slots hold id HORA_NO_ID and distance +inf (the reference returns a
@@ -116,12 +117,14 @@ typedef enum {
   HORA_OPT_ACCUM_F64 = 5,      /* k-means centroid sums in FP64 (default 1) */
   HORA_OPT_CAND_CAP = 6,       /* brute-force per-query candidate capacity */
   HORA_OPT_LEARNED_NPROBE = 7, /* IVF-PQ: use the trained nprobe model (0/1) */
-  HORA_OPT_NPROBE_MARGIN = 8,  /* learned nprobe: additive margin in log2 units */
+  HORA_OPT_NPROBE_MARGIN = 8,  /* learned nprobe: margin in log2 units added to
+                                  the one training calibrated (default 0) */
   HORA_OPT_NPROBE_MAX = 9,     /* learned nprobe: upper clamp */
   HORA_OPT_IVF_RERANK = 10,    /* IVF-PQ: exact FP32 rerank of this many ADC
                                   candidates (0 = off, reference behaviour) */
   HORA_OPT_NPROBE_PHASE1 = 11, /* learned nprobe: lists probed before the model
-                                  reads its features (default 4; fixed at training) */
+                                  reads its features (0..64, default 4; fixed at
+                                  training) */
   HORA_OPT_BF_PROBE = 12       /* BF16 Euclidean brute force on >= 65,536 rows:
                                   start each query's scan from a threshold probed
                                   in its nearest pivot cluster (default 1; 0 =
@@ -222,9 +225,13 @@ int hora_search_nprobe(hora_index *h, const float *queries, uint64_t nq, uint64_
 /* ---- learned nprobe (GPU-only; no reference counterpart) ----------------- */
 /* Generates labels on n_train training queries (host or device memory): the
  * smallest nprobe in the grid 1,2,4..max_nprobe whose top-10 reaches the
- * recall target against exact brute force, trains the MLP on the GPU with
- * the library's forward/backward kernels and installs it.  stats_out (may
- * be NULL) receives [final loss, label mean, label max, epochs]. */
+ * recall target against exact brute force (per query: with k = 10 a target
+ * of 0.95 means all ten), trains the MLP on the GPU with the library's
+ * forward/backward kernels on the first nine tenths, calibrates the margin
+ * on the last tenth (the smallest that keeps its recall@10 at or above the
+ * target) and installs the model; hora_idx_info reports the calibration.
+ * stats_out (may be NULL) receives [final loss, label mean, label max,
+ * epochs]. */
 int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t n_train,
                             uint64_t max_nprobe, double recall_target, uint64_t epochs,
                             double *stats_out);
@@ -269,13 +276,17 @@ int hora_server_stats(hora_server *s, double *out7);
  * its own pool and budget, or a latency-critical path where cudaMalloc /
  * cudaFree would synchronise the device).  base (n x dim), queries (nq x dim),
  * ids_out and dist_out (nq x k, row numbers and distances as hora_search
- * returns them) are all device memory; dim must be a multiple of 4 and the
- * rows 16-byte aligned.  Scratch comes from one fixed 2.1 MiB device array
- * that every GPU loading the library holds until the process exits: at most
- * 256 queries and k <= 64 per call (HORA_ECAP beyond), metrics Euclidean,
- * Manhattan and DotProduct.  Calls share that array: calls that overlap on
- * the GPU race.  The first call on each device resolves the array's device
- * address; make it before any stream capture.  stream may be NULL. */
+ * returns them) are all memory of the current device (or managed memory;
+ * anything else is HORA_EINVAL); dim must be a multiple of 4 and the rows
+ * 16-byte aligned.  A NaN or Inf element in the queries or the base is
+ * HORA_ENAN (reported before any result is written).  Scratch comes from one
+ * fixed 2.1 MiB device array that every GPU loading the library holds until
+ * the process exits: at most 256 queries and k <= 64 per call (HORA_ECAP
+ * beyond), metrics Euclidean, Manhattan and DotProduct.  Calls share that
+ * array: calls that overlap on the GPU race.  The call is synchronous: it
+ * returns once the results are in ids_out / dist_out.  The first call on each
+ * device resolves the array's device address; make it before any stream
+ * capture.  stream may be NULL. */
 int hora_bf_search_noalloc(const float *base, uint64_t n, uint64_t dim, const float *queries,
                            uint64_t nq, uint64_t k, int metric, uint64_t *ids_out,
                            float *dist_out, void *stream);
