@@ -325,28 +325,37 @@ def run_ivf(a, H, base, q, exact):
         del ex
     except Exception as e:  # the CPU leg is a reported baseline only
         out["cpu_baseline"] = {"error": str(e)}
-    # learned nprobe (trained on queries from the same distribution, disjoint from the bench's)
+    # learned nprobe (config 4): labels on 200k training queries from the
+    # same mixture (a stream disjoint from the 10k evaluated here) = the
+    # smallest nprobe whose top-10 reaches recall 0.95 against exact brute
+    # force; the margin is calibrated on the last tenth of the training
+    # queries for an aggregate recall@10 of 0.95; evaluated on the 10k
+    # held-out bench queries against every fixed nprobe
     try:
         tq = synth.mixture(a.ivf_train_queries, DIM, N_CENTERS, stream=7)
         out["learned_train"] = []
-        for p1 in (4, 1):  # lists probed before the model reads its features
+        out["learned"] = []
+        for p1 in (0, 1, 4):  # lists probed before the model reads its features
             ix.set_option(H.Option.NPROBE_PHASE1, p1)
+            ix.set_option(H.Option.NPROBE_MARGIN, 0.0)
             t0 = time.perf_counter()
-            st = ix.train_nprobe(tq, max_nprobe=128, recall_target=1.0, epochs=20)
+            st = ix.train_nprobe(tq, max_nprobe=128, recall_target=0.95, epochs=20)
             train_s = time.perf_counter() - t0
+            model = json.loads(ix.idx_info())["ivfpq"]["nprobe_model"]
             ix.set_option(H.Option.LEARNED_NPROBE, 1)
-            for margin in ((-2.0, -1.5, -1.25, -1.0, -0.5, 0.0) if p1 == 1 else (0.0, 0.5)):
-                ix.set_option(H.Option.NPROBE_MARGIN, margin)
+            for extra in (0.0, 0.25):  # on top of the calibrated margin
+                ix.set_option(H.Option.NPROBE_MARGIN, extra)
                 r = timed(0)
-                r["mean_nprobe"] = float(np.maximum(ix.predict_nprobe(q), p1).mean())
-                r["margin"] = margin
+                r["mean_nprobe"] = float(np.maximum(ix.predict_nprobe(q), max(p1, 1)).mean())
+                r["margin"] = model["margin"] + extra
                 r["phase1_probes"] = p1
-                out.setdefault("learned", []).append(r)
+                out["learned"].append(r)
             ix.set_option(H.Option.LEARNED_NPROBE, 0)
+            ix.set_option(H.Option.NPROBE_MARGIN, 0.0)
             out["learned_train"].append({"phase1_probes": p1, "queries": a.ivf_train_queries,
                                          "seconds": train_s, "final_loss": st[0],
-                                         "label_mean_log2": st[1]})
-        ok = [v for v in sweep.values() if (v["recall@10"] or 0) >= 0.95]
+                                         "label_mean_log2": st[1], "model": model})
+        ok = [dict(v, nprobe=int(p)) for p, v in sweep.items() if (v["recall@10"] or 0) >= 0.95]
         out["fixed_best_at_0.95"] = max(ok, key=lambda v: v["qps"]) if ok else None
         okl = [v for v in out["learned"] if (v["recall@10"] or 0) >= 0.95]
         out["learned_best_at_0.95"] = max(okl, key=lambda v: v["qps"]) if okl else None

@@ -83,6 +83,7 @@ struct SearchWorkspace {
       keys2, tmp;
   // IVF-PQ
   DevBuf coarse, probes, pair_cnt, pair_off, pair_q, pair_c, pair_slot, ivf_cand, best_r, tmp_keys;
+  DevBuf adc_next, adc_gmap;  // the ADC kernel's group counter and group -> list map
   // low-precision scoring
   DevBuf lq, lqsq, lqscale, lqgather, lerr;
   // BF16 starting thresholds: query -> pivot keys, queries bucketed by pivot,

@@ -43,6 +43,9 @@ struct IvfState {
   std::vector<int64_t> h_offsets;
   std::vector<uint8_t> h_trained;
   int64_t max_list = 0;
+  // every subspace spans 4 dimensions starting at a multiple of 4 (the ADC
+  // LUT build then reads each residual slice as one aligned 16-byte load)
+  bool sub_aligned4 = false;
   // metric of the PQ stages: Euclidean inside an IVF-PQ index (pq_idx.rs:71),
   // the build metric for a flat PQIndex (pq_idx.rs:198-202)
   int pq_metric = M_L2;
@@ -595,338 +598,595 @@ __global__ void pair_scatter_kernel(const uint64_t *probes, int64_t nq, int pmax
   pslot[pos] = (uint32_t)j;
 }
 
-// CTA-wide selection of the k smallest of L 32-bit order keys held in smem.
-// The keys' range [kmin, kmax] comes first; the radix select then runs on
-// key - kmin with its first 11-bit digit at the top of that range (plain
-// shared atomics: the keys spread over the bins) and stops as soon as the
-// k-th key's bin is taken whole; otherwise it resolves the k-th key exactly
-// and ties at it go to the lowest positions.  sel receives the k positions
-// (unordered).  L and k are uniform, 0 < k < L.  hist: kSelBins u32, zero on
-// entry and on return; scratch: 48 ints.
-__device__ void cta_select_k(const uint32_t *keys, int L, int k, int *sel, uint32_t *hist,
-                             int *scratch) {
-  // scratch: [0] remaining k, [1] digit, [2] below, [3] taken, [5] count at the digit,
-  // [8..16) scan, [16..24) / [24..32) per-warp minima / maxima
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  uint32_t lo = 0xffffffffu, hi = 0;
-  for (int i = threadIdx.x; i < L; i += blockDim.x) {
-    const uint32_t v = keys[i];
-    lo = min(lo, v);
-    hi = max(hi, v);
+// Groups of pairs: per list c, ceil(cnt[c] / G) groups of up to G pairs
+// (the list's pairs in scatter order).  One CTA computes the exclusive scans
+// of the pair counts (pair_off, C + 1 entries) and of the group counts
+// (grp_off, C + 1 entries; grp_off[C] = the number of groups).
+__global__ void group_scan_kernel(const int64_t *cnt, int C, int G, int64_t *pair_off, int64_t *grp_off) {
+  __shared__ int64_t part_p[1024], part_g[1024];
+  const int t = threadIdx.x;
+  const int per = (C + blockDim.x - 1) / blockDim.x;
+  const int lo = t * per, hi = min(C, lo + per);
+  int64_t sp = 0, sg = 0;
+  for (int c = lo; c < hi; ++c) {
+    sp += cnt[c];
+    sg += (cnt[c] + G - 1) / G;
   }
-  lo = __reduce_min_sync(0xffffffffu, lo);
-  hi = __reduce_max_sync(0xffffffffu, hi);
-  if (lane == 0) {
-    scratch[16 + warp] = (int)lo;
-    scratch[24 + warp] = (int)hi;
-  }
-  if (threadIdx.x == 0) {
-    scratch[0] = k;
-    scratch[3] = 0;
+  part_p[t] = sp;
+  part_g[t] = sg;
+  __syncthreads();
+  if (t == 0) {
+    int64_t rp = 0, rg = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      const int64_t vp = part_p[i], vg = part_g[i];
+      part_p[i] = rp;
+      part_g[i] = rg;
+      rp += vp;
+      rg += vg;
+    }
+    pair_off[C] = rp;
+    grp_off[C] = rg;
   }
   __syncthreads();
-  uint32_t kmin = 0xffffffffu, kmax = 0;
-  for (int x = 0; x < nwarp; ++x) {
-    kmin = min(kmin, (uint32_t)scratch[16 + x]);
-    kmax = max(kmax, (uint32_t)scratch[24 + x]);
-  }
-  int shift = 32 - __clz((int)(kmax - kmin)) - 11;  // __clz(0) = 32
-  shift = shift < 0 ? 0 : shift;
-  uint32_t prefix = 0, mask = 0;
-  bool whole = false;
-  for (;;) {
-    for (int i = threadIdx.x; i < L; i += blockDim.x) {
-      const uint32_t d = keys[i] - kmin;
-      if ((d & mask) == prefix) atomicAdd(&hist[(d >> shift) & (kSelBins - 1)], 1u);
-    }
-    __syncthreads();
-    if (warp == 0) {
-      warp_find_bin(hist, kSelBins, (uint32_t)scratch[0], scratch + 1);
-      __syncwarp();
-      const int d = scratch[1];
-      const uint32_t at_d = hist[d];
-      const int below = scratch[2];
-      __syncwarp();
-      for (int b = lane; b < kSelBins; b += 32) hist[b] = 0;
-      if (lane == 0) {
-        scratch[0] -= below;
-        scratch[5] = (int)at_d;
-      }
-    }
-    __syncthreads();
-    prefix |= (uint32_t)scratch[1] << shift;
-    mask |= (uint32_t)(kSelBins - 1) << shift;
-    if (scratch[5] == scratch[0]) {  // every key in this bin is taken
-      whole = true;
-      break;
-    }
-    if (shift == 0) break;
-    shift = shift >= 11 ? shift - 11 : 0;
-  }
-  if (whole) {
-    // exactly k keys lie at or below the bin's largest d
-    const uint32_t bound = prefix | ((1u << shift) - 1u);
-    for (int i0 = 0; i0 < L; i0 += blockDim.x) {
-      const int i = i0 + threadIdx.x;
-      const bool p = i < L && keys[i] - kmin <= bound;
-      const unsigned pm = __ballot_sync(0xffffffffu, p);
-      if (pm) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(&scratch[3], __popc(pm));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (p) sel[base + __popc(pm & ((1u << lane) - 1u))] = i;
-      }
-    }
-    __syncthreads();
-    return;
-  }
-  prefix += kmin;  // the k-th key itself
-  const uint32_t kth = prefix;
-  const int need_eq = scratch[0];  // keys equal to kth that are taken (>= 1)
-  const bool all_eq = scratch[5] == need_eq;
-  // keys below kth (and, when every key equal to kth is taken, those too)
-  for (int i0 = 0; i0 < L; i0 += blockDim.x) {
-    const int i = i0 + threadIdx.x;
-    const uint32_t v = i < L ? keys[i] : 0xffffffffu;
-    const bool p = i < L && (v < kth || (all_eq && v == kth));
-    const unsigned pm = __ballot_sync(0xffffffffu, p);
-    if (pm) {
-      int base = 0;
-      if (lane == 0) base = atomicAdd(&scratch[3], __popc(pm));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (p) sel[base + __popc(pm & ((1u << lane) - 1u))] = i;
-    }
-  }
-  if (all_eq) {
-    __syncthreads();
-    return;
-  }
-  __syncthreads();
-  const int base_lt = scratch[3];
-  // keys equal to kth in position order: chunked block scan
-  int run = 0;
-  const int nw = blockDim.x >> 5;
-  for (int i0 = 0; i0 < L && run < need_eq; i0 += blockDim.x) {
-    const int i = i0 + threadIdx.x;
-    const bool f = i < L && keys[i] == kth;
-    const unsigned b = __ballot_sync(0xffffffffu, f);
-    if (lane == 0) scratch[8 + warp] = __popc(b);
-    __syncthreads();
-    int before = run;
-    for (int x = 0; x < warp; ++x) before += scratch[8 + x];
-    int total = 0;
-    for (int x = 0; x < nw; ++x) total += scratch[8 + x];
-    if (f) {
-      const int r = before + __popc(b & ((1u << lane) - 1u));
-      if (r < need_eq) sel[base_lt + r] = i;
-    }
-    run += total;
-    __syncthreads();
+  int64_t rp = part_p[t], rg = part_g[t];
+  for (int c = lo; c < hi; ++c) {
+    pair_off[c] = rp;
+    grp_off[c] = rg;
+    rp += cnt[c];
+    rg += (cnt[c] + G - 1) / G;
   }
 }
 
-constexpr int kAdcThreads = 256;
-constexpr int kAdcChunk = 2048;
+constexpr int kAdcThreads = 512;
+constexpr int kAdcChunk = 2048;  // code rows scored per selection round
 
-// The sum over subspaces of LUT[m][code[m]] in subspace order (pq_idx.rs
-// 180-186), with the code row read VB bytes at a time (VB divides M and the
-// row pitch, so every load is aligned); KC = K when it is a compile-time 256.
-template <int VB, int KC>
-__device__ __forceinline__ float adc_row(const uint8_t *code, const float *lut, int M, int Kr) {
-  const int K = KC ? KC : Kr;  // a constant K folds the table offsets into the loads
-  float d = 0.0f;
+// G sums over subspaces of LUT[m][code[m]] (one per query of the group),
+// each in subspace order (pq_idx.rs:180-186).  The LUT holds the G queries'
+// entries of one (m, j) side by side (one 4G-byte load per code byte); the
+// code row is read VB bytes at a time (VB divides M and the row pitch, so
+// every load is aligned); KC = K when it is a compile-time 256.
+template <int G, int VB, int KC>
+__device__ __forceinline__ void adc_row_g(const uint8_t *code, const float *lut, int M, int Kr,
+                                          float (&d)[G]) {
+  const int K = KC ? KC : Kr;
+#pragma unroll
+  for (int g = 0; g < G; ++g) d[g] = 0.0f;
+  auto add = [&](int m, uint32_t j) {
+    const int e = m * K + (int)j;
+    if (G == 4) {
+      const float4 v = reinterpret_cast<const float4 *>(lut)[e];
+      d[0] = __fadd_rn(d[0], v.x);
+      d[1 % G] = __fadd_rn(d[1 % G], v.y);
+      d[2 % G] = __fadd_rn(d[2 % G], v.z);
+      d[3 % G] = __fadd_rn(d[3 % G], v.w);
+    } else if (G == 2) {
+      const float2 v = reinterpret_cast<const float2 *>(lut)[e];
+      d[0] = __fadd_rn(d[0], v.x);
+      d[1 % G] = __fadd_rn(d[1 % G], v.y);
+    } else {
+      d[0] = __fadd_rn(d[0], lut[e]);
+    }
+  };
   if (VB == 16) {
     const uint4 *p = reinterpret_cast<const uint4 *>(code);
-    for (int g = 0; g < M / 16; ++g) {
-      const uint4 w = __ldg(p + g);
+    for (int gq = 0; gq < M / 16; ++gq) {
+      const uint4 w = __ldg(p + gq);
 #pragma unroll
       for (int t = 0; t < 16; ++t) {
         const uint32_t wt = t < 4 ? w.x : t < 8 ? w.y : t < 12 ? w.z : w.w;
-        d = __fadd_rn(d, lut[(g * 16 + t) * K + ((wt >> (8 * (t & 3))) & 255u)]);
+        add(gq * 16 + t, (wt >> (8 * (t & 3))) & 255u);
       }
     }
   } else if (VB == 8) {
     const uint2 *p = reinterpret_cast<const uint2 *>(code);
-    for (int g = 0; g < M / 8; ++g) {
-      const uint2 w = __ldg(p + g);
+    for (int gq = 0; gq < M / 8; ++gq) {
+      const uint2 w = __ldg(p + gq);
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        const uint32_t wt = t < 4 ? w.x : w.y;
-        d = __fadd_rn(d, lut[(g * 8 + t) * K + ((wt >> (8 * (t & 3))) & 255u)]);
-      }
+      for (int t = 0; t < 8; ++t) add(gq * 8 + t, ((t < 4 ? w.x : w.y) >> (8 * (t & 3))) & 255u);
     }
   } else if (VB == 4) {
     const uint32_t *p = reinterpret_cast<const uint32_t *>(code);
-    for (int g = 0; g < M / 4; ++g) {
-      const uint32_t w = __ldg(p + g);
+    for (int gq = 0; gq < M / 4; ++gq) {
+      const uint32_t w = __ldg(p + gq);
 #pragma unroll
-      for (int t = 0; t < 4; ++t) d = __fadd_rn(d, lut[(g * 4 + t) * K + ((w >> (8 * t)) & 255u)]);
+      for (int t = 0; t < 4; ++t) add(gq * 4 + t, (w >> (8 * t)) & 255u);
     }
   } else {
-    for (int m = 0; m < M; ++m) d = __fadd_rn(d, lut[m * K + __ldg(code + m)]);
+    for (int m = 0; m < M; ++m) add(m, __ldg(code + m));
   }
-  return d;
 }
 
-// LUT[m][j] = metric(z[range_m], C[m][j]) in t order (pq_idx.rs:170-179):
-// Euclidean inside IVF-PQ, the build metric for a flat PQIndex; the DM floats
-// of a codeword are one aligned vector load.
-template <int MT, int DM>
-__device__ __forceinline__ float lut_entry(const float *cj, const float *zq, int len) {
-  float c[DM];
-  if (DM % 4 == 0) {
+// The same sums for a 32-subspace code row already in registers (two
+// 16-byte words), K = 256.
+template <int G>
+__device__ __forceinline__ void adc_row32_g(const uint4 w0, const uint4 w1, const float *lut, float (&d)[G]) {
 #pragma unroll
-    for (int u = 0; u < DM; u += 4) {
-      const float4 t = __ldg(reinterpret_cast<const float4 *>(cj + u));
-      c[u] = t.x;
-      c[u + 1] = t.y;
-      c[u + 2] = t.z;
-      c[u + 3] = t.w;
+  for (int g = 0; g < G; ++g) d[g] = 0.0f;
+#pragma unroll
+  for (int m = 0; m < 32; ++m) {
+    const uint4 w = m < 16 ? w0 : w1;
+    const int t = m & 15;
+    const uint32_t wt = t < 4 ? w.x : t < 8 ? w.y : t < 12 ? w.z : w.w;
+    const int e = m * 256 + (int)((wt >> (8 * (t & 3))) & 255u);
+    if (G == 4) {
+      const float4 v = reinterpret_cast<const float4 *>(lut)[e];
+      d[0] = __fadd_rn(d[0], v.x);
+      d[1 % G] = __fadd_rn(d[1 % G], v.y);
+      d[2 % G] = __fadd_rn(d[2 % G], v.z);
+      d[3 % G] = __fadd_rn(d[3 % G], v.w);
+    } else if (G == 2) {
+      const float2 v = reinterpret_cast<const float2 *>(lut)[e];
+      d[0] = __fadd_rn(d[0], v.x);
+      d[1 % G] = __fadd_rn(d[1 % G], v.y);
+    } else {
+      d[0] = __fadd_rn(d[0], lut[e]);
     }
-  } else if (DM == 2) {
-    const float2 t = __ldg(reinterpret_cast<const float2 *>(cj));
-    c[0] = t.x;
-    c[DM - 1] = t.y;
-  } else {
-#pragma unroll
-    for (int u = 0; u < DM; ++u) c[u] = __ldg(cj + u);
   }
-  float s = 0.0f;
-#pragma unroll
-  for (int u = 0; u < DM; ++u)
-    if (u < len) s = dist_op<MT>(s, zq[u], c[u]);
-  return s;
 }
 
-// One CTA handles `per` consecutive (query, list) pairs (sorted by list):
-// LUT, ADC scan of the list in chunks, and the pair's kk best (distance,
-// row) keys -> cand[(q * pmax + slot) * kk ...].
-template <int DM, int VB>
-__global__ void __launch_bounds__(kAdcThreads) adc_scan_kernel(
+// LUT[m][j] for the G queries of a group from one load of the codeword
+// C[m][j] (pq_idx.rs:170-179: metric(z[range_m], C[m][j]) summed in t order;
+// Euclidean inside IVF-PQ, the build metric for a flat PQIndex).  With
+// 4-float codewords (DMC = 4) every thread has 8 codeword loads in flight
+// before it computes; other widths read the codeword per query.
+template <int G, int MT>
+__device__ __forceinline__ void lut_store_g(float *lut, int e, const float (&acc)[G]) {
+  if (G == 4)
+    reinterpret_cast<float4 *>(lut)[e] = make_float4(acc[0], acc[1 % G], acc[2 % G], acc[3 % G]);
+  else if (G == 2)
+    reinterpret_cast<float2 *>(lut)[e] = make_float2(acc[0], acc[1 % G]);
+  else
+    lut[e] = acc[0];
+}
+
+template <int G, int MT, int DMC>
+__device__ __forceinline__ void lut_build_g(const float *book, const float *zq, int dz, const int *sbs,
+                                            const int *sls, int MK, int kbits, int dm, float *lut) {
+  if (DMC == 4) {
+    // every subspace spans 4 dimensions starting at a multiple of 4: the
+    // residual slice of each query is one aligned 16-byte load
+    const float4 *b4 = reinterpret_cast<const float4 *>(book);
+    for (int e0 = threadIdx.x; e0 < MK; e0 += 8 * blockDim.x) {
+      float4 cv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + u * blockDim.x;
+        if (e < MK) cv[u] = __ldg(b4 + e);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + u * blockDim.x;
+        if (e < MK) {
+          const int zo = sbs[e >> kbits];
+          float acc[G];
+#pragma unroll
+          for (int g = 0; g < G; ++g) {
+            const float4 z = *reinterpret_cast<const float4 *>(zq + g * dz + zo);
+            float a = dist_op<MT>(0.0f, z.x, cv[u].x);
+            a = dist_op<MT>(a, z.y, cv[u].y);
+            a = dist_op<MT>(a, z.z, cv[u].z);
+            acc[g] = dist_op<MT>(a, z.w, cv[u].w);
+          }
+          lut_store_g<G, MT>(lut, e, acc);
+        }
+      }
+    }
+  } else {
+    for (int e = threadIdx.x; e < MK; e += blockDim.x) {
+      const int m = e >> kbits, len = sls[m];
+      const float *cj = book + (int64_t)e * dm;
+      float acc[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const float *z = zq + g * dz + sbs[m];
+        float a = 0.0f;
+        for (int t = 0; t < len; ++t) a = dist_op<MT>(a, z[t], __ldg(cj + t));
+        acc[g] = a;
+      }
+      lut_store_g<G, MT>(lut, e, acc);
+    }
+  }
+}
+
+// Per list of a group, the selection state (ints): the range of the
+// distance words, the radix digit position, keys still to take, prefix and
+// mask of the digits fixed so far, done, phase (0: distance digits, 1: row
+// digits among the keys equal to tau), tau, the row bound, the compaction
+// count.
+enum : int {
+  kStMin = 0, kStMax, kStShift, kStRem, kStPrefix, kStMask, kStDone, kStPhase, kStTau, kStRBound,
+  kStCnt, kStWords = 16
+};
+constexpr int kSelDigitBits = 11, kSelNB = 1 << kSelDigitBits;
+
+// Every lane of the warp: the bin of a kSelNB-bin histogram whose
+// cumulative count first reaches rem (1 <= rem <= total) and the count below
+// it.  Lane l owns bins [64 l, 64 l + 64), summed in a rotated order
+// (conflict-free banks); the warp then scans the chosen lane's 64 bins
+// together, two per lane.
+__device__ __forceinline__ void warp_find_bin_all(const uint32_t *hist, uint32_t rem, int &bin,
+                                                  uint32_t &below) {
+  constexpr int nb = kSelNB / 32;
+  const int lane = threadIdx.x & 31;
+  uint32_t sum = 0;
+#pragma unroll 16
+  for (int i = 0; i < nb; ++i) sum += hist[lane * nb + ((i + lane) & (nb - 1))];
+  uint32_t inc = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  const uint32_t exc = inc - sum;
+  const unsigned who = __ballot_sync(0xffffffffu, exc < rem && inc >= rem);
+  const int src = who ? __ffs(who) - 1 : 31;
+  const uint32_t base = __shfl_sync(0xffffffffu, exc, src);
+  // the chosen lane's 64 bins: bins 2 l, 2 l + 1 of its range on lane l
+  const uint32_t b0 = hist[src * nb + 2 * lane], b1 = hist[src * nb + 2 * lane + 1];
+  uint32_t pinc = b0 + b1;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, pinc, o);
+    if (lane >= o) pinc += y;
+  }
+  const uint32_t pexc = base + pinc - (b0 + b1);
+  const bool first = pexc < rem && pexc + b0 >= rem;
+  const bool second = !first && pexc + b0 < rem && pexc + b0 + b1 >= rem;
+  const unsigned w2 = __ballot_sync(0xffffffffu, first || second);
+  const int l2 = w2 ? __ffs(w2) - 1 : 31;
+  const int d = src * nb + 2 * lane + (second ? 1 : 0);
+  const uint32_t run = second ? pexc + b0 : pexc;
+  bin = __shfl_sync(0xffffffffu, w2 ? d : src * nb + nb - 1, l2);
+  below = __shfl_sync(0xffffffffu, run, l2);
+}
+
+// The CTA keeps, for each of the gc lists of a group, the k smallest keys
+// (distance word, row) of its L = held + ch entries: distance words dk[g *
+// stride + i], rows hrow[g * k + i] for i < held (the kept head) and
+// crow[i - held] after it (the chunk, shared by the lists); rows are
+// distinct within a list, so the selection is exact.  A radix select for
+// all lists at once (every thread works in every pass): 11-bit digits of
+// the distance word minus the list's minimum, from the top of its range,
+// stopping per list once the k-th key's bin is taken whole; a list whose
+// k-th distance is tied past the last digit continues on the row digits of
+// the tied keys.  The kept keys go through od / orow to the head.  st holds
+// the per-list state (kStWords ints per list, kStMin / kStMax already set by
+// the caller); hist is zero on entry and on return.  0 < k < L.
+template <int G>
+__device__ __forceinline__ void cta_select_group(uint32_t *dk, int stride, uint32_t *hrow,
+                                                 const uint32_t *crow, int held, int gc, int L, int k,
+                                                 uint32_t *hist, int *st, uint32_t *od, uint32_t *orow) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x < gc) {
+    int *q = st + threadIdx.x * kStWords;
+    const uint32_t span = (uint32_t)q[kStMax] - (uint32_t)q[kStMin];
+    const int sh = 32 - __clz((int)span) - kSelDigitBits;  // __clz(0) = 32
+    q[kStShift] = sh < 0 ? 0 : sh;
+    q[kStRem] = k;
+    q[kStPrefix] = 0;
+    q[kStMask] = 0;
+    q[kStDone] = 0;
+    q[kStPhase] = 0;
+    q[kStTau] = 0;
+    q[kStRBound] = -1;
+    q[kStCnt] = 0;
+  }
+  __syncthreads();
+  for (int pass = 0; pass < 8; ++pass) {
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (g >= gc) break;
+      const int *q = st + g * kStWords;
+      if (q[kStDone]) continue;
+      const uint32_t prefix = (uint32_t)q[kStPrefix], mask = (uint32_t)q[kStMask];
+      const int shift = q[kStShift];
+      uint32_t *h = hist + g * kSelNB;
+      if (q[kStPhase] == 0) {
+        const uint32_t kmin = (uint32_t)q[kStMin];
+        for (int i = threadIdx.x; i < L; i += blockDim.x) {
+          const uint32_t d = dk[g * stride + i] - kmin;
+          if ((d & mask) == prefix) atomicAdd(&h[(d >> shift) & (kSelNB - 1)], 1u);
+        }
+      } else {
+        const uint32_t tau = (uint32_t)q[kStTau];
+        for (int i = threadIdx.x; i < L; i += blockDim.x) {
+          if (dk[g * stride + i] != tau) continue;
+          const uint32_t r = i < held ? hrow[g * k + i] : crow[i - held];
+          if ((r & mask) == prefix) atomicAdd(&h[(r >> shift) & (kSelNB - 1)], 1u);
+        }
+      }
+    }
+    __syncthreads();
+    if (warp < gc && !st[warp * kStWords + kStDone]) {
+      int *q = st + warp * kStWords;
+      uint32_t *h = hist + warp * kSelNB;
+      int bin;
+      uint32_t below;
+      warp_find_bin_all(h, (uint32_t)q[kStRem], bin, below);
+      const uint32_t at = h[bin];
+      __syncwarp();
+      for (int i = lane; i < kSelNB; i += 32) h[i] = 0;
+      if (lane == 0) {
+        const int shift = q[kStShift];
+        const uint32_t rem = (uint32_t)q[kStRem] - below;
+        const uint32_t prefix = (uint32_t)q[kStPrefix] | ((uint32_t)bin << shift);
+        const uint32_t low = shift ? (1u << shift) - 1u : 0u;
+        q[kStRem] = (int)rem;
+        if (at == rem) {  // every key of this bin is kept
+          if (q[kStPhase] == 0) {
+            q[kStTau] = (int)((uint32_t)q[kStMin] + (prefix | low));
+            q[kStRBound] = -1;
+          } else {
+            q[kStRBound] = (int)(prefix | low);
+          }
+          q[kStDone] = 1;
+        } else if (shift == 0 && q[kStPhase] == 0) {
+          // the k-th distance itself, tied: the smallest rows among the ties
+          q[kStTau] = (int)((uint32_t)q[kStMin] + prefix);
+          q[kStPhase] = 1;
+          q[kStShift] = 32 - kSelDigitBits;
+          q[kStPrefix] = 0;
+          q[kStMask] = 0;
+        } else if (shift == 0) {  // unreachable with distinct rows
+          q[kStRBound] = (int)prefix;
+          q[kStDone] = 1;
+        } else {
+          q[kStPrefix] = (int)prefix;
+          q[kStMask] = (int)((uint32_t)q[kStMask] | ((uint32_t)(kSelNB - 1) << shift));
+          q[kStShift] = shift > kSelDigitBits ? shift - kSelDigitBits : 0;
+        }
+      }
+    }
+    __syncthreads();
+    bool all = true;
+    for (int g = 0; g < gc; ++g) all = all && st[g * kStWords + kStDone];
+    if (all) break;
+  }
+  // kept: distance below tau, or equal with the row at or below the bound
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    if (g >= gc) break;
+    const uint32_t tau = (uint32_t)st[g * kStWords + kStTau], rb = (uint32_t)st[g * kStWords + kStRBound];
+    int *cnt = st + g * kStWords + kStCnt;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+      const uint32_t d = dk[g * stride + i];
+      if (d > tau) continue;
+      const uint32_t r = i < held ? hrow[g * k + i] : crow[i - held];
+      if (d < tau || r <= rb) {
+        const int pos = atomicAdd(cnt, 1);
+        if (pos < k) {
+          od[g * k + pos] = d;
+          orow[g * k + pos] = r;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < gc * k; t += blockDim.x) {
+    const int g = t / k, r = t - g * k;
+    dk[g * stride + r] = od[t];
+    hrow[t] = orow[t];
+  }
+  __syncthreads();
+}
+
+// The G-wide LUT's floats, rounded up to a multiple of 4 so that the
+// residual queries behind it start on a 16-byte boundary.
+__host__ __device__ inline size_t adc_lut_floats(int G, int M, int K) {
+  return ((size_t)M * K * G + 3) & ~(size_t)3;
+}
+
+// Dynamic shared memory of adc_group_kernel: the G-wide LUT, the G residual
+// queries, per query the distance words of the kept R plus a chunk and the
+// rows of the kept R, the rows of a chunk, per query a selection histogram
+// and 2 R words of selection output, the selection state, the subspace
+// table.
+__host__ __device__ inline size_t adc_group_smem(int G, int M, int K, int dz, int R) {
+  return sizeof(float) * (adc_lut_floats(G, M, K) + (size_t)G * dz) +
+         sizeof(uint32_t) * ((size_t)G * (kAdcChunk + R) + (size_t)G * R + kAdcChunk +
+                             (size_t)G * kSelNB + (size_t)2 * G * R) +
+         sizeof(int) * ((size_t)kStWords * G + 2 * M);
+}
+
+// One CTA per group of up to G (query, probe slot) pairs of one list
+// (IVFPQIndex::search_knn_adc per probed list, pq_idx.rs:165-194 and
+// 424-437): the G residuals z = q - c_list, one LUT build that reads the
+// list's codebook once for all G queries, one pass over the list's code
+// rows in chunks that reads each row once and scores it for all G queries
+// (the ADC sums bit-identical to a per-query scan), and per chunk a radix
+// select keeping each query's R smallest (distance, row) keys.  Output: the
+// pair's R keys at cand[(q * pmax + slot) * R ...], empty keys past the
+// list's length.  The CTAs are persistent: each takes the next group from
+// *next (zero before the launch) until grp_off[C] groups are done; gmap
+// gives each group's list.
+template <int G, int VB>
+__global__ void __launch_bounds__(kAdcThreads, 1) adc_group_kernel(
     const float *Q, int64_t ldq, const float *centers, int64_t ldc, const float *books,
     const uint8_t *codes, const uint32_t *items, const int64_t *offs, const uint8_t *trained,
-    const uint32_t *pq, const uint32_t *pc, const uint32_t *pslot, int64_t npairs, int per, int M,
-    int K, const int *sb, const int *sl, int mt, int kk, int pmax, uint64_t *cand) {
+    const uint32_t *pq, const uint32_t *pslot, const int64_t *pair_off, const int64_t *grp_off,
+    const uint32_t *gmap, int C, int M, int K, int dm, int aligned4, const int *sb, const int *sl,
+    int mt, int R, int pmax, uint64_t *cand, unsigned long long *next) {
+  const int64_t T = grp_off[C];
   extern __shared__ __align__(16) unsigned char smraw[];
-  float *lut = reinterpret_cast<float *>(smraw);                       // M x K
-  uint32_t *hist = reinterpret_cast<uint32_t *>(lut + M * K);          // kSelBins
-  uint32_t *dkeys = hist + kSelBins;                                   // kAdcChunk + kk
-  uint32_t *rows = dkeys + kAdcChunk + kk;                             // kAdcChunk + kk
-  int *sel = reinterpret_cast<int *>(rows + kAdcChunk + kk);           // kk
-  int *scratch = sel + kk;                                             // 48
-  int *sbs = scratch + 48;                                             // M subspace starts
-  int *sls = sbs + M;                                                  // M subspace lengths
-  __shared__ __align__(16) float zq[1024];
-  for (int b = threadIdx.x; b < kSelBins; b += blockDim.x) hist[b] = 0;
+  __shared__ int s_c, s_gc;
+  __shared__ long long s_p0, s_b;
+  const int dcov = sb[M - 1] + sl[M - 1];
+  const int dz = (dcov + 3) & ~3;
+  const int stride = kAdcChunk + R;
+  float *lut = reinterpret_cast<float *>(smraw);                       // M * K * G (rounded to 4)
+  float *zq = lut + adc_lut_floats(G, M, K);                           // G * dz, 16-byte aligned
+  uint32_t *dk = reinterpret_cast<uint32_t *>(zq + G * dz);           // G * (R + chunk)
+  uint32_t *hrow = dk + G * stride;                                    // G * R
+  uint32_t *crow = hrow + G * R;                                       // chunk
+  uint32_t *hist = crow + kAdcChunk;                                   // G * kSelNB
+  uint32_t *od = hist + G * kSelNB;                                    // G * R
+  uint32_t *orow = od + G * R;                                         // G * R
+  int *st = reinterpret_cast<int *>(orow + G * R);                     // G * kStWords
+  int *sbs = st + G * kStWords;                                        // M
+  int *sls = sbs + M;                                                  // M
   for (int m = threadIdx.x; m < M; m += blockDim.x) {
     sbs[m] = sb[m];
     sls[m] = sl[m];
   }
+  for (int t = threadIdx.x; t < G * kSelNB; t += blockDim.x) hist[t] = 0;
   const int kbits = 31 - __clz(K);  // K = 2^sub_bits
-  for (int64_t pi = (int64_t)blockIdx.x * per; pi < min(npairs, (int64_t)(blockIdx.x + 1) * per); ++pi) {
-    const int64_t q = pq[pi];
-    const int c = (int)pc[pi];
-    const int slot = (int)pslot[pi];
-    uint64_t *out = cand + (q * pmax + slot) * kk;
-    const int64_t lo = offs[c], L = offs[c + 1] - lo;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const long long b = (long long)atomicAdd(next, 1ull);
+      s_b = b;
+      if (b < T) {
+        const int c = (int)gmap[b];
+        const int64_t p0 = pair_off[c] + (b - grp_off[c]) * G;
+        s_c = c;
+        s_p0 = p0;
+        s_gc = (int)min((int64_t)G, pair_off[c + 1] - p0);
+      }
+    }
+    __syncthreads();
+    if (s_b >= T) return;
+    const int c = s_c, gc = s_gc;
+    const int64_t p0 = s_p0;
+    const int64_t lrow = offs[c], L = offs[c + 1] - lrow;
     if (!trained[c] || L == 0) {
-      for (int r = threadIdx.x; r < kk; r += blockDim.x) out[r] = kEmptyKey;
+      for (int t = threadIdx.x; t < gc * R; t += blockDim.x) {
+        const int64_t pi = p0 + t / R;
+        cand[((int64_t)pq[pi] * pmax + pslot[pi]) * R + t % R] = kEmptyKey;
+      }
+      __syncthreads();  // s_c / s_p0 / s_gc are read before the next group overwrites them
       continue;
     }
-    // z = q - c_list over the covered dimensions (pq_idx.rs:158-161)
-    const int dcov = sb[M - 1] + sl[M - 1];
-    __syncthreads();  // the previous pair is done with zq and the LUT
-    for (int t = threadIdx.x; t < dcov; t += blockDim.x)
-      zq[t] = __fsub_rn(Q[q * ldq + t], centers[(int64_t)c * ldc + t]);
+    // z = q - c_list over the covered dimensions (pq_idx.rs:158-161); group
+    // slots past gc repeat the first query (their results are not written)
+    for (int t = threadIdx.x; t < G * dcov; t += blockDim.x) {
+      const int g = t / dcov, u = t - g * dcov;
+      const int64_t q = pq[p0 + (g < gc ? g : 0)];
+      zq[g * dz + u] = __fsub_rn(Q[q * ldq + u], centers[(int64_t)c * ldc + u]);
+    }
     __syncthreads();
-    const float *book = books + (int64_t)c * M * K * DM;
-    if (DM == 4 && mt == M_L2) {
-      // 8 codewords' loads in flight per thread before any entry is computed
-      const float4 *b4 = reinterpret_cast<const float4 *>(book);
-      const int MK = M * K;
-      for (int e0 = threadIdx.x; e0 < MK; e0 += 8 * kAdcThreads) {
-        float4 cv[8];
+    const float *book = books + (int64_t)c * M * K * dm;
+    if (mt == M_L2 && aligned4)
+      lut_build_g<G, M_L2, 4>(book, zq, dz, sbs, sls, M * K, kbits, dm, lut);
+    else if (mt == M_L2)
+      lut_build_g<G, M_L2, 0>(book, zq, dz, sbs, sls, M * K, kbits, dm, lut);
+    else if (mt == M_L1)
+      lut_build_g<G, M_L1, 0>(book, zq, dz, sbs, sls, M * K, kbits, dm, lut);
+    else
+      lut_build_g<G, M_IP, 0>(book, zq, dz, sbs, sls, M * K, kbits, dm, lut);
+    const uint8_t *lcodes = codes + lrow * M;
+    int held = 0;
+    for (int64_t c0 = 0; c0 < L; c0 += kAdcChunk) {
+      const int ch = (int)min((int64_t)kAdcChunk, L - c0);
+      if (threadIdx.x < G) {
+        st[threadIdx.x * kStWords + kStMin] = -1;  // 0xffffffff as unsigned
+        st[threadIdx.x * kStWords + kStMax] = 0;
+      }
+      __syncthreads();  // the LUT is built; the previous chunk's selection is done
+      uint32_t kmin[G], kmax[G];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int e = e0 + u * kAdcThreads;
-          if (e < MK) cv[u] = __ldg(b4 + e);
+      for (int g = 0; g < G; ++g) {
+        kmin[g] = 0xffffffffu;
+        kmax[g] = 0u;
+      }
+      for (int i = threadIdx.x; i < held; i += blockDim.x) {  // the kept head is in the range
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+          const uint32_t v = dk[g * stride + i];
+          kmin[g] = min(kmin[g], v);
+          kmax[g] = max(kmax[g], v);
         }
+      }
+      if (VB == 16 && M == 32 && K == 256) {
+        // 32-byte code rows: the next row's words are loaded while this
+        // row is scored
+        const uint4 *rows4 = reinterpret_cast<const uint4 *>(lcodes + c0 * 32);
+        int i = threadIdx.x;
+        uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0;
+        uint32_t row = 0;
+        if (i < ch) {
+          w0 = __ldg(rows4 + 2 * i);
+          w1 = __ldg(rows4 + 2 * i + 1);
+          row = items[lrow + c0 + i];
+        }
+        for (; i < ch; i += blockDim.x) {
+          const int in = i + blockDim.x;
+          uint4 n0 = w0, n1 = w1;
+          uint32_t nrow = 0;
+          if (in < ch) {
+            n0 = __ldg(rows4 + 2 * in);
+            n1 = __ldg(rows4 + 2 * in + 1);
+            nrow = items[lrow + c0 + in];
+          }
+          float d[G];
+          adc_row32_g<G>(w0, w1, lut, d);
+          crow[i] = row;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int e = e0 + u * kAdcThreads;
-          if (e < MK) {
-            const int m = e >> kbits, len = sls[m];
-            const float *z = zq + sbs[m];
-            const float cw[4] = {cv[u].x, cv[u].y, cv[u].z, cv[u].w};
-            float acc = 0.0f;
+          for (int g = 0; g < G; ++g) {
+            const uint32_t v = f2ord(d[g]);
+            dk[g * stride + held + i] = v;
+            kmin[g] = min(kmin[g], v);
+            kmax[g] = max(kmax[g], v);
+          }
+          w0 = n0;
+          w1 = n1;
+          row = nrow;
+        }
+      } else {
+        for (int i = threadIdx.x; i < ch; i += blockDim.x) {
+          float d[G];
+          if (K == 256)
+            adc_row_g<G, VB, 256>(lcodes + (c0 + i) * M, lut, M, K, d);
+          else
+            adc_row_g<G, VB, 0>(lcodes + (c0 + i) * M, lut, M, K, d);
+          crow[i] = items[lrow + c0 + i];
 #pragma unroll
-            for (int t = 0; t < 4; ++t)
-              if (t < len) acc = dist_op<M_L2>(acc, z[t], cw[t]);
-            lut[e] = acc;
+          for (int g = 0; g < G; ++g) {
+            const uint32_t v = f2ord(d[g]);
+            dk[g * stride + held + i] = v;
+            kmin[g] = min(kmin[g], v);
+            kmax[g] = max(kmax[g], v);
           }
         }
       }
-    } else if (mt == M_L2) {
-      for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
-        const int m = e >> kbits;
-        lut[e] = lut_entry<M_L2, DM>(book + (int64_t)e * DM, zq + sbs[m], sls[m]);
-      }
-    } else if (mt == M_L1) {
-      for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
-        const int m = e >> kbits;
-        lut[e] = lut_entry<M_L1, DM>(book + (int64_t)e * DM, zq + sbs[m], sls[m]);
-      }
-    } else {
-      for (int e = threadIdx.x; e < M * K; e += blockDim.x) {
-        const int m = e >> kbits;
-        lut[e] = lut_entry<M_IP, DM>(book + (int64_t)e * DM, zq + sbs[m], sls[m]);
+      const int tot = held + ch;
+      if (tot > R) {
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+          const uint32_t lo = __reduce_min_sync(0xffffffffu, kmin[g]);
+          const uint32_t hi = __reduce_max_sync(0xffffffffu, kmax[g]);
+          if ((threadIdx.x & 31) == 0 && g < gc) {
+            atomicMin(reinterpret_cast<unsigned *>(&st[g * kStWords + kStMin]), lo);
+            atomicMax(reinterpret_cast<unsigned *>(&st[g * kStWords + kStMax]), hi);
+          }
+        }
+        __syncthreads();
+        cta_select_group<G>(dk, stride, hrow, crow, held, gc, tot, R, hist, st, od, orow);
+        held = R;
+      } else {
+        // short so far: the chunk's rows join the head as they are
+        __syncthreads();
+        for (int t = threadIdx.x; t < gc * ch; t += blockDim.x) {
+          const int g = t / ch, i = t - g * ch;
+          hrow[g * R + held + i] = crow[i];
+        }
+        held = tot;
       }
     }
     __syncthreads();
-    // scan in chunks; running kk best kept at the head of dkeys/rows
-    int held = 0;
-    const uint8_t *lcodes = codes + lo * M;
-    for (int64_t c0 = 0; c0 < L; c0 += kAdcChunk) {
-      const int ch = (int)(kAdcChunk < L - c0 ? (int64_t)kAdcChunk : L - c0);
-      for (int i = threadIdx.x; i < ch; i += blockDim.x) {
-        const float d = K == 256 ? adc_row<VB, 256>(lcodes + (c0 + i) * M, lut, M, K)
-                                 : adc_row<VB, 0>(lcodes + (c0 + i) * M, lut, M, K);
-        dkeys[held + i] = f2ord(d);
-        rows[held + i] = items[lo + c0 + i];
-      }
-      __syncthreads();
-      const int tot = held + ch;
-      if (tot <= kk) {
-        held = tot;
-        continue;
-      }
-      cta_select_k(dkeys, tot, kk, sel, hist, scratch);
-      // gather the selection to the head (through registers: sel is unordered)
-      static_assert(kAdcThreads * 4 >= 1024, "kk <= 1024 is held in 4 registers a thread");
-      uint32_t kv[4], rv[4];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int r = threadIdx.x + t * kAdcThreads;
-        if (r < kk) {
-          kv[t] = dkeys[sel[r]];
-          rv[t] = rows[sel[r]];
-        }
-      }
-      __syncthreads();
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int r = threadIdx.x + t * kAdcThreads;
-        if (r < kk) {
-          dkeys[r] = kv[t];
-          rows[r] = rv[t];
-        }
-      }
-      held = kk;
-      __syncthreads();
+    for (int t = threadIdx.x; t < gc * R; t += blockDim.x) {
+      const int g = t / R, r = t - g * R;
+      const int64_t pi = p0 + g;
+      cand[((int64_t)pq[pi] * pmax + pslot[pi]) * R + r] =
+          r < held ? (((uint64_t)dk[g * stride + r] << 32) | hrow[g * R + r]) : kEmptyKey;
     }
-    for (int r = threadIdx.x; r < kk; r += blockDim.x)
-      out[r] = r < held ? (((uint64_t)dkeys[r] << 32) | rows[r]) : kEmptyKey;
+    __syncthreads();  // the group's shared state is read before the next group overwrites it
   }
+}
+
+// Group g's list: for every list c, the groups grp_off[c] .. grp_off[c+1].
+__global__ void group_map_kernel(const int64_t *grp_off, int C, uint32_t *gmap) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  for (int64_t g = grp_off[c]; g < grp_off[c + 1]; ++g) gmap[g] = (uint32_t)c;
 }
 
 // ---------------------------------------------------------------------------
@@ -1024,6 +1284,9 @@ static void init_layout(hora_index *h, IvfState &v) {
     v.sub_begin[i] = (int)b;
     v.sub_len[i] = (int)(e - b);
   }
+  v.sub_aligned4 = v.dmax == 4;
+  for (int64_t i = 0; i < v.n_sub; ++i)
+    v.sub_aligned4 = v.sub_aligned4 && v.sub_begin[i] == 4 * i && v.sub_len[i] == 4;
 }
 
 static int upload_layout(IvfState &v, cudaStream_t s) {
@@ -1254,35 +1517,49 @@ int ivf_set_codebooks(hora_index *h, const float *centers, const float *codebook
   return HORA_OK;
 }
 
-template <int DM, int VB>
-static int launch_adc_vb(IvfState &v, SearchWorkspace &ws, const float *Q, int64_t ldq, int64_t ldc,
-                         int64_t npairs, int per, int kk, int pmax, uint64_t *cand, cudaStream_t s) {
-  // LUT, histogram, keys + rows of a chunk and the carried kk, selection, scratch
-  size_t smem = sizeof(float) * v.n_sub * v.K + sizeof(uint32_t) * kSelBins +
-                2 * sizeof(uint32_t) * (kAdcChunk + kk) + sizeof(int) * kk + sizeof(int) * 48 +
-                2 * sizeof(int) * v.n_sub;
-  if (smem > 200 * 1024) return fail(HORA_ECAP, "IVF-PQ: LUT too large for shared memory");
-  HORA_SMEM_ATTR((adc_scan_kernel<DM, VB>), smem);
-  unsigned grid = (unsigned)ceil_div(npairs, per);
-  if (grid == 0) return HORA_OK;
+template <int G, int VB>
+static int launch_adc_g(IvfState &v, SearchWorkspace &ws, const float *Q, int64_t ldq, int64_t ldc,
+                        int64_t max_groups, int dz, int R, int pmax, uint64_t *cand, cudaStream_t s) {
+  const size_t smem = adc_group_smem(G, (int)v.n_sub, (int)v.K, dz, R);
+  HORA_SMEM_ATTR((adc_group_kernel<G, VB>), smem);
+  if (max_groups <= 0) return HORA_OK;
+  // persistent CTAs: as many as are resident at once, at most one per group
+  int dev = 0, nsm = 0, per_sm = 0;
+  HORA_CUDA_TRY(cudaGetDevice(&dev));
+  HORA_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  HORA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adc_group_kernel<G, VB>, kAdcThreads, smem));
+  const int64_t grid = std::min<int64_t>(max_groups, (int64_t)nsm * std::max(per_sm, 1));
+  HORA_TRY(ws.adc_next.reserve(sizeof(unsigned long long)));
+  HORA_CUDA_TRY(cudaMemsetAsync(ws.adc_next.ptr, 0, sizeof(unsigned long long), s));
   ProfScope ps("adc_scan", s);
-  adc_scan_kernel<DM, VB><<<grid, kAdcThreads, smem, s>>>(
+  adc_group_kernel<G, VB><<<(unsigned)grid, kAdcThreads, smem, s>>>(
       Q, ldq, v.centers.as<float>(), ldc, v.books.as<float>(), v.codes.as<uint8_t>(),
       v.items.as<uint32_t>(), v.offsets.as<int64_t>(), v.trained.as<uint8_t>(), ws.pair_q.as<uint32_t>(),
-      ws.pair_c.as<uint32_t>(), ws.pair_slot.as<uint32_t>(), npairs, per, (int)v.n_sub, (int)v.K,
-      v.sub_begin_d.as<int>(), v.sub_len_d.as<int>(), v.pq_metric, kk, pmax, cand);
+      ws.pair_slot.as<uint32_t>(), ws.pair_off.as<int64_t>(), ws.pair_off.as<int64_t>() + (v.n_list + 1),
+      ws.adc_gmap.as<uint32_t>(), (int)v.n_list, (int)v.n_sub, (int)v.K, (int)v.dmax, v.sub_aligned4 ? 1 : 0,
+      v.sub_begin_d.as<int>(), v.sub_len_d.as<int>(), v.pq_metric, R, pmax, cand,
+      ws.adc_next.as<unsigned long long>());
   HORA_LAUNCHED();
   return HORA_OK;
 }
 
 // Code rows are n_sub bytes apart: the widest load that divides n_sub.
-template <int DM>
-static int launch_adc(IvfState &v, SearchWorkspace &ws, const float *Q, int64_t ldq, int64_t ldc,
-                      int64_t npairs, int per, int kk, int pmax, uint64_t *cand, cudaStream_t s) {
-  if (v.n_sub % 16 == 0) return launch_adc_vb<DM, 16>(v, ws, Q, ldq, ldc, npairs, per, kk, pmax, cand, s);
-  if (v.n_sub % 8 == 0) return launch_adc_vb<DM, 8>(v, ws, Q, ldq, ldc, npairs, per, kk, pmax, cand, s);
-  if (v.n_sub % 4 == 0) return launch_adc_vb<DM, 4>(v, ws, Q, ldq, ldc, npairs, per, kk, pmax, cand, s);
-  return launch_adc_vb<DM, 1>(v, ws, Q, ldq, ldc, npairs, per, kk, pmax, cand, s);
+template <int G>
+static int launch_adc_vb(IvfState &v, SearchWorkspace &ws, const float *Q, int64_t ldq, int64_t ldc,
+                         int64_t max_groups, int dz, int R, int pmax, uint64_t *cand, cudaStream_t s) {
+  if (v.n_sub % 16 == 0) return launch_adc_g<G, 16>(v, ws, Q, ldq, ldc, max_groups, dz, R, pmax, cand, s);
+  if (v.n_sub % 8 == 0) return launch_adc_g<G, 8>(v, ws, Q, ldq, ldc, max_groups, dz, R, pmax, cand, s);
+  if (v.n_sub % 4 == 0) return launch_adc_g<G, 4>(v, ws, Q, ldq, ldc, max_groups, dz, R, pmax, cand, s);
+  return launch_adc_g<G, 1>(v, ws, Q, ldq, ldc, max_groups, dz, R, pmax, cand, s);
+}
+
+// Queries per ADC group: the most (4, 2 or 1) whose shared memory fits.
+constexpr size_t kAdcSmemMax = 227 * 1024;  // dynamic shared memory a CTA may use
+
+static int adc_group_width(const IvfState &v, int dz, int R) {
+  for (int G = 4; G > 1; G >>= 1)
+    if (adc_group_smem(G, (int)v.n_sub, (int)v.K, dz, R) <= kAdcSmemMax) return G;
+  return 1;
 }
 
 int ivf_pmax(const hora_index *h, int64_t nprobe) {
@@ -1327,34 +1604,38 @@ int ivf_adc_merge(hora_index *h, int64_t nq, int pmax, int jbegin, const uint32_
   IvfState &v = *h->ivfs;
   const int C = (int)v.n_list;
   const float *Q = ws.q.as<float>();
+  const int dcov = v.sub_begin.back() + v.sub_len.back();
+  const int dz = (dcov + 3) & ~3;
+  const int G = adc_group_width(v, dz, R);
+  if (adc_group_smem(G, (int)v.n_sub, (int)v.K, dz, R) > kAdcSmemMax)
+    return fail(HORA_ECAP, "IVF-PQ: LUT too large for shared memory");
   HORA_TRY(ws.pair_cnt.reserve(sizeof(int64_t) * (C + 1) * 2));
-  HORA_TRY(ws.pair_off.reserve(sizeof(int64_t) * (C + 1)));
+  HORA_TRY(ws.pair_off.reserve(sizeof(int64_t) * (C + 1) * 2));  // pair offsets, then group offsets
   int64_t *cnt = ws.pair_cnt.as<int64_t>();
   int64_t *cursor = cnt + (C + 1);
+  int64_t *poff = ws.pair_off.as<int64_t>();
   HORA_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (C + 1) * 2, s));
   const int64_t tot = nq * pmax;
-  {
-    ProfScope ps("ivf_pairs", s);
-    pair_hist_kernel<<<ceil_div(tot, 256), 256, 0, s>>>(ws.probes.as<uint64_t>(), nq, pmax, jbegin,
-                                                       d_nprobe, C, cnt);
-    HORA_LAUNCHED();
-    offsets_scan_kernel<<<1, 1024, 0, s>>>(cnt, C, ws.pair_off.as<int64_t>());
-    HORA_LAUNCHED();
-  }
-  int64_t npairs = nq * (pmax - jbegin);
-  if (d_nprobe) {
-    HORA_CUDA_TRY(cudaMemcpyAsync(&npairs, ws.pair_off.as<int64_t>() + C, sizeof(int64_t),
-                                  cudaMemcpyDeviceToHost, s));
-    HORA_CUDA_TRY(cudaStreamSynchronize(s));
-  }
-  if (npairs <= 0) return HORA_OK;
+  // pairs (query, probe slot) grouped by list, no host round trip: the ADC
+  // grid is an upper bound on the number of groups
+  const int64_t max_pairs = nq * (int64_t)(pmax - jbegin);
+  if (max_pairs <= 0) return HORA_OK;
+  const int64_t max_groups = ceil_div(max_pairs, G) + std::min<int64_t>(C, max_pairs);
+  HORA_TRY(ws.adc_gmap.reserve(sizeof(uint32_t) * max_groups));
   HORA_TRY(ws.pair_q.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
   HORA_TRY(ws.pair_c.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
   HORA_TRY(ws.pair_slot.reserve(sizeof(uint32_t) * std::max<int64_t>(tot, 1)));
   {
     ProfScope ps("ivf_pairs", s);
+    pair_hist_kernel<<<ceil_div(tot, 256), 256, 0, s>>>(ws.probes.as<uint64_t>(), nq, pmax, jbegin,
+                                                       d_nprobe, C, cnt);
+    HORA_LAUNCHED();
+    group_scan_kernel<<<1, 1024, 0, s>>>(cnt, C, G, poff, poff + (C + 1));
+    HORA_LAUNCHED();
+    group_map_kernel<<<ceil_div(C, 256), 256, 0, s>>>(poff + (C + 1), C, ws.adc_gmap.as<uint32_t>());
+    HORA_LAUNCHED();
     pair_scatter_kernel<<<ceil_div(tot, 256), 256, 0, s>>>(
-        ws.probes.as<uint64_t>(), nq, pmax, jbegin, d_nprobe, C, ws.pair_off.as<int64_t>(), cursor,
+        ws.probes.as<uint64_t>(), nq, pmax, jbegin, d_nprobe, C, poff, cursor,
         ws.pair_q.as<uint32_t>(), ws.pair_c.as<uint32_t>(), ws.pair_slot.as<uint32_t>());
     HORA_LAUNCHED();
   }
@@ -1372,13 +1653,11 @@ int ivf_adc_merge(hora_index *h, int64_t nq, int pmax, int jbegin, const uint32_
                                                          ws.count.as<uint32_t>());
     HORA_LAUNCHED();
   }
-  const int per = 4;
-  switch (v.dmax) {
-    case 1: HORA_TRY(launch_adc<1>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
-    case 2: HORA_TRY(launch_adc<2>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
-    case 4: HORA_TRY(launch_adc<4>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
-    case 8: HORA_TRY(launch_adc<8>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
-    default: HORA_TRY(launch_adc<16>(v, ws, Q, h->ld, h->ld, npairs, per, R, pmax, ws.ivf_cand.as<uint64_t>(), s)); break;
+  uint64_t *cand = ws.ivf_cand.as<uint64_t>();
+  switch (G) {
+    case 4: HORA_TRY(launch_adc_vb<4>(v, ws, Q, h->ld, h->ld, max_groups, dz, R, pmax, cand, s)); break;
+    case 2: HORA_TRY(launch_adc_vb<2>(v, ws, Q, h->ld, h->ld, max_groups, dz, R, pmax, cand, s)); break;
+    default: HORA_TRY(launch_adc_vb<1>(v, ws, Q, h->ld, h->ld, max_groups, dz, R, pmax, cand, s)); break;
   }
   // per-query merge of the candidates (pq_idx.rs:429-436): each query's
   // slots [jbegin, nprobe) are contiguous, so the merge reads

@@ -15,7 +15,9 @@
 // Training (hora_ivfpq_train_nprobe): labels come from the method itself —
 // for each training query the smallest nprobe in 1, 2, 4, ... max whose
 // top-10 reaches the recall target against exact brute force (with k = 10 a
-// per-query recall of 0.95 means all ten) — and the MLP is fitted on the GPU
+// per-query recall of 0.95 means all ten; a query that no grid nprobe brings
+// there takes the smallest nprobe reaching its best recall) — and the MLP is
+// fitted on the GPU
 // with this file's forward / backward / Adam kernels (asymmetric squared
 // error: under-predicting nprobe costs recall and is weighted more).  The
 // last tenth of the training queries is held out: on it the model's margin
@@ -289,11 +291,10 @@ __global__ void fill_u32_kernel(uint32_t *a, int64_t n, uint32_t v) {
   if (i < n) a[i] = v;
 }
 
-// per-query recall@10 of result keys vs exact keys -> label update; the hit
-// count at every grid nprobe is kept for the margin calibration
-__global__ void label_kernel(const uint64_t *res, int kr, const uint64_t *exact, int ke, int64_t nq,
-                             float target, float log2p, float *label, uint8_t *done, uint8_t *hits,
-                             int gi, int ng) {
+// per query, the number of its exact top-10 rows found by the search at
+// grid nprobe number gi (the labels and the margin calibration read these)
+__global__ void hits_kernel(const uint64_t *res, int kr, const uint64_t *exact, int ke, int64_t nq,
+                            uint8_t *hits, int gi, int ng) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq) return;
   int hit = 0, tot = 0;
@@ -308,11 +309,6 @@ __global__ void label_kernel(const uint64_t *res, int kr, const uint64_t *exact,
       }
   }
   hits[q * ng + gi] = (uint8_t)(tot == 0 ? ke : hit);
-  if (done[q]) return;
-  if (tot == 0 || (float)hit >= target * (float)tot - 1e-6f) {
-    label[q] = log2p;
-    done[q] = 1;
-  }
 }
 
 // ---- search with the model ---------------------------------------------------------------
@@ -505,23 +501,15 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
   // the last tenth is held out for the margin calibration
   const int64_t n_cal = N >= 2048 ? N / 10 : 0;
   const int64_t N_fit = N - n_cal;
-  DevBuf feats, labels, done, hits, exact, res, M, npq;
+  DevBuf feats, labels, hits, exact, res, M, npq;
   HORA_TRY(feats.reserve(4 * N * kF));
   HORA_TRY(labels.reserve(4 * N));
-  HORA_TRY(done.reserve(N));
   HORA_TRY(hits.reserve((size_t)N * ng));
   const int64_t chunk = 8192;
   HORA_TRY(exact.reserve(8 * chunk * kk));
   HORA_TRY(res.reserve(8 * chunk * kk));
   HORA_TRY(M.reserve(8 * chunk * std::max(R, kk)));
   HORA_TRY(npq.reserve(4 * chunk));
-  HORA_CUDA_TRY(cudaMemsetAsync(done.ptr, 0, N, s));
-  const float lmax = std::log2((float)pm);
-  {
-    std::vector<float> init(N, lmax);
-    HORA_CUDA_TRY(cudaMemcpyAsync(labels.ptr, init.data(), 4 * N, cudaMemcpyHostToDevice, s));
-    HORA_CUDA_TRY(cudaStreamSynchronize(s));
-  }
   const int saved_learned = h->learned_nprobe;
   h->learned_nprobe = 0;
   BaseView bv = base_view(h);
@@ -534,14 +522,11 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
     int retries = 0;
     HORA_TRY(bf_topk_exact(bv, h->metric, ws.q.as<float>(), ws.qnorm.as<float>(), nq, kk, h->cand_cap,
                            ws, exact.as<uint64_t>(), s, &retries));
-    // labels: smallest grid nprobe whose top-10 reaches the target; hits at every grid nprobe
+    // hits at every grid nprobe (the labels are derived from them below)
     for (int gi = 0; gi < ng; ++gi) {
-      const int p = grid[gi];
-      HORA_TRY(ivf_search_keys(h, nq, kk, p, nullptr, ws, res.as<uint64_t>(), s));
-      label_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(res.as<uint64_t>(), kk, exact.as<uint64_t>(), kk, nq,
-                                                     (float)recall_target, std::log2((float)p),
-                                                     labels.as<float>() + lo, done.as<uint8_t>() + lo,
-                                                     hits.as<uint8_t>() + lo * ng, gi, ng);
+      HORA_TRY(ivf_search_keys(h, nq, kk, grid[gi], nullptr, ws, res.as<uint64_t>(), s));
+      hits_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(res.as<uint64_t>(), kk, exact.as<uint64_t>(), kk, nq,
+                                                    hits.as<uint8_t>() + lo * ng, gi, ng);
       HORA_LAUNCHED();
     }
     // features after the first p1 probes
@@ -562,9 +547,24 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
   std::vector<float> hf(N * kF), hl(N);
   std::vector<uint8_t> hh((size_t)N * ng);
   HORA_CUDA_TRY(cudaMemcpyAsync(hf.data(), feats.ptr, 4 * N * kF, cudaMemcpyDeviceToHost, s));
-  HORA_CUDA_TRY(cudaMemcpyAsync(hl.data(), labels.ptr, 4 * N, cudaMemcpyDeviceToHost, s));
   HORA_CUDA_TRY(cudaMemcpyAsync(hh.data(), hits.ptr, (size_t)N * ng, cudaMemcpyDeviceToHost, s));
   HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  // label: log2 of the smallest grid nprobe whose top-10 reaches the target
+  // (ceil(target x 10) of the exact ten: all ten for 0.95); a query whose
+  // best recall over the whole grid stays below that (its neighbours are
+  // lost to PQ error, not to unprobed lists) is labelled with the smallest
+  // nprobe reaching that best recall: more lists would not help it
+  const int need = (int)std::ceil(recall_target * kk - 1e-6);
+  for (int64_t i = 0; i < N; ++i) {
+    const uint8_t *hq = hh.data() + (size_t)i * ng;
+    int best = 0;
+    for (int gi = 0; gi < ng; ++gi) best = std::max(best, (int)hq[gi]);
+    const int reach = std::min(need, best);
+    int gi = 0;
+    while (gi + 1 < ng && hq[gi] < reach) ++gi;
+    hl[i] = std::log2((float)grid[gi]);
+  }
+  HORA_CUDA_TRY(cudaMemcpyAsync(labels.ptr, hl.data(), 4 * N, cudaMemcpyHostToDevice, s));
   std::vector<float> mean(kF, 0.0f), inv(kF, 1.0f);
   for (int t = 0; t < kF; ++t) {
     double m = 0, v = 0;
@@ -647,7 +647,7 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
   // each query's nprobe as the search computes it, and its recall taken from
   // the hits measured at the largest grid nprobe not above that (nprobe 3 is
   // scored as 2); the smallest margin whose held-out recall@10 reaches the
-  // target wins
+  // target (less two standard errors) wins
   if (n_cal > 0) {
     DevBuf pred;
     HORA_TRY(pred.reserve(4 * n_cal));
@@ -661,18 +661,25 @@ int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t 
     bool found = false;
     for (int mi = -160; mi <= 160 && !found; ++mi) {
       const float m = (float)mi / 32.0f;
-      double hit = 0, probes = 0;
+      double hit = 0, hit2 = 0, probes = 0;
       for (int64_t i = 0; i < n_cal; ++i) {
         float e = std::min(hp[i] + m, 20.0f);
         int p = (int)std::ceil(std::exp2(e) - 1e-4f);
         p = std::min(std::max(p, lo), std::max(hi, lo));
         int gi = 0;
         while (gi + 1 < ng && grid[gi + 1] <= p) ++gi;
-        hit += hh[(size_t)(N_fit + i) * ng + gi];
+        const double r = hh[(size_t)(N_fit + i) * ng + gi] / 10.0;
+        hit += r;
+        hit2 += r * r;
         probes += p;
       }
-      const double rec = hit / (10.0 * (double)n_cal);
-      if (rec >= recall_target || mi == 160) {
+      // the held-out recall must clear the target by two standard errors of
+      // its mean (per-query recalls), so that other queries of the same law
+      // land at or above the target
+      const double rec = hit / (double)n_cal;
+      const double var = std::max(0.0, hit2 / (double)n_cal - rec * rec);
+      const double se = std::sqrt(var / (double)n_cal);
+      if (rec - 2.0 * se >= recall_target || mi == 160) {
         md->margin = m;
         md->cal_recall = rec;
         md->cal_nprobe = probes / (double)n_cal;

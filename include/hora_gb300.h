@@ -226,12 +226,13 @@ int hora_search_nprobe(hora_index *h, const float *queries, uint64_t nq, uint64_
 /* Generates labels on n_train training queries (host or device memory): the
  * smallest nprobe in the grid 1,2,4..max_nprobe whose top-10 reaches the
  * recall target against exact brute force (per query: with k = 10 a target
- * of 0.95 means all ten), trains the MLP on the GPU with the library's
- * forward/backward kernels on the first nine tenths, calibrates the margin
- * on the last tenth (the smallest that keeps its recall@10 at or above the
- * target) and installs the model; hora_idx_info reports the calibration.
- * stats_out (may be NULL) receives [final loss, label mean, label max,
- * epochs]. */
+ * of 0.95 means all ten; a query no grid nprobe brings there takes the
+ * smallest nprobe reaching its best recall), trains the MLP on the GPU with
+ * the library's forward/backward kernels on the first nine tenths,
+ * calibrates the margin on the last tenth (the smallest that keeps its
+ * recall@10 at or above the target) and installs the model; hora_idx_info
+ * reports the calibration.  stats_out (may be NULL) receives [final loss,
+ * label mean, label max, epochs]. */
 int hora_ivfpq_train_nprobe(hora_index *h, const float *train_queries, uint64_t n_train,
                             uint64_t max_nprobe, double recall_target, uint64_t epochs,
                             double *stats_out);

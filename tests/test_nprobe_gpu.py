@@ -45,12 +45,22 @@ def _ivf(hora, synth, n=200_000, d=64, lists=256):
 
 
 def test_learned_nprobe_trains_and_gains(hora, oracle, gpu):
+    """Labels at a per-query recall of 0.95 (all ten of the exact top-10),
+    the margin calibrated on the training queries' held-out tenth for an
+    aggregate recall@10 of 0.95, then judged on other held-out queries:
+    recall near the target with fewer probes than the smallest fixed nprobe
+    that reaches the same recall."""
+    import json
     from hora_gb300 import synth
     ix, X = _ivf(hora, synth)
     train = synth.mixture(20_000, 64, 512, stream=52, spread=1.2)
     held = synth.mixture(2_000, 64, 512, stream=53, spread=1.2)
-    stats = ix.train_nprobe(train, max_nprobe=64, recall_target=0.9, epochs=20)
+    ix.set_option(hora.Option.NPROBE_PHASE1, 1)
+    stats = ix.train_nprobe(train, max_nprobe=64, recall_target=0.95, epochs=20)
     assert np.isfinite(stats[0]) and stats[2] <= 6.0
+    model = json.loads(ix.idx_info())["ivfpq"]["nprobe_model"]
+    assert model["phase1"] == 1 and model["target"] == 0.95 and model["heldout_queries"] == 2000
+    assert model["heldout_recall"] >= 0.95, model
     # exact neighbours of the held-out queries
     bfi = hora.BruteForceIndex(64)
     bfi.madd(X, None)
@@ -65,11 +75,10 @@ def test_learned_nprobe_trains_and_gains(hora, oracle, gpu):
         ids, _ = ix.search_batch(held, 10, nprobe=npb)
         fixed[npb] = rec(ids)
     ix.set_option(hora.Option.LEARNED_NPROBE, 1)
-    ix.set_option(hora.Option.NPROBE_MARGIN, 1.0)
     ids, d = ix.search_batch(held, 10)
     r_learned = rec(ids)
     pred = ix.predict_nprobe(held)
-    mean_probes = float(np.maximum(pred, 4).mean())
+    mean_probes = float(pred.mean())
     # the gain: fewer probes than the smallest fixed nprobe reaching the same
     # recall, or more recall than fixed search at the same average probes
     need = min([p for p, r in fixed.items() if r >= r_learned - 1e-9] or [64])
@@ -80,11 +89,66 @@ def test_learned_nprobe_trains_and_gains(hora, oracle, gpu):
     w = 0.0 if hi == lo else (np.log2(m) - np.log2(lo)) / (np.log2(hi) - np.log2(lo))
     fixed_at_same_cost = fixed[lo] + w * (fixed[hi] - fixed[lo])
     print("fixed", fixed, "learned", r_learned, "mean probes", mean_probes, "fixed needs", need,
-          "fixed at the same cost", fixed_at_same_cost)
-    assert r_learned >= 0.95
+          "fixed at the same cost", fixed_at_same_cost, "model", model)
+    # calibrated on other queries of the same law: the target within sampling error
+    assert r_learned >= 0.94
     assert mean_probes < need or r_learned > fixed_at_same_cost + 0.002, \
         (mean_probes, need, fixed, r_learned)
     # features are finite and the model's nprobe respects the clamp
     F = ix.nprobe_features(held[:64])
     assert F.shape == (64, 40) and np.isfinite(F).all()
     assert pred.min() >= 1 and pred.max() <= 64
+
+
+def test_learned_nprobe_beats_best_fixed_on_mixture_index(hora, gpu):
+    """The configuration's learned-nprobe setting on a reduced index of the
+    same shape and generator (Gaussian-mixture rows, 32 x 8-bit PQ, about a
+    thousand rows per list, exact rerank of 100): labels at recall 0.95,
+    margin calibrated on held-out training queries, features from the coarse
+    distances alone (no phase-1 probes).  On other held-out queries it must
+    reach recall@10 >= 0.95 with fewer lists and less time than the fastest
+    fixed nprobe that reaches 0.95."""
+    import json
+
+    import torch
+    from hora_gb300 import synth
+    n, d, lists = 256_000, 128, 256
+    X = synth.mixture(n, d, 1024, stream=61)
+    ix = hora.IVFPQIndex(d, hora.IVFPQParams(n_sub=32, sub_bits=8, n_kmeans_center=lists,
+                                             search_n_center=2, train_epoch=10))
+    ix.set_option(hora.Option.TRAIN_SIZE, 128_000)
+    ix.madd(torch.from_numpy(X).cuda(), None)
+    ix.build(hora.Metric.Euclidean)
+    ix.set_option(hora.Option.IVF_RERANK, 100)
+    ix.set_option(hora.Option.NPROBE_PHASE1, 0)
+    ix.train_nprobe(synth.mixture(40_000, d, 1024, stream=62), max_nprobe=64, recall_target=0.95,
+                    epochs=20)
+    held = synth.mixture(8_000, d, 1024, stream=63)
+    bfi = hora.BruteForceIndex(d)
+    bfi.madd(torch.from_numpy(X).cuda(), None)
+    bfi.build(hora.Metric.Euclidean)
+    exact, _ = bfi.search_batch(held, 10)
+    dq = torch.from_numpy(held).cuda()
+    ids_d = torch.empty((held.shape[0], 10), dtype=torch.int64, device="cuda")
+    dist_d = torch.empty((held.shape[0], 10), dtype=torch.float32, device="cuda")
+
+    def run(nprobe=0, reps=7):
+        ms = []
+        for _ in range(reps):
+            ix.search_batch(dq, 10, nprobe=nprobe, ids_out=ids_d, dist_out=dist_d)
+            ms.append(json.loads(ix.idx_info())["last_search_ms"])
+        ids = ids_d.cpu().numpy()
+        rec = np.mean([len(set(a.tolist()) & set(b.tolist())) / 10 for a, b in zip(ids, exact)])
+        return rec, float(np.median(ms[1:]))
+
+    fixed = {p: run(p) for p in (1, 2, 4, 8)}
+    ok = [p for p, (r, _) in fixed.items() if r >= 0.95]
+    assert ok, fixed
+    best = min(ok, key=lambda p: fixed[p][1])
+    ix.set_option(hora.Option.LEARNED_NPROBE, 1)
+    r_l, ms_l = run()
+    mean_probes = float(ix.predict_nprobe(held).mean())
+    print("fixed", fixed, "learned", r_l, ms_l, "mean probes", mean_probes)
+    assert r_l >= 0.95
+    assert mean_probes < best
+    assert ms_l < fixed[best][1], (ms_l, fixed)
