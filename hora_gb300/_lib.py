@@ -90,6 +90,8 @@ SIGNATURES = {
     "hora_server_submit": (C.c_int, [vp, C.c_uint32, vp, u64, u64, vp, vp, u64p]),
     "hora_server_wait": (C.c_int, [vp, u64, C.c_int64, f64p]),
     "hora_server_stats": (C.c_int, [vp, f64p]),
+    "hora_server_request_bytes": (C.c_int, [vp, C.c_uint32, u64, u64, u64p]),
+    "hora_server_info": (C.c_int, [vp, C.c_char_p, u64]),
     "hora_bf_search_noalloc": (C.c_int, [vp, u64, u64, vp, u64, u64, C.c_int, vp, vp, vp]),
 }
 

@@ -141,7 +141,7 @@ int stage_queries(hora_index *h, const float *queries, int64_t nq, SearchWorkspa
                                     cudaMemcpyHostToDevice, s));
   float *qn = nullptr;
   double *qsq = nullptr;
-  if (h->metric == M_COS || h->precision != HORA_PREC_FP32) {
+  if (h->metric == M_COS || h->precision != HORA_PREC_FP32 || exact_tc_eligible(h, 1)) {
     HORA_TRY(ws.qnorm.reserve(sizeof(float) * nq + sizeof(double) * nq + 16));
     qn = ws.qnorm.as<float>();
     qsq = reinterpret_cast<double *>(ws.qnorm.as<char>() + round_up(sizeof(float) * nq, 16));
@@ -171,8 +171,10 @@ int stage_queries(hora_index *h, const float *queries, int64_t nq, SearchWorkspa
 
 int bf_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
                    cudaStream_t s) {
-  if (h->metric == M_COS || h->precision != HORA_PREC_FP32) HORA_TRY(ensure_norms(h, s));
+  const bool xtc = exact_tc_eligible(h, k);
+  if (h->metric == M_COS || h->precision != HORA_PREC_FP32 || xtc) HORA_TRY(ensure_norms(h, s));
   if (h->precision != HORA_PREC_FP32) return lowp_search_keys(h, nq, k, ws, d_best, s);
+  if (xtc) return exact_tc_search_keys(h, nq, k, ws, d_best, s);
   int retries = 0;
   HORA_TRY(bf_topk_exact(base_view(h), h->metric, ws.q.as<float>(), ws.qnorm.as<float>(), nq, k,
                          h->cand_cap, ws, d_best, s, &retries));
@@ -187,6 +189,10 @@ int prepare_for_concurrent_search(hora_index *h) {
   if (h->metric == M_COS || h->precision != HORA_PREC_FP32) HORA_TRY(ensure_norms(h, s));
   if (h->kind == HORA_INDEX_BRUTE_FORCE && h->precision != HORA_PREC_FP32 && h->metric != M_L1)
     HORA_TRY(lowp_prepare(h, s));
+  if (h->kind == HORA_INDEX_BRUTE_FORCE && exact_tc_eligible(h, 1)) {
+    HORA_TRY(ensure_norms(h, s));
+    HORA_TRY(exact_tc_prepare(h, s));
+  }
   HORA_CUDA_TRY(cudaStreamSynchronize(s));
   return HORA_OK;
 }
@@ -562,6 +568,7 @@ int hora_idx_info(const hora_index *h, char *buf, uint64_t cap) {
   s += ",\"last_search_ms\":" + std::to_string(h->last_ms.load());
   s += ",\"last_overflow_rescans\":" + std::to_string(h->last_retries.load());
   s += ",\"last_threshold_probe\":" + std::to_string(h->last_probe.load());
+  s += ",\"last_fallback_queries\":" + std::to_string(h->last_fallback.load());
   if (h->kind != HORA_INDEX_BRUTE_FORCE) {
     std::string iv;
     ivf_info(h, iv);
@@ -702,6 +709,7 @@ int hora_set_option(hora_index *h, int key, double v) {
       h->ivf_rerank = (int)v;
       return HORA_OK;
     case HORA_OPT_BF_PROBE: h->bf_probe = v != 0; return HORA_OK;
+    case HORA_OPT_EXACT_TC: h->exact_tc = v != 0; return HORA_OK;
   }
   return fail(HORA_EINVAL, "unknown option");
 }
@@ -721,6 +729,7 @@ int hora_get_option(const hora_index *h, int key, double *out) {
     case HORA_OPT_IVF_RERANK: *out = h->ivf_rerank; return HORA_OK;
     case HORA_OPT_NPROBE_PHASE1: *out = h->nprobe_phase1; return HORA_OK;
     case HORA_OPT_BF_PROBE: *out = h->bf_probe; return HORA_OK;
+    case HORA_OPT_EXACT_TC: *out = h->exact_tc; return HORA_OK;
   }
   return fail(HORA_EINVAL, "unknown option");
 }

@@ -223,10 +223,12 @@ int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint
 // conflict-free column reads); each lane then sums its own row from the tile
 // in dimension order.
 constexpr int kRrMaxWarps = 8, kRrSlab = 64;
+// With count, query q's list holds min(count[q], R) keys (the rest of its R
+// slots are neither read nor written); in and outk may be the same buffer.
 template <int MT>
 __global__ void __launch_bounds__(kRrMaxWarps * 32) rerank_exact_kernel(
     const float *Q, int64_t ld, const float *X, int64_t dim, const float *qnorm, const float *xnorm,
-    const uint64_t *in, int R, uint64_t *outk) {
+    const uint64_t *in, int R, const uint32_t *count, uint64_t *outk) {
   extern __shared__ float rr_smem[];  // per warp a 32 x (kRrSlab + 1) tile, then the query row
   const int nw = blockDim.x >> 5;
   float *qs = rr_smem + nw * 32 * (kRrSlab + 1);
@@ -237,9 +239,10 @@ __global__ void __launch_bounds__(kRrMaxWarps * 32) rerank_exact_kernel(
   const int64_t n4 = (dim + 3) / 4;  // the zero-padded columns up to 4*n4 add exact zeros
   float(*tw)[kRrSlab + 1] = reinterpret_cast<float(*)[kRrSlab + 1]>(rr_smem + warp * 32 * (kRrSlab + 1));
   const int half = lane >> 4, c4 = lane & 15;
-  for (int r0 = warp * 32; r0 < R; r0 += nw * 32) {
+  const int Rq = count ? (int)min(count[q], (uint32_t)R) : R;
+  for (int r0 = warp * 32; r0 < Rq; r0 += nw * 32) {
     const int r = r0 + lane;
-    const uint64_t key = r < R ? in[q * R + r] : kEmptyKey;
+    const uint64_t key = r < Rq ? in[q * R + r] : kEmptyKey;
     float s = 0.0f;
     for (int64_t d0 = 0; d0 < 4 * n4; d0 += kRrSlab) {
       const int w = (int)(4 * n4 - d0 < kRrSlab ? 4 * n4 - d0 : kRrSlab);  // multiple of 4
@@ -270,7 +273,7 @@ __global__ void __launch_bounds__(kRrMaxWarps * 32) rerank_exact_kernel(
       for (int t = 0; t < w; ++t) s = dist_op<OP>(s, qs[d0 + t], tw[lane][t]);
       __syncwarp();
     }
-    if (r < R) {
+    if (r < Rq) {
       if (key == kEmptyKey) {
         outk[q * R + r] = kEmptyKey;
       } else {
@@ -284,12 +287,12 @@ __global__ void __launch_bounds__(kRrMaxWarps * 32) rerank_exact_kernel(
 
 int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, int64_t dim,
                         const float *qnorm, const float *xnorm, const uint64_t *in, int64_t nq,
-                        int R, uint64_t *out, cudaStream_t s) {
+                        int R, uint64_t *out, cudaStream_t s, const uint32_t *count) {
   if (nq <= 0) return HORA_OK;
   if (ld % 4) return fail(HORA_EINVAL, "rerank: pitch not a multiple of 4");
   ProfScope ps("rerank_exact", s);
   unsigned g = (unsigned)nq;
-  const int nw = std::max(1, std::min(kRrMaxWarps, (R + 31) / 32));
+  const int nw = count ? kRrMaxWarps : std::max(1, std::min(kRrMaxWarps, (R + 31) / 32));
   const int T = nw * 32;
   // the warps' tiles and the query row in dynamic shared memory
   const size_t qb = sizeof(float) * ((size_t)nw * 32 * (kRrSlab + 1) + (size_t)ld);
@@ -299,10 +302,10 @@ int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, 
   HORA_SMEM_ATTR(rerank_exact_kernel<M_IP>, qb);
   HORA_SMEM_ATTR(rerank_exact_kernel<M_COS>, qb);
   switch (metric) {
-    case M_L2: rerank_exact_kernel<M_L2><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
-    case M_L1: rerank_exact_kernel<M_L1><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
-    case M_IP: rerank_exact_kernel<M_IP><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
-    case M_COS: rerank_exact_kernel<M_COS><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, out); break;
+    case M_L2: rerank_exact_kernel<M_L2><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, out); break;
+    case M_L1: rerank_exact_kernel<M_L1><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, out); break;
+    case M_IP: rerank_exact_kernel<M_IP><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, out); break;
+    case M_COS: rerank_exact_kernel<M_COS><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, out); break;
     default: return fail(HORA_EMETRIC, "unknown method");
   }
   HORA_LAUNCHED();

@@ -78,6 +78,9 @@ struct LowpState {
   DevBuf cmem;     // n uint32 member rows, cluster after cluster, ascending
   DevBuf xsqmax;   // 1 f32: the largest squared row norm
   DevBuf ctiles;   // the pivots' BF16 tile image (same layout as tiles)
+  // BF16 Euclidean: the largest |x - bf16(x)| over the rows (1 f32, rounded
+  // up), the rows' share of the certified exact search's error bound
+  DevBuf dxmax;
 };
 
 void lowp_state_free(LowpState *p) { delete p; }
@@ -592,6 +595,23 @@ __global__ void norm_block_kernel(const double *sq, int64_t n, __nv_bfloat16 *ou
   for (int i = 3; i < 16; ++i) o[i] = __float2bfloat16_rn(0.0f);
 }
 
+// The largest Euclidean norm of x - bf16(x) over the rows (one warp per row,
+// f64 sums, rounded up to the next f32) into *out as ordered bits.
+__global__ void bf16_residual_max_kernel(const float *X, int64_t n, int64_t ld, int64_t dim, unsigned *out) {
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  double acc = 0.0;
+  for (int64_t t = lane; t < dim; t += 32) {
+    const float x = X[r * ld + t];
+    const double e = (double)x - (double)__bfloat162float(__float2bfloat16_rn(x));
+    acc += e * e;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) atomicMax(out, __float_as_uint(nextafterf((float)sqrt(acc), INFINITY)));
+}
+
 // one warp per row: per-row absmax scale so the row's largest entry maps to 448
 __global__ void to_e4m3_kernel(const float *X, int64_t n, int64_t ld, int64_t dim, int64_t Dp,
                                uint8_t *out, float *scale) {
@@ -795,7 +815,8 @@ __global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, i
 // differ by less than 3.5e-5 of it.  A cluster with fewer than R members
 // gives -FLT_MAX: the scan keeps nothing and the query is rescheduled.
 __global__ void probe_select_kernel(const uint64_t *pkeys, const int64_t *coff, const float *pdist,
-                                    const float *qsq, const float *xsqmax, int64_t nq, int R, float *tau) {
+                                    const float *qsq, const float *xsqmax, int64_t nq, int R,
+                                    const float *slack, float *tau) {
   const int64_t q = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (q >= nq) return;
@@ -825,7 +846,13 @@ __global__ void probe_select_kernel(const uint64_t *pkeys, const int64_t *coff, 
     for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     if (cnt < R) a = tt;
   }
-  if (lane == 0) tau[q] = ord2f(a | ((1u << kSelectSkip) - 1)) + 1e-4f * (qsq[q] + *xsqmax);
+  if (lane == 0) {
+    float t = ord2f(a | ((1u << kSelectSkip) - 1)) + 1e-4f * (qsq[q] + *xsqmax);
+    // the certified exact search widens it by its error bound (and by a
+    // relative 2^-20 against the rounding of these f32 additions)
+    if (slack) t = t + slack[q] + 0x1p-20f * fabsf(t + slack[q]);
+    tau[q] = t;
+  }
 }
 
 // Probe work items: pivot c owns ceil(queries / kProbeQ) of them, from
@@ -1048,6 +1075,11 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
         HORA_TRY(normblk.reserve(std::max<int64_t>(h->n, 1) * 16 * 2));
         norm_block_kernel<<<ceil_div(h->n, 256), 256, 0, s>>>(h->xsq64.as<double>(), h->n,
                                                               normblk.as<__nv_bfloat16>());
+        HORA_LAUNCHED();
+        HORA_TRY(st->dxmax.reserve(sizeof(float)));
+        HORA_CUDA_TRY(cudaMemsetAsync(st->dxmax.ptr, 0, sizeof(float), s));
+        bf16_residual_max_kernel<<<ceil_div(h->n, 8), 256, 0, s>>>(h->base.as<float>(), h->n, h->ld, h->dim,
+                                                                   st->dxmax.as<unsigned>());
       }
     } else {
       HORA_TRY(st->xscale.reserve(sizeof(float) * std::max<int64_t>(h->n, 1)));
@@ -1186,7 +1218,8 @@ static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
 // tensor map ta, ws.lqsq) into ws.ptau.  lp carries the search's scan
 // parameters; its candidate lists take the pivot scores (C <= cap).
 static int probe_thresholds(hora_index *h, LowpState &L, int64_t nq, int R, int64_t Dp, SearchWorkspace &ws,
-                            const CUtensorMap &ta, const LpParams &lp, cudaStream_t s) {
+                            const CUtensorMap &ta, const LpParams &lp, cudaStream_t s,
+                            const float *slack = nullptr) {
   const int C = L.pc;
   // sized for a power of two of at least 1,024 queries: a serving slot whose
   // batches vary reallocates (and with that waits for the device) rarely
@@ -1225,7 +1258,7 @@ static int probe_thresholds(hora_index *h, LowpState &L, int64_t nq, int R, int6
   ProfScope ps("probe_select", s);
   probe_select_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(
       ws.pkeys.as<uint64_t>(), L.coff.as<int64_t>(), ws.pdist.as<float>(), ws.lqsq.as<float>(),
-      L.xsqmax.as<float>(), nq, R, ws.ptau.as<float>());
+      L.xsqmax.as<float>(), nq, R, slack, ws.ptau.as<float>());
   HORA_LAUNCHED();
   return HORA_OK;
 }
@@ -1236,6 +1269,15 @@ int lowp_prepare(hora_index *h, cudaStream_t s) {
   HORA_TRY(ensure_lowp(h, h->precision, s));
   if (probe_eligible(h)) HORA_TRY(ensure_pivots(h, *h->lowp, s));
   return HORA_OK;
+}
+
+int lowp_rerank_width(const hora_index *h, int k) {
+  const int64_t kbe = h->precision == HORA_PREC_BF16 ? 64 : 128;
+  if (h->metric == M_L1 || round_up((int64_t)h->dim, kbe) / kbe > 2) return 0;  // the exact path answers
+  int R = h->rerank > 0 ? h->rerank
+                        : (h->precision == HORA_PREC_BF16 ? std::max(2 * k, k + 64) : std::max(4 * k, k + 128));
+  R = std::max(R, k);
+  return (int)std::min<int64_t>(R, std::max<int64_t>(h->n, k));
 }
 
 int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
@@ -1255,9 +1297,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   }
   HORA_TRY(ensure_lowp(h, prec, s));
   LowpState &L = *h->lowp;
-  int R = h->rerank > 0 ? h->rerank : (prec == HORA_PREC_BF16 ? std::max(2 * k, k + 64) : std::max(4 * k, k + 128));
-  R = std::max(R, k);
-  R = (int)std::min<int64_t>(R, std::max<int64_t>(h->n, k));
+  const int R = lowp_rerank_width(h, k);
   if (R > 4096) return fail(HORA_ECAP, "rerank width must be <= 4096");
   int cap = std::max(h->cand_cap, 2 * R);
   cap = (int)round_up(cap, 128);
@@ -1460,6 +1500,195 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   }
   h->last_retries = rounds;
   if (redo) HORA_TRY(finish());
+  return HORA_OK;
+}
+
+// ---- exact search certified on the tensor cores ------------------------------------
+// Exact FP32 Euclidean search (the reference's result, distances bit for
+// bit) on at least kProbeMinRows rows with the BF16 scan as a certified
+// filter.  For every row x and query q the scan's value s(q, x) = |q|^2 -
+// 2 (<q~, x~> - |x|^2 / 2) and the reference's sequential f32 sum r(q, x)
+// differ by at most eps(q):
+//   <q~, x~> - <q, x> = <q~, x~ - x> + <q~ - q, x>, so by Cauchy-Schwarz
+//   |.| <= |q~| max|x - x~| + |q - q~| max|x|               (term A)
+//   the tensor core's FP32 accumulation of Dp + 16 exact products,
+//   bounded generously by (Dp + 16) 2^-22 (|q~| max|x~| + max|x|^2 / 2)  (B)
+//   the f32 roundings of |x|^2 / 2, |q|^2 and the final FMA            (C)
+//   the reference's own f32 sum, (dim + 4) 2^-23 (|q| + max|x|)^2     (E)
+//   eps = 2 A + 2 B + C + E.
+// The probe (probe_dist_kernel, same products, another f32 order, within
+// delta = 1e-4 (|q|^2 + max|x|^2) of the scan) puts a query's k-th smallest
+// probe value t among its pivot cluster's members.  k rows then have r <= t
+// + delta + eps, so the exact k-th distance is at most that, and every row
+// of the exact top k has s <= t + delta + 2 eps: the filter pass from that
+// threshold keeps them all.  The kept rows are rescored exactly (reference
+// op order) and the k best returned.  A query whose cluster has fewer than k
+// members, or whose kept rows overflow the candidate capacity, is answered
+// by the CUDA-core exact scan instead; either way the result is exact.
+
+// 2 eps(q) per query (rounded up), from the staged f32 query rows.
+__global__ void exact_tc_slack_kernel(const float *Q, int64_t nq, int64_t ld, int64_t dim, int64_t Dp,
+                                      const double *qsq64, const float *dxmax, const float *xsqmax,
+                                      float *slack) {
+  const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  double sb = 0.0, sd = 0.0;
+  for (int64_t t = lane; t < dim; t += 32) {
+    const float x = Q[q * ld + t];
+    const double b = (double)__bfloat162float(__float2bfloat16_rn(x));
+    sb += b * b;
+    sd += ((double)x - b) * ((double)x - b);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    sb += __shfl_xor_sync(0xffffffffu, sb, o);
+    sd += __shfl_xor_sync(0xffffffffu, sd, o);
+  }
+  if (lane) return;
+  const double qb = sqrt(sb) * (1.0 + 0x1p-40), dq = sqrt(sd) * (1.0 + 0x1p-40);
+  const double qsq = qsq64[q], qn = sqrt(qsq);
+  const double xsq = (double)*xsqmax * (1.0 + 0x1p-22), xn = sqrt(xsq);
+  const double dx = (double)*dxmax;
+  const double xb = xn * (1.0 + 0x1p-8) + dx;  // |bf16(x)| <= |x| + |x - bf16(x)|
+  const double A = qb * dx + dq * xn;
+  const double B = (double)(Dp + 16) * 0x1p-22 * (qb * xb + 0.5 * xsq);
+  const double Cr = 0x1p-22 * (qsq + 2.0 * qb * xb + xsq);
+  const double E = (double)(dim + 4) * 0x1p-23 * (qn + xn) * (qn + xn);
+  const double eps = 2.0 * A + 2.0 * B + Cr + E;
+  slack[q] = nextafterf((float)(2.0 * eps * (1.0 + 0x1p-10)), INFINITY);
+}
+
+// Queries the certified pass cannot answer: fewer than k rows kept (no
+// valid probe) or more than the capacity (overflow).
+__global__ void exact_tc_fallback_kernel(const uint32_t *count, int64_t nq, int k, int cap, int *n, int *list) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq && (count[q] < (uint32_t)k || count[q] > (uint32_t)cap)) list[atomicAdd(n, 1)] = (int)q;
+}
+
+__global__ void gather_rows_f32_kernel(const float *src, int64_t ld, const int *list, int64_t nl, float *dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nl * ld) dst[i] = src[(int64_t)list[i / ld] * ld + (i % ld)];
+}
+
+__global__ void scatter_keys_kernel(const uint64_t *src, int k, const int *list, int64_t nl, uint64_t *dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nl * k) dst[(int64_t)list[i / k] * k + (i % k)] = src[i];
+}
+
+bool exact_tc_eligible(const hora_index *h, int k) {
+  return h->exact_tc && h->precision == HORA_PREC_FP32 && h->metric == M_L2 && h->n >= kProbeMinRows &&
+         round_up((int64_t)h->dim, 64) / 64 <= 2 && k <= kProbeMaxR &&
+         probe_pivot_count(h->n) <= (int)round_up(std::max(h->cand_cap, 2 * k), 128);
+}
+
+int exact_tc_prepare(hora_index *h, cudaStream_t s) {
+  HORA_TRY(ensure_lowp(h, HORA_PREC_BF16, s));
+  return ensure_pivots(h, *h->lowp, s);
+}
+
+int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
+                         cudaStream_t s) {
+  const int64_t Dp = round_up((int64_t)h->dim, 64);
+  const int nkb = (int)(Dp / 64);
+  HORA_TRY(ensure_lowp(h, HORA_PREC_BF16, s));
+  LowpState &L = *h->lowp;
+  HORA_TRY(ensure_pivots(h, L, s));
+  const int cap = (int)round_up(std::max(h->cand_cap, 2 * k), 128);
+  const int stages = lp_stages(nkb, true);
+  // BF16 queries, their f32 squared norms and the certified slack
+  HORA_TRY(ws.lq.reserve(std::max<int64_t>(nq, 1) * Dp * 2));
+  HORA_TRY(ws.lerr.reserve(16));
+  HORA_TRY(ws.lqsq.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
+  HORA_TRY(ws.xslack.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
+  const double *qsq64 = reinterpret_cast<const double *>(ws.qnorm.as<char>() + round_up(sizeof(float) * nq, 16));
+  {
+    ProfScope ps("lowp_convert", s);
+    to_bf16_kernel<<<ceil_div(nq * Dp, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, nullptr,
+                                                          ws.lq.as<__nv_bfloat16>());
+    HORA_LAUNCHED();
+    f64_to_f32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(qsq64, nq, ws.lqsq.as<float>());
+    HORA_LAUNCHED();
+    exact_tc_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, qsq64,
+                                                          L.dxmax.as<float>(), L.xsqmax.as<float>(),
+                                                          ws.xslack.as<float>());
+    HORA_LAUNCHED();
+  }
+  CUtensorMap ta;
+  HORA_TRY(make_tmap(&ta, ws.lq.ptr, HORA_PREC_BF16, Dp, nq, kLpBM));
+  HORA_TRY(ws.xempty.reserve(sizeof(uint64_t) * std::max<int64_t>(nq, 1)));
+  HORA_TRY(ws.cand.reserve(sizeof(uint64_t) * nq * cap));
+  HORA_TRY(ws.count.reserve(sizeof(uint32_t) * nq));
+  HORA_TRY(ws.ovf_flag.reserve(nq));
+  HORA_TRY(ws.ovf_counter.reserve(sizeof(uint32_t)));
+  HORA_TRY(ws.xlist.reserve(sizeof(int) * std::max<int64_t>(nq, 1)));
+  uint32_t *count = ws.count.as<uint32_t>();
+  uint8_t *flags = ws.ovf_flag.as<uint8_t>();
+  uint32_t *ovc = ws.ovf_counter.as<uint32_t>();
+  int *lerr = ws.lerr.as<int>();  // [0] a pipeline wait timed out, [1] fallback queries
+  HORA_CUDA_TRY(cudaMemsetAsync(ws.xempty.ptr, 0xff, sizeof(uint64_t) * nq, s));
+  HORA_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t) * nq, s));
+  HORA_CUDA_TRY(cudaMemsetAsync(flags, 0, nq, s));
+  HORA_CUDA_TRY(cudaMemsetAsync(ovc, 0, sizeof(uint32_t), s));
+  HORA_CUDA_TRY(cudaMemsetAsync(ws.lerr.ptr, 0, 16, s));
+  LpParams p{};
+  p.nq = nq;
+  p.nkb = nkb;
+  p.stages = stages;
+  p.xsq = L.xsq.as<float>();
+  p.xnorm = h->xnorm.as<float>();
+  p.qsq = ws.lqsq.as<float>();
+  p.qnorm = ws.qnorm.as<float>();
+  p.best = ws.xempty.as<uint64_t>();  // no list: the probed threshold alone decides
+  p.k = 1;
+  p.cand = ws.cand.as<uint64_t>();
+  p.cap = cap;
+  p.count = count;
+  p.err = lerr;
+  HORA_TRY(probe_thresholds(h, L, nq, k, Dp, ws, ta, p, s, ws.xslack.as<float>()));
+  p.tau0 = ws.ptau.as<float>();
+  const int64_t n = h->n;
+  const int64_t max_chunk = (int64_t)60000 * kLpBN * kLpMinTilesPerCta;
+  for (int64_t lo = 0; lo < n; lo += max_chunk) {
+    p.r_begin = lo;
+    p.r_end = std::min<int64_t>(n, lo + max_chunk);
+    p.tpc = lp_tiles_per_cta(nq, p.r_end - p.r_begin);
+    HORA_TRY(launch_lp(HORA_PREC_BF16, M_L2, TILE_FILTER, ta, L, p, s));
+  }
+  // the queries the pass cannot answer (read before the merge, which
+  // consumes the counts), every kept row rescored exactly, then the k best
+  exact_tc_fallback_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(count, nq, k, cap, lerr + 1,
+                                                                     ws.xlist.as<int>());
+  HORA_LAUNCHED();
+  HORA_TRY(launch_rerank_exact(M_L2, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim, nullptr, nullptr,
+                               p.cand, nq, cap, p.cand, s, count));
+  HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
+  HORA_TRY(launch_merge_topk(d_best, k, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s));
+  int hs[2] = {0, 0};
+  HORA_CUDA_TRY(cudaMemcpyAsync(hs, lerr, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hs[0]) return fail(HORA_ETIMEDOUT, "tensor-core scan: a pipeline wait timed out");
+  h->last_probe = 1;
+  h->last_retries = 0;
+  h->last_fallback = hs[1];
+  if (hs[1] > 0) {
+    // the queries the certified pass could not answer: the CUDA-core scan
+    h->last_probe = 2;
+    const int64_t nl = hs[1];
+    HORA_TRY(ws.xq.reserve(sizeof(float) * nl * h->ld));
+    HORA_TRY(ws.xkeys.reserve(sizeof(uint64_t) * nl * k));
+    gather_rows_f32_kernel<<<ceil_div(nl * (int64_t)h->ld, 256), 256, 0, s>>>(ws.q.as<float>(), h->ld,
+                                                                             ws.xlist.as<int>(), nl,
+                                                                             ws.xq.as<float>());
+    HORA_LAUNCHED();
+    int retries = 0;
+    HORA_TRY(bf_topk_exact(base_view(h), M_L2, ws.xq.as<float>(), nullptr, nl, k, h->cand_cap, ws,
+                           ws.xkeys.as<uint64_t>(), s, &retries));
+    scatter_keys_kernel<<<ceil_div(nl * (int64_t)k, 256), 256, 0, s>>>(ws.xkeys.as<uint64_t>(), k,
+                                                                      ws.xlist.as<int>(), nl, d_best);
+    HORA_LAUNCHED();
+    h->last_retries = retries;
+  }
   return HORA_OK;
 }
 

@@ -48,6 +48,7 @@ struct hora_index {
   int ivf_rerank = 0;
   int nprobe_phase1 = 4;
   int bf_probe = 1;
+  int exact_tc = 1;
 
   cudaStream_t stream = nullptr;
   std::mutex mu;
@@ -59,6 +60,8 @@ struct hora_index {
   std::atomic<int> last_retries{0};
   // BF16 starting-threshold probe: 0 not used, 1 answered, 2 fell back to the chunked schedule
   std::atomic<int> last_probe{0};
+  // certified exact search: queries the last search handed to the CUDA-core scan
+  std::atomic<int64_t> last_fallback{0};
   std::atomic<double> last_ms{0.0};
 };
 
@@ -88,6 +91,16 @@ int bf_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64
 int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
                      cudaStream_t s);
 int lowp_prepare(hora_index *h, cudaStream_t s);
+// Candidates a low-precision search keeps for its exact rerank (0 when the
+// exact path answers: Manhattan, or dimensions beyond the resident tile).
+int lowp_rerank_width(const hora_index *h, int k);
+// Exact FP32 Euclidean search with the BF16 tensor-core scan as a certified
+// filter (bf_lowp.cu): whether it answers a k-NN search on this index, its
+// lazily built state, the search itself.
+bool exact_tc_eligible(const hora_index *h, int k);
+int exact_tc_prepare(hora_index *h, cudaStream_t s);
+int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
+                         cudaStream_t s);
 
 // IVF-PQ (ivfpq.cu)
 int ivf_build(hora_index *h);

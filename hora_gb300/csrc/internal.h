@@ -50,10 +50,11 @@ int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint
                         cudaStream_t s);
 
 // Exact FP32 distances (reference op order) for R candidate rows per query:
-// in = approximate keys (row in the low word), out = exact keys.
+// in = approximate keys (row in the low word), out = exact keys.  With
+// count, query q has min(count[q], R) keys in its R slots (in may be out).
 int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, int64_t dim,
                         const float *qnorm, const float *xnorm, const uint64_t *in, int64_t nq,
-                        int R, uint64_t *out, cudaStream_t s);
+                        int R, uint64_t *out, cudaStream_t s, const uint32_t *count = nullptr);
 
 // ---- selection (topk.cu) ------------------------------------------------------
 // Merges each query's candidates into its sorted k-best key list (dedup by
@@ -91,12 +92,27 @@ struct SearchWorkspace {
   DevBuf pkeys, poff, pmem, pblk, pcnt, pdist, ptau;
   // learned nprobe
   DevBuf feats, pred, npq;
+  // certified tensor-core exact search: per-query threshold slack, one empty
+  // key per query, the queries answered by the CUDA-core scan instead (list,
+  // their rows, their keys)
+  DevBuf xslack, xempty, xlist, xq, xkeys;
   std::vector<uint8_t> h_flags;
   // the finiteness flag of the staged queries, read before the results are written
   DevBuf d_status;
   HostBuf h_status;
   EventBox ev_status;
   bool status_pending = false;
+  // device bytes the workspace holds (its buffers only grow)
+  size_t device_bytes() const {
+    const DevBuf *all[] = {&q, &qnorm, &best, &cand, &count, &ovf_flag, &ovf_counter, &qlist, &out_ids,
+                           &out_dist, &rows, &keys2, &tmp, &coarse, &probes, &pair_cnt, &pair_off, &pair_q,
+                           &pair_c, &pair_slot, &ivf_cand, &best_r, &tmp_keys, &adc_next, &adc_gmap, &lq,
+                           &lqsq, &lqscale, &lqgather, &lerr, &pkeys, &poff, &pmem, &pblk, &pcnt, &pdist,
+                           &ptau, &feats, &pred, &npq, &xslack, &xempty, &xlist, &xq, &xkeys, &d_status};
+    size_t b = 0;
+    for (const DevBuf *d : all) b += d->bytes;
+    return b;
+  }
   // the search's own start / end events (timed), created once per workspace
   EventBox ev_t0, ev_t1;
 };

@@ -5,9 +5,12 @@
 // from any thread.  Each of n_slots workers owns a CUDA stream and a search
 // workspace.  A free worker takes the oldest request whose working-set bytes
 // fit under the HBM budget next to the requests already in flight, and folds
-// in every further queued request for the same index and k (up to 8,192
-// queries per batch) that still fits, so requests arriving while others run
-// join the next batch on the next free slot.  Work on different slots
+// in every further queued request for the same index whose k gives the same
+// candidate width (search_width: any k on the exact paths; every k up to the
+// rerank width on the approximate ones) and that still fits (up to 8,192
+// queries per batch); the batch runs at its largest k and each request takes
+// its first k columns.  Requests arriving while others run join the next
+// batch on the next free slot.  Work on different slots
 // overlaps on the GPU.  Results are bit-identical to running each request
 // alone: every path is deterministic per query and a batch only concatenates
 // queries.  Latency is measured per request from submit to completion.
@@ -68,27 +71,50 @@ struct hora_server {
   std::vector<double> lat_ms;
   uint64_t completed = 0, completed_q = 0, rejected = 0, inflight = 0, max_inflight = 0;
   uint64_t max_admitted = 0;
+  uint64_t batches = 0, mixed_k_batches = 0;
 };
 
 namespace hora {
 
 constexpr uint64_t kMaxBatchQueries = 8192;
 
-// Device working set of one request: staged queries, k-best lists,
-// candidate buffers and outputs (an upper estimate of what its search
-// reserves in the slot's workspace).
+// Device working set of one request of nq queries (or of a batch at the
+// batch's largest k): staged queries and their copies, k-best and candidate
+// lists, outputs, and the per-search buffers with minimum sizes (the
+// probed threshold buffers are sized for at least 1,024 queries, the IVF
+// pair tables per list) — an upper estimate of what its search reserves in
+// the slot's workspace.
 static size_t request_bytes(const hora_index *h, uint64_t nq, uint64_t k) {
-  size_t per_q = h->ld * 4 + 16 + k * (8 + 8 + 4);
+  const size_t ld = h->ld, Dp = (size_t)round_up((int64_t)h->dim, 64) * 2;  // BF16 row, or 128 FP8 bytes
+  size_t per_q = ld * 4 * 2 + 64 + k * (8 + 8 + 8 + 12);  // queries (and a gathered copy), norms, keys, outputs
+  size_t fixed = 64 << 10;                                  // small buffers and 256-byte minimums
   if (h->kind == HORA_INDEX_BRUTE_FORCE) {
-    int R = (int)std::max<uint64_t>(k, h->rerank > 0 ? (uint64_t)h->rerank : 2 * k + 64);
-    per_q += (size_t)std::max<int>(h->cand_cap, 2 * R) * 8 + (size_t)R * 16 + h->ld * 2;
+    const int R = std::max<int>((int)k, lowp_rerank_width(h, (int)k));
+    const size_t cap = (size_t)round_up(std::max(h->cand_cap, 2 * R), 128);
+    per_q += Dp * 2 + cap * 8 + (size_t)R * 16 + 64;
+    const size_t C = 4096;                                  // pivots at most
+    const size_t nres = std::max<size_t>(1024, nq);         // probe buffers: a power of two >= 1,024
+    fixed += 2 * nres * (8 + 4 + 4 + 1024 * 4) + C * 64;
   } else {
-    int64_t pmax = std::max<int64_t>(32, std::max<int64_t>((int64_t)h->ivf.search_n_center, h->nprobe_max));
-    pmax = std::min<int64_t>(pmax, (int64_t)h->ivf.n_kmeans_center);
-    int R = std::max<int>((int)k, h->ivf_rerank);
-    per_q += (size_t)h->ivf.n_kmeans_center * 4 + (size_t)pmax * (8 + 12) + (size_t)pmax * R * 8 + (size_t)R * 16;
+    const size_t C = h->ivf.n_kmeans_center;
+    size_t pmax = std::max<size_t>(32, std::max<size_t>(h->ivf.search_n_center, (size_t)h->nprobe_max));
+    pmax = std::min(pmax, C);
+    const size_t R = std::max<size_t>(k, (size_t)h->ivf_rerank);
+    per_q += C * 4 + pmax * (8 + 12 + 4) + pmax * R * 8 + R * 16 + 40 * 4 + 16;
+    fixed += (C + 1) * 32 + C * 4;
   }
-  return per_q * nq;
+  return per_q * nq + fixed;
+}
+
+// The candidates a search of index h keeps before its final k best: 0 when
+// the k best are a prefix of any larger k's (every exact path, and IVF-PQ
+// without a rerank, whose per-list k best contain the global k best).  Two
+// requests with the same width run as one batch at the larger k, each
+// taking the first k of its rows: the same result as alone.
+static int64_t search_width(const hora_index *h, uint64_t k) {
+  if (h->kind == HORA_INDEX_BRUTE_FORCE) return h->precision == HORA_PREC_FP32 ? 0 : lowp_rerank_width(h, (int)k);
+  if (h->ivf_rerank <= 0) return 0;
+  return ivf_rerank_width(h, (int)k);
 }
 
 static int ensure_pinned(Slot &sl, size_t nq, size_t dim, size_t kk) {
@@ -126,28 +152,51 @@ static void worker(hora_server *sv, int slot_no) {
       sv->queue.pop_front();
       batch.push_back(head);
       sv->admitted += head->bytes;
-      uint64_t total = head->nq;
+      uint64_t total = head->nq, kmax = head->k;
+      const hora_index *hi = sv->idx[head->index_no];
+      const int64_t width = search_width(hi, head->k);
       for (auto it = sv->queue.begin(); it != sv->queue.end();) {
         Request *r = *it;
-        if (r->index_no == head->index_no && r->k == head->k && total + r->nq <= kMaxBatchQueries &&
-            sv->admitted + r->bytes <= sv->budget) {
-          batch.push_back(r);
-          sv->admitted += r->bytes;
-          total += r->nq;
-          it = sv->queue.erase(it);
-        } else {
+        if (r->index_no != head->index_no || search_width(hi, r->k) != width || total + r->nq > kMaxBatchQueries) {
           ++it;
+          continue;
         }
+        // the batch runs at its largest k: every member is charged at it
+        const uint64_t kn = std::max(kmax, r->k);
+        size_t extra = request_bytes(hi, r->nq, kn);
+        if (kn > kmax)
+          for (Request *m : batch) extra += request_bytes(hi, m->nq, kn) - m->bytes;
+        if (sv->admitted + extra > sv->budget) {
+          ++it;
+          continue;
+        }
+        if (kn > kmax)
+          for (Request *m : batch) m->bytes = request_bytes(hi, m->nq, kn);
+        r->bytes = request_bytes(hi, r->nq, kn);
+        sv->admitted += extra;
+        kmax = kn;
+        batch.push_back(r);
+        total += r->nq;
+        it = sv->queue.erase(it);
       }
+      sv->batches += 1;
+      for (Request *m : batch)
+        if (m->k != kmax) {
+          sv->mixed_k_batches += 1;
+          break;
+        }
       sv->inflight += batch.size();
       sv->max_inflight = std::max(sv->max_inflight, sv->inflight);
       sv->max_admitted = std::max(sv->max_admitted, sv->admitted);
     }
-    // run the batch
+    // run the batch at its largest k
     hora_index *h = sv->idx[batch[0]->index_no];
-    const uint64_t k = batch[0]->k, dim = h->dim;
-    uint64_t total = 0;
-    for (Request *r : batch) total += r->nq;
+    const uint64_t dim = h->dim;
+    uint64_t total = 0, k = 0;
+    for (Request *r : batch) {
+      total += r->nq;
+      k = std::max(k, r->k);
+    }
     int rc = ensure_pinned(sl, total, dim, k);
     std::string err;
     if (rc == HORA_OK) {
@@ -160,8 +209,11 @@ static void worker(hora_server *sv, int slot_no) {
       if (rc == HORA_OK) {
         off = 0;
         for (Request *r : batch) {
-          std::memcpy(r->ids, sl.h_ids + off * k, sizeof(uint64_t) * r->nq * k);
-          std::memcpy(r->dist, sl.h_dist + off * k, sizeof(float) * r->nq * k);
+          // each request's first r->k of the batch's k columns
+          for (uint64_t i = 0; i < r->nq; ++i) {
+            std::memcpy(r->ids + i * r->k, sl.h_ids + (off + i) * k, sizeof(uint64_t) * r->k);
+            std::memcpy(r->dist + i * r->k, sl.h_dist + (off + i) * k, sizeof(float) * r->k);
+          }
           off += r->nq;
         }
       }
@@ -294,6 +346,28 @@ int hora_server_wait(hora_server *sv, uint64_t ticket, int64_t timeout_ms, doubl
   sv->all.erase(it);
   delete r;
   return rc == HORA_OK ? HORA_OK : fail(rc, err);
+}
+
+int hora_server_request_bytes(hora_server *sv, uint32_t index_no, uint64_t nq, uint64_t k, uint64_t *out) {
+  if (!sv || !out) return fail(HORA_EINVAL, "null argument");
+  if (index_no >= sv->idx.size()) return fail(HORA_EINVAL, "index_no out of range");
+  *out = request_bytes(sv->idx[index_no], nq, k);
+  return HORA_OK;
+}
+
+int hora_server_info(hora_server *sv, char *buf, uint64_t cap) {
+  if (!sv || !buf || cap == 0) return fail(HORA_EINVAL, "null argument");
+  std::string s;
+  {
+    std::lock_guard<std::mutex> g(sv->mu);
+    s = "{\"batches\":" + std::to_string(sv->batches) + ",\"mixed_k_batches\":" +
+        std::to_string(sv->mixed_k_batches) + ",\"slot_workspace_bytes\":[";
+    for (size_t i = 0; i < sv->slots.size(); ++i)
+      s += (i ? "," : "") + std::to_string(sv->slots[i]->ws.device_bytes());
+    s += "]}";
+  }
+  std::snprintf(buf, cap, "%s", s.c_str());
+  return s.size() + 1 > cap ? fail(HORA_ECAP, "buffer too small") : HORA_OK;
 }
 
 int hora_server_stats(hora_server *sv, double *out) {

@@ -52,6 +52,7 @@ class Option(enum.IntEnum):
     IVF_RERANK = 10
     NPROBE_PHASE1 = 11
     BF_PROBE = 12
+    EXACT_TC = 13
 
 
 @dataclass
@@ -442,6 +443,17 @@ class Server:
         keys = ("completed", "queries", "p50_ms", "p99_ms", "max_inflight", "max_admitted_bytes",
                 "rejected")
         return dict(zip(keys, list(o)))
+
+    def request_bytes(self, index_no: int, nq: int, k: int) -> int:
+        out = C.c_uint64()
+        check(lib().hora_server_request_bytes(self._h, index_no, nq, k, C.byref(out)))
+        return out.value
+
+    def info(self) -> dict:
+        import json
+        buf = C.create_string_buffer(1 << 14)
+        check(lib().hora_server_info(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
 
     def close(self):
         if self._h:

@@ -125,10 +125,15 @@ typedef enum {
   HORA_OPT_NPROBE_PHASE1 = 11, /* learned nprobe: lists probed before the model
                                   reads its features (0..64, default 4; fixed at
                                   training) */
-  HORA_OPT_BF_PROBE = 12       /* BF16 Euclidean brute force on >= 65,536 rows:
+  HORA_OPT_BF_PROBE = 12,      /* BF16 Euclidean brute force on >= 65,536 rows:
                                   start each query's scan from a threshold probed
                                   in its nearest pivot cluster (default 1; 0 =
                                   chunked schedule only; same results either way) */
+  HORA_OPT_EXACT_TC = 13       /* exact FP32 Euclidean brute force on >= 65,536
+                                  rows, k <= 256: the BF16 tensor-core scan as a
+                                  filter certified by a rounding-error bound, then
+                                  every kept row rescored exactly (default 1; 0 =
+                                  the CUDA-core scan; same results either way) */
 } hora_option;
 
 typedef struct hora_index hora_index;
@@ -270,6 +275,13 @@ int hora_server_wait(hora_server *s, uint64_t ticket, int64_t timeout_ms, double
 /* Aggregate statistics: [completed requests, completed queries, p50 ms,
  * p99 ms, max in-flight requests, max admitted bytes, rejected]. */
 int hora_server_stats(hora_server *s, double *out7);
+/* The device bytes a request of nq queries at k is charged against the HBM
+ * budget (an upper estimate of what its search reserves in a slot). */
+int hora_server_request_bytes(hora_server *s, uint32_t index_no, uint64_t nq, uint64_t k,
+                              uint64_t *out);
+/* JSON diagnostics: batches run, batches that mixed different k, and the
+ * device bytes each slot's search workspace holds. */
+int hora_server_info(hora_server *s, char *buf, uint64_t cap);
 
 /* ---- brute force without device allocation ------------------------------- */
 /* No counterpart in the reference.  Exact brute-force k-NN for callers that

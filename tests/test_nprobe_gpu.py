@@ -102,8 +102,9 @@ def test_learned_nprobe_trains_and_gains(hora, oracle, gpu):
 
 def test_learned_nprobe_beats_best_fixed_on_mixture_index(hora, gpu):
     """The configuration's learned-nprobe setting on a reduced index of the
-    same shape and generator (Gaussian-mixture rows, 32 x 8-bit PQ, about a
-    thousand rows per list, exact rerank of 100): labels at recall 0.95,
+    same shape and generator (Gaussian-mixture rows, one list per mixture
+    centre, about a thousand rows per list, 32 x 8-bit PQ, exact rerank of
+    100): labels at recall 0.95,
     margin calibrated on held-out training queries, features from the coarse
     distances alone (no phase-1 probes).  On other held-out queries it must
     reach recall@10 >= 0.95 with fewer lists and less time than the fastest
@@ -113,7 +114,7 @@ def test_learned_nprobe_beats_best_fixed_on_mixture_index(hora, gpu):
     import torch
     from hora_gb300 import synth
     n, d, lists = 256_000, 128, 256
-    X = synth.mixture(n, d, 1024, stream=61)
+    X = synth.mixture(n, d, lists, stream=61)
     ix = hora.IVFPQIndex(d, hora.IVFPQParams(n_sub=32, sub_bits=8, n_kmeans_center=lists,
                                              search_n_center=2, train_epoch=10))
     ix.set_option(hora.Option.TRAIN_SIZE, 128_000)
@@ -121,9 +122,9 @@ def test_learned_nprobe_beats_best_fixed_on_mixture_index(hora, gpu):
     ix.build(hora.Metric.Euclidean)
     ix.set_option(hora.Option.IVF_RERANK, 100)
     ix.set_option(hora.Option.NPROBE_PHASE1, 0)
-    ix.train_nprobe(synth.mixture(40_000, d, 1024, stream=62), max_nprobe=64, recall_target=0.95,
+    ix.train_nprobe(synth.mixture(40_000, d, lists, stream=62), max_nprobe=64, recall_target=0.95,
                     epochs=20)
-    held = synth.mixture(8_000, d, 1024, stream=63)
+    held = synth.mixture(8_000, d, lists, stream=63)
     bfi = hora.BruteForceIndex(d)
     bfi.madd(torch.from_numpy(X).cuda(), None)
     bfi.build(hora.Metric.Euclidean)

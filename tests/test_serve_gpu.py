@@ -70,3 +70,34 @@ def test_budget_rejects_and_limits(hora, gpu):
     st = srv.stats()
     assert st["rejected"] == 1 and st["max_admitted_bytes"] <= 64 << 20
     srv.close()
+
+
+def test_mixed_k_batches_and_byte_estimate(hora, gpu):
+    """Requests of different k on one index share a batch when their search
+    keeps the same candidate width (here: exact brute force, and IVF-PQ with
+    a rerank of 128 >= every k); each one's result equals the request run
+    alone.  On fresh single-slot servers, the bytes a request is charged are
+    at least what its search actually reserved in the slot's workspace."""
+    from hora_gb300 import synth
+    X, idx = _indexes(hora)
+    srv = hora.Server(idx, n_slots=1, hbm_budget_bytes=4 << 30)
+    reqs = [(w, synth.mixture(int(nq), 64, 256, stream=2000 + i), int(k))
+            for i, (w, nq, k) in enumerate([(0, 7, 1), (0, 40, 100), (0, 3, 10), (1, 5, 10), (1, 64, 1),
+                                            (1, 9, 100), (0, 100, 10), (1, 33, 100)] * 4)]
+    tickets = [srv.submit(w, q, k) for w, q, k in reqs]
+    outs = [srv.wait(t) for t in tickets]
+    info = srv.info()
+    srv.close()
+    assert info["mixed_k_batches"] >= 1, info
+    for (w, q, k), (ids, dist, _) in zip(reqs, outs):
+        a_ids, a_d = idx[w].search_batch(q, k)
+        np.testing.assert_array_equal(ids, a_ids)
+        np.testing.assert_array_equal(dist, a_d)
+    for w in (0, 1):
+        for nq, k in ((1, 1), (256, 100), (2048, 10)):
+            s = hora.Server([idx[w]], n_slots=1, hbm_budget_bytes=16 << 30)
+            est = s.request_bytes(0, nq, k)
+            s.wait(s.submit(0, X[:nq], k))
+            used = s.info()["slot_workspace_bytes"][0]
+            s.close()
+            assert 0 < used <= est, (w, nq, k, used, est)
