@@ -42,7 +42,7 @@ def args_parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--forms", default="fp32,bf16,bf16r132,fp8",
+    ap.add_argument("--forms", default="fp32,bf16,bf16r132,fp8,fp8r132",
                     help="scoring forms: fp32, bf16, fp8, optionally with an explicit rerank "
                          "width (bf16r132 = BF16 scoring + exact rerank of 132 candidates)")
     ap.add_argument("--cpu-sample", type=int, default=0, help="queries in the CPU baseline sample")
@@ -156,9 +156,12 @@ class Clocks:
 
 # DRAM traffic of the BF16 scan in one step of the headline form (1M x 128,
 # 10k queries, R = 132: the pivot pass and the probed pass over the base),
-# from one ncu capture of dram__bytes_read.sum + dram__bytes_write.sum:
-# 295.1 MB read + 37.3 MB written.
-SCAN_TRAFFIC_BYTES_PER_STEP = 332.4e6
+# from an ncu capture of dram__bytes_read.sum + dram__bytes_write.sum of the
+# same kernel build (the command is in profiles/bf16_tc_scan_bf_1Mx128.md):
+# pivot pass 2.9 MB read + 24.9 MB written, base pass 292.1 MB read + 12.8 MB
+# written.  ncu is not run inside the bench; the value is reported beside the
+# live timing as the capture's figure.
+SCAN_TRAFFIC_BYTES_PER_STEP = 332.7e6
 
 
 def peaks() -> dict:

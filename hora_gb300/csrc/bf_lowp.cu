@@ -77,7 +77,9 @@ struct LowpState {
   DevBuf coff;     // pc + 1 int64 member offsets
   DevBuf cmem;     // n uint32 member rows, cluster after cluster, ascending
   DevBuf xsqmax;   // 1 f32: the largest squared row norm
-  DevBuf ctiles;   // the pivots' BF16 tile image (same layout as tiles)
+  DevBuf ctiles;   // the pivots' BF16 tile image (the BF16 base's layout, also for an FP8 base)
+  int64_t ctile_bytes = 0;
+  int cnkb = 0;    // the pivot image's 128-byte K blocks
   // BF16 Euclidean: the largest |x - bf16(x)| over the rows (1 f32, rounded
   // up), the rows' share of the certified exact search's error bound
   DevBuf dxmax;
@@ -663,13 +665,14 @@ constexpr int64_t kProbeRowsPerPivot = 1024;
 constexpr int64_t kProbeMinRows = 65536;
 constexpr int kProbeMaxMembers = 1024;  // members a query is scored against
 constexpr int kProbeMaxR = 256;         // widest R-best list the probe serves
+constexpr int kExactTcMaxK = 256;       // largest k of the certified exact search
 constexpr int kProbeMinCluster = 256;   // smaller clusters are dissolved at the end
 constexpr int kProbeReseed = 128;       // Lloyd steps re-seed clusters below this
 constexpr int kProbeLloyd = 6;
 constexpr int kProbeQ = 32;       // queries per pass of a probe CTA
 constexpr int kProbeRows = 128;   // member rows per shared-memory tile
 constexpr int kProbePitch = 132;  // f32 pitch of a staged row (spreads the banks)
-constexpr int kProbeSmem = (kProbeQ + kProbeRows) * kProbePitch * 4 + kProbeMaxMembers * 8;
+constexpr int kProbeSmem = (kProbeQ + kProbeRows) * kProbePitch * 4 + kProbeMaxMembers * 12;
 
 __device__ __forceinline__ void bf16x8_to_f32(const uint4 &v, float *out) {
   const uint32_t w[4] = {v.x, v.y, v.z, v.w};
@@ -678,6 +681,23 @@ __device__ __forceinline__ void bf16x8_to_f32(const uint4 &v, float *out) {
     out[2 * i] = __uint_as_float(w[i] << 16);
     out[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
   }
+}
+
+// The 16 e4m3 values of a 16-byte chunk as f32 (through the library's
+// FP8 -> half conversion, exact).
+__device__ __forceinline__ void e4m3x16_to_f32(const uint4 &v, float *out) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const __nv_fp8_storage_t b = (__nv_fp8_storage_t)((w[i >> 2] >> (8 * (i & 3))) & 0xffu);
+    out[i] = __half2float(__half(__nv_cvt_fp8_to_halfraw(b, __NV_E4M3)));
+  }
+}
+
+// Elements per 16-byte chunk of a row: 8 BF16 values or 16 e4m3 values.
+template <bool FP8>
+__device__ __forceinline__ void chunk_to_f32(const uint4 &v, float *out) {
+  if (FP8) e4m3x16_to_f32(v, out); else bf16x8_to_f32(v, out);
 }
 
 // The 16-byte chunks of member rows mt.. (kProbeRows of them) that thread t
@@ -701,18 +721,24 @@ __device__ __forceinline__ void probe_load_tile(uint4 (&buf)[8], const uint32_t 
 // first kProbeMaxMembers member rows, read from the tile image.  Thread (qg, rg)
 // of the 8 x 32 layout scores queries qg + 8i against rows rg + 32j, the
 // products summed over ascending dimensions with one f32 FMA each, then the
-// folded norm added: dist = qsq - 2 (sum + (-|x|^2 / 2)).
+// scan's distance formed from the sum: BF16 (norm folded) qsq - 2 (sum +
+// (-|x|^2 / 2)); FP8 (per-row scales) qsq + |x|^2 - 2 sum (qscale xscale).
+template <bool FP8>
 __global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, int64_t tile_bytes,
-                                                         const float *xsq, const int64_t *coff,
-                                                         const uint32_t *cmem, const __nv_bfloat16 *lq,
+                                                         const float *xsq, const float *xscale,
+                                                         const int64_t *coff, const uint32_t *cmem,
+                                                         const uint8_t *lq, const float *lqscale,
                                                          int64_t Dp, const float *qsq, const int64_t *qoff,
                                                          const uint32_t *qmem, const int *item_off, int C,
                                                          float *pdist) {
   extern __shared__ __align__(16) float psm[];
   float *qs = psm;                           // kProbeQ x kProbePitch
   float *xs = qs + kProbeQ * kProbePitch;    // kProbeRows x kProbePitch
-  float *xh = xs + kProbeRows * kProbePitch;                       // per member: -|x|^2 / 2
-  uint32_t *ids = reinterpret_cast<uint32_t *>(xh + kProbeMaxMembers);  // per member: its row
+  float *xh = xs + kProbeRows * kProbePitch;                       // per member: -|x|^2 / 2 (FP8: |x|^2)
+  float *xc = xh + kProbeMaxMembers;                               // per member: its scale (FP8)
+  uint32_t *ids = reinterpret_cast<uint32_t *>(xc + kProbeMaxMembers);  // per member: its row
+  constexpr int kPer = FP8 ? 16 : 8;  // elements per 16-byte chunk
+  constexpr int esz = FP8 ? 1 : 2;
   // work item blockIdx.x: batch (item - item_off[c]) of pivot c's queries
   const int b = blockIdx.x;
   if (b >= item_off[C]) return;
@@ -726,7 +752,7 @@ __global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, i
   const int64_t m_lo = coff[c];
   const int L = (int)(coff[c + 1] - m_lo < kProbeMaxMembers ? coff[c + 1] - m_lo : kProbeMaxMembers);
   const int t = threadIdx.x, qg = t & 7, rg = t >> 3;
-  const int D = (int)Dp, nch = D / 8;
+  const int D = (int)Dp, nch = D / kPer;
   {
     const int64_t qb = (int64_t)(b - item_off[c]) * kProbeQ;
     const int nb = (int)(nqc - qb < kProbeQ ? nqc - qb : kProbeQ);
@@ -734,18 +760,21 @@ __global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, i
     for (int j = t; j < L; j += 256) {
       const uint32_t r = cmem[m_lo + j];
       ids[j] = r;
-      xh[j] = -0.5f * xsq[r];
+      xh[j] = FP8 ? xsq[r] : -0.5f * xsq[r];
+      xc[j] = FP8 ? xscale[r] : 1.0f;
     }
     for (int i = t; i < kProbeQ * nch; i += 256) {
       const int qi = i / nch, ch = i % nch;
-      float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float f[16];
+#pragma unroll
+      for (int e = 0; e < kPer; ++e) f[e] = 0.0f;
       if (qi < nb) {
         const uint32_t qid = qmem[q_lo + qb + qi];
-        bf16x8_to_f32(*reinterpret_cast<const uint4 *>(lq + (int64_t)qid * Dp + ch * 8), f);
+        chunk_to_f32<FP8>(*reinterpret_cast<const uint4 *>(lq + ((int64_t)qid * Dp + ch * kPer) * esz), f);
       }
-      float4 *dst = reinterpret_cast<float4 *>(qs + qi * kProbePitch + ch * 8);
-      dst[0] = make_float4(f[0], f[1], f[2], f[3]);
-      dst[1] = make_float4(f[4], f[5], f[6], f[7]);
+      float4 *dst = reinterpret_cast<float4 *>(qs + qi * kProbePitch + ch * kPer);
+#pragma unroll
+      for (int e = 0; e < kPer / 4; ++e) dst[e] = make_float4(f[4 * e], f[4 * e + 1], f[4 * e + 2], f[4 * e + 3]);
     }
     __syncthreads();  // member rows and queries staged
     // a tile's 16-byte chunks in registers: the next tile's loads are in
@@ -758,11 +787,11 @@ __global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, i
       for (int u = 0; u < 8; ++u) {
         const int i = t + 256 * u, j = i / nch, ch = i % nch;
         if (i < kProbeRows * nch) {
-          float f[8];
-          bf16x8_to_f32(buf[u], f);
-          float4 *dst = reinterpret_cast<float4 *>(xs + j * kProbePitch + ch * 8);
-          dst[0] = make_float4(f[0], f[1], f[2], f[3]);
-          dst[1] = make_float4(f[4], f[5], f[6], f[7]);
+          float f[16];
+          chunk_to_f32<FP8>(buf[u], f);
+          float4 *dst = reinterpret_cast<float4 *>(xs + j * kProbePitch + ch * kPer);
+#pragma unroll
+          for (int e = 0; e < kPer / 4; ++e) dst[e] = make_float4(f[4 * e], f[4 * e + 1], f[4 * e + 2], f[4 * e + 3]);
         }
       }
       __syncthreads();
@@ -797,10 +826,13 @@ __global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, i
         if (i >= ni || qi >= nb) continue;
         const uint32_t qid = qmem[q_lo + qb + qi];
         const float qa = qsq[qid];
+        const float qsc = FP8 ? lqscale[qid] : 1.0f;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int m = mt + rg + 32 * j;
-          if (m < L) pdist[(int64_t)qid * kProbeMaxMembers + m] = fmaf(-2.0f, acc[i][j] + xh[m], qa);
+          if (m < L)
+            pdist[(int64_t)qid * kProbeMaxMembers + m] =
+                FP8 ? fmaf(-2.0f, acc[i][j] * (qsc * xc[m]), qa + xh[m]) : fmaf(-2.0f, acc[i][j] + xh[m], qa);
         }
       }
     }
@@ -1106,7 +1138,8 @@ static int probe_pivot_count(int64_t n) {
 }
 
 static bool probe_eligible(const hora_index *h) {
-  return h->bf_probe && h->precision == HORA_PREC_BF16 && h->metric == M_L2 && h->n >= kProbeMinRows;
+  return h->bf_probe && (h->precision == HORA_PREC_BF16 || h->precision == HORA_PREC_FP8) && h->metric == M_L2 &&
+         h->n >= kProbeMinRows;
 }
 
 // Pivot clusters of the base (exact FP32 nearest-pivot assignment): evenly
@@ -1192,14 +1225,16 @@ static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
   max_nonneg_kernel<<<152, 256, 0, s>>>(L.xsq.as<float>(), n, L.xsqmax.as<unsigned>());
   HORA_LAUNCHED();
   // the pivots' tile image (BF16 rows and folded norms, like the base's)
-  const int64_t Dp = L.Dp;
+  const int64_t Dp = round_up((int64_t)h->dim, 64);  // BF16, whatever the base's precision
   const int nkb = (int)(Dp / 64);
+  L.cnkb = nkb;
+  L.ctile_bytes = (int64_t)nkb * kLpBN * 128 + kNormBytesB;
   const int64_t ctiles = ceil_div((int64_t)C, (int64_t)kLpBN);
   DevBuf crow, cnorm, csq;
   HORA_TRY(crow.reserve(sizeof(__nv_bfloat16) * C * Dp));
   HORA_TRY(cnorm.reserve(sizeof(__nv_bfloat16) * C * 16));
   HORA_TRY(csq.reserve(sizeof(double) * C));
-  HORA_TRY(L.ctiles.reserve(ctiles * L.tile_bytes));
+  HORA_TRY(L.ctiles.reserve(ctiles * L.ctile_bytes));
   HORA_TRY(launch_row_norms(L.centers.as<float>(), C, ld, h->dim, nullptr, csq.as<double>(), s));
   to_bf16_kernel<<<ceil_div((int64_t)C * Dp, 256), 256, 0, s>>>(L.centers.as<float>(), C, ld, h->dim, Dp, nullptr,
                                                                 crow.as<__nv_bfloat16>());
@@ -1207,7 +1242,7 @@ static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
   norm_block_kernel<<<ceil_div((int64_t)C, 256), 256, 0, s>>>(csq.as<double>(), C, cnorm.as<__nv_bfloat16>());
   HORA_LAUNCHED();
   tile_image_kernel<<<ceil_div(ctiles * kLpBN * (nkb * 8 + 2), 256), 256, 0, s>>>(
-      crow.as<uint8_t>(), C, Dp * 2, nkb, cnorm.as<uint8_t>(), L.tile_bytes, ctiles, L.ctiles.as<uint8_t>());
+      crow.as<uint8_t>(), C, Dp * 2, nkb, cnorm.as<uint8_t>(), L.ctile_bytes, ctiles, L.ctiles.as<uint8_t>());
   HORA_LAUNCHED();
   HORA_CUDA_TRY(cudaStreamSynchronize(s));  // the temporaries are freed on return
   L.pc = C;
@@ -1217,8 +1252,11 @@ static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
 // Starting thresholds of nq staged queries (ws.q f32, ws.lq BF16 under the
 // tensor map ta, ws.lqsq) into ws.ptau.  lp carries the search's scan
 // parameters; its candidate lists take the pivot scores (C <= cap).
-static int probe_thresholds(hora_index *h, LowpState &L, int64_t nq, int R, int64_t Dp, SearchWorkspace &ws,
-                            const CUtensorMap &ta, const LpParams &lp, cudaStream_t s,
+// ta16: the queries' BF16 tile map (the pivot pass runs in BF16 whatever
+// the base's precision); the probe scores members in the base's precision
+// (prec), from ws.lq (and ws.lqscale for FP8).
+static int probe_thresholds(hora_index *h, LowpState &L, int prec, int64_t nq, int R, int64_t Dp,
+                            SearchWorkspace &ws, const CUtensorMap &ta16, const LpParams &lp, cudaStream_t s,
                             const float *slack = nullptr) {
   const int C = L.pc;
   // sized for a power of two of at least 1,024 queries: a serving slot whose
@@ -1240,19 +1278,32 @@ static int probe_thresholds(hora_index *h, LowpState &L, int64_t nq, int R, int6
   a.tpc = lp_tiles_per_cta(nq, C);
   a.tau0 = nullptr;
   a.dense_hits = 0;
-  HORA_TRY(launch_lp2<HORA_PREC_BF16>(M_L2, TILE_DENSE, ta, a, s));
+  a.nkb = L.cnkb;
+  a.stages = lp_stages(L.cnkb, true);
+  HORA_TRY(launch_lp2<HORA_PREC_BF16>(M_L2, TILE_DENSE, ta16, a, s));
   HORA_CUDA_TRY(cudaMemsetAsync(ws.pkeys.ptr, 0xff, sizeof(uint64_t) * nq, s));
   HORA_TRY(launch_merge_topk(ws.pkeys.as<uint64_t>(), 1, a.cand, a.count, a.cap, C, nullptr, nq, nullptr, nullptr, s));
   HORA_TRY(sort_labels(ws.pkeys.as<uint64_t>(), nullptr, nq, C, ws.pblk, ws.pcnt, qoff, ws.pmem.as<uint32_t>(), s));
-  HORA_SMEM_ATTR(probe_dist_kernel, kProbeSmem);
+  const bool fp8 = prec == HORA_PREC_FP8;
+  if (fp8)
+    HORA_SMEM_ATTR(probe_dist_kernel<true>, kProbeSmem);
+  else
+    HORA_SMEM_ATTR(probe_dist_kernel<false>, kProbeSmem);
   {
     ProfScope ps("probe_scores", s);
     probe_items_kernel<<<1, 1024, 0, s>>>(qoff, C, item_off);
     HORA_LAUNCHED();
-    probe_dist_kernel<<<(unsigned)(C + ceil_div(nq, (int64_t)kProbeQ)), 256, kProbeSmem, s>>>(
-      L.tiles.as<uint8_t>(), L.tile_bytes, L.xsq.as<float>(), L.coff.as<int64_t>(), L.cmem.as<uint32_t>(),
-      ws.lq.as<__nv_bfloat16>(), Dp, ws.lqsq.as<float>(), qoff, ws.pmem.as<uint32_t>(), item_off, C,
-      ws.pdist.as<float>());
+    const unsigned grid = (unsigned)(C + ceil_div(nq, (int64_t)kProbeQ));
+    if (fp8)
+      probe_dist_kernel<true><<<grid, 256, kProbeSmem, s>>>(
+          L.tiles.as<uint8_t>(), L.tile_bytes, L.xsq.as<float>(), L.xscale.as<float>(), L.coff.as<int64_t>(),
+          L.cmem.as<uint32_t>(), ws.lq.as<uint8_t>(), ws.lqscale.as<float>(), Dp, ws.lqsq.as<float>(), qoff,
+          ws.pmem.as<uint32_t>(), item_off, C, ws.pdist.as<float>());
+    else
+      probe_dist_kernel<false><<<grid, 256, kProbeSmem, s>>>(
+          L.tiles.as<uint8_t>(), L.tile_bytes, L.xsq.as<float>(), nullptr, L.coff.as<int64_t>(),
+          L.cmem.as<uint32_t>(), ws.lq.as<uint8_t>(), nullptr, Dp, ws.lqsq.as<float>(), qoff,
+          ws.pmem.as<uint32_t>(), item_off, C, ws.pdist.as<float>());
     HORA_LAUNCHED();
   }
   ProfScope ps("probe_select", s);
@@ -1410,11 +1461,22 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   };
   int *lerr = ws.lerr.as<int>();  // [0] a pipeline wait timed out, [1] short lists after the probed pass
   // the pivot pass writes one key per pivot into each query's candidate list
-  const bool probe = probe_eligible(h) && R <= kProbeMaxR && probe_pivot_count(n) <= cap;
+  // (the probe kernel stages rows of at most 128 values)
+  const bool probe = probe_eligible(h) && R <= kProbeMaxR && probe_pivot_count(n) <= cap && Dp <= 128;
   if (probe) {
     // one filter pass from the probed thresholds
     HORA_TRY(ensure_pivots(h, L, s));
-    HORA_TRY(probe_thresholds(h, L, nq, R, Dp, ws, ta, p, s));
+    CUtensorMap ta16 = ta;
+    if (prec == HORA_PREC_FP8) {
+      // the pivot pass reads the queries in BF16
+      const int64_t Dp16 = round_up((int64_t)h->dim, 64);
+      HORA_TRY(ws.lq16.reserve(std::max<int64_t>(nq, 1) * Dp16 * 2));
+      to_bf16_kernel<<<ceil_div(nq * Dp16, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp16, nullptr,
+                                                               ws.lq16.as<__nv_bfloat16>());
+      HORA_LAUNCHED();
+      HORA_TRY(make_tmap(&ta16, ws.lq16.ptr, HORA_PREC_BF16, Dp16, nq, kLpBM));
+    }
+    HORA_TRY(probe_thresholds(h, L, prec, nq, R, Dp, ws, ta16, p, s));
     p.tau0 = ws.ptau.as<float>();
     p.dense_hits = 0;
     for (int64_t lo = 0; lo < n; lo += max_chunk) {
@@ -1578,7 +1640,7 @@ __global__ void scatter_keys_kernel(const uint64_t *src, int k, const int *list,
 
 bool exact_tc_eligible(const hora_index *h, int k) {
   return h->exact_tc && h->precision == HORA_PREC_FP32 && h->metric == M_L2 && h->n >= kProbeMinRows &&
-         round_up((int64_t)h->dim, 64) / 64 <= 2 && k <= kProbeMaxR &&
+         round_up((int64_t)h->dim, 64) / 64 <= 2 && k <= kExactTcMaxK &&
          probe_pivot_count(h->n) <= (int)round_up(std::max(h->cand_cap, 2 * k), 128);
 }
 
@@ -1645,7 +1707,7 @@ int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, 
   p.cap = cap;
   p.count = count;
   p.err = lerr;
-  HORA_TRY(probe_thresholds(h, L, nq, k, Dp, ws, ta, p, s, ws.xslack.as<float>()));
+  HORA_TRY(probe_thresholds(h, L, HORA_PREC_BF16, nq, k, Dp, ws, ta, p, s, ws.xslack.as<float>()));
   p.tau0 = ws.ptau.as<float>();
   const int64_t n = h->n;
   const int64_t max_chunk = (int64_t)60000 * kLpBN * kLpMinTilesPerCta;

@@ -87,6 +87,7 @@ struct SearchWorkspace {
   DevBuf adc_next, adc_gmap;  // the ADC kernel's group counter and group -> list map
   // low-precision scoring
   DevBuf lq, lqsq, lqscale, lqgather, lerr;
+  DevBuf lq16;  // an FP8 search's BF16 query copy (the pivot pass reads it)
   // BF16 starting thresholds: query -> pivot keys, queries bucketed by pivot,
   // probe distances (queries x members), thresholds
   DevBuf pkeys, poff, pmem, pblk, pcnt, pdist, ptau;
@@ -107,7 +108,7 @@ struct SearchWorkspace {
     const DevBuf *all[] = {&q, &qnorm, &best, &cand, &count, &ovf_flag, &ovf_counter, &qlist, &out_ids,
                            &out_dist, &rows, &keys2, &tmp, &coarse, &probes, &pair_cnt, &pair_off, &pair_q,
                            &pair_c, &pair_slot, &ivf_cand, &best_r, &tmp_keys, &adc_next, &adc_gmap, &lq,
-                           &lqsq, &lqscale, &lqgather, &lerr, &pkeys, &poff, &pmem, &pblk, &pcnt, &pdist,
+                           &lqsq, &lqscale, &lqgather, &lerr, &lq16, &pkeys, &poff, &pmem, &pblk, &pcnt, &pdist,
                            &ptau, &feats, &pred, &npq, &xslack, &xempty, &xlist, &xq, &xkeys, &d_status};
     size_t b = 0;
     for (const DevBuf *d : all) b += d->bytes;

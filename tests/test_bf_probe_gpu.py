@@ -1,5 +1,5 @@
-"""Starting thresholds from pivot clusters (BF16 Euclidean brute force on at
-least 65,536 rows).
+"""Starting thresholds from pivot clusters (BF16 and FP8 Euclidean brute force
+on at least 65,536 rows).
 
 The probed schedule must return exactly what the chunked schedule returns
 (the same approximate R-best set, hence the same exact rerank), fall back to
@@ -14,11 +14,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def build(hora, base, R):
+def build(hora, base, R, prec=1):
     ix = hora.BruteForceIndex(base.shape[1])
     ix.madd(base, None)
     ix.build(hora.Metric.Euclidean)
-    ix.set_option(hora.Option.PRECISION, 1)
+    ix.set_option(hora.Option.PRECISION, prec)
     ix.set_option(hora.Option.RERANK, R)
     return ix
 
@@ -31,14 +31,15 @@ def run(hora, ix, q, k, probe):
 
 @pytest.mark.parametrize("dim,R,k", [(128, 132, 100), (64, 256, 10), (32, 200, 1), (48, 400, 10)])
 def test_probe_matches_chunked(hora, oracle, gpu, dim, R, k):
-    """R-best lists wider than 256 keep the chunked schedule."""
+    """R-best lists wider than 256 keep the chunked schedule; a query whose
+    pivot cluster holds fewer than R members is answered by it too."""
     from hora_gb300 import synth
     base = synth.mixture(100_000, dim, 256, stream=41)
     q = synth.mixture(700, dim, 256, stream=42)
     ix = build(hora, base, R)
     ids1, d1, info1 = run(hora, ix, q, k, 1)
     ids0, d0, info0 = run(hora, ix, q, k, 0)
-    assert info1["last_threshold_probe"] == (1 if R <= 256 else 0)
+    assert info1["last_threshold_probe"] in ((1, 2) if R <= 256 else (0,))
     assert info0["last_threshold_probe"] == 0
     np.testing.assert_array_equal(ids1, ids0)
     np.testing.assert_array_equal(d1, d0)
@@ -103,3 +104,21 @@ def test_small_candidate_capacity_keeps_chunked(hora, gpu):
     assert info2["last_threshold_probe"] == 0
     np.testing.assert_array_equal(ids1, ids2)
     np.testing.assert_array_equal(d1, d2)
+
+
+@pytest.mark.parametrize("dim,R,k", [(128, 256, 100), (128, 132, 100), (64, 200, 10)])
+def test_fp8_probe_matches_chunked(hora, oracle, gpu, dim, R, k):
+    """FP8 e4m3 scoring (per-row scales): the probe scores the cluster members
+    with the scan's FP8 operands and scales; the probed pass returns the
+    chunked schedule's lists bit for bit."""
+    from hora_gb300 import synth
+    base = synth.mixture(100_000, dim, 256, stream=45)
+    q = synth.mixture(700, dim, 256, stream=46)
+    ix = build(hora, base, R, prec=2)
+    ids1, d1, info1 = run(hora, ix, q, k, 1)
+    ids0, d0, info0 = run(hora, ix, q, k, 0)
+    assert info1["last_threshold_probe"] in (1, 2) and info0["last_threshold_probe"] == 0
+    np.testing.assert_array_equal(ids1, ids0)
+    np.testing.assert_array_equal(d1, d0)
+    for qi in range(0, 700, 97):
+        assert d1[qi, 0] == oracle.metric(q[qi], base[int(ids1[qi, 0])], 3)
