@@ -472,6 +472,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       thr = MT == M_L2 ? 0.5f * (qa - tau_d) - slack : (MT == M_IP ? tau_d + slack : -tau_d - slack);
     }
     uint64_t *hbuf = reinterpret_cast<uint64_t *>(bars + kLpBarSlots);
+    uint64_t amin = kEmptyKey;  // TILE_ARGMIN: this thread's smallest key so far
     DrainCtx c{p.cand, p.count, hbuf + (threadIdx.x - 64), qid, 0, p.r_begin, p.r_end, p.cap, qa, tau_d, tau_r};
     int nb = 0;  // keys staged in this thread's column
     for (int t = 0; t < T; ++t) {
@@ -503,7 +504,26 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         tc::mbar_arrive(acc_empty + b);
       }
       if (FAST) {
-        if constexpr (MODE == TILE_DENSE) {
+        if constexpr (MODE == TILE_ARGMIN) {
+          // the smallest (distance, row) key of the slice: strict < keeps the
+          // lowest column among equal distances
+          if (qid >= 0) {
+            float dm = __int_as_float(0x7f800000);
+            int jm = -1;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const float d = drain_dist<MT, TILE_DENSE, true>(v[j], qa);
+              if (c.rt + j < c.r_end && d < dm) {
+                dm = d;
+                jm = j;
+              }
+            }
+            if (jm >= 0) {
+              const uint64_t key = make_key(dm, (uint32_t)(c.rt + jm));
+              amin = key < amin ? key : amin;
+            }
+          }
+        } else if constexpr (MODE == TILE_DENSE) {
           if (qid >= 0) drain_mask<MT, MODE, true>(v, 0xffffffffu, c, nb);
         } else {
           // the slice's extreme decides whether any column can hit; the
@@ -558,6 +578,8 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       }
     }
     if (qid >= 0 && nb > 0) flush_hits(c, nb);
+    if (MODE == TILE_ARGMIN && qid >= 0 && amin != kEmptyKey)
+      atomicMin(reinterpret_cast<unsigned long long *>(p.best + qid), (unsigned long long)amin);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -1249,9 +1271,9 @@ static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
   return HORA_OK;
 }
 
-// Starting thresholds of nq staged queries (ws.q f32, ws.lq BF16 under the
-// tensor map ta, ws.lqsq) into ws.ptau.  lp carries the search's scan
-// parameters; its candidate lists take the pivot scores (C <= cap).
+// Starting thresholds of nq staged queries (ws.q f32, ws.lq, ws.lqsq) into
+// ws.ptau.  lp carries the search's scan parameters; the pivot pass keeps
+// each query's nearest pivot key in ws.pkeys.
 // ta16: the queries' BF16 tile map (the pivot pass runs in BF16 whatever
 // the base's precision); the probe scores members in the base's precision
 // (prec), from ws.lq (and ws.lqscale for FP8).
@@ -1280,9 +1302,11 @@ static int probe_thresholds(hora_index *h, LowpState &L, int prec, int64_t nq, i
   a.dense_hits = 0;
   a.nkb = L.cnkb;
   a.stages = lp_stages(L.cnkb, true);
-  HORA_TRY(launch_lp2<HORA_PREC_BF16>(M_L2, TILE_DENSE, ta16, a, s));
+  // each drain thread's smallest key, combined by a 64-bit atomic minimum
+  // per query (no per-pivot keys written)
+  a.best = ws.pkeys.as<uint64_t>();
   HORA_CUDA_TRY(cudaMemsetAsync(ws.pkeys.ptr, 0xff, sizeof(uint64_t) * nq, s));
-  HORA_TRY(launch_merge_topk(ws.pkeys.as<uint64_t>(), 1, a.cand, a.count, a.cap, C, nullptr, nq, nullptr, nullptr, s));
+  HORA_TRY((launch_lp3<HORA_PREC_BF16, M_L2, TILE_ARGMIN>(ta16, a, s)));
   HORA_TRY(sort_labels(ws.pkeys.as<uint64_t>(), nullptr, nq, C, ws.pblk, ws.pcnt, qoff, ws.pmem.as<uint32_t>(), s));
   const bool fp8 = prec == HORA_PREC_FP8;
   if (fp8)
@@ -1460,9 +1484,8 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     return make_tmap(tg, ws.lqgather.ptr, prec, Dp, nl, kLpBM);
   };
   int *lerr = ws.lerr.as<int>();  // [0] a pipeline wait timed out, [1] short lists after the probed pass
-  // the pivot pass writes one key per pivot into each query's candidate list
   // (the probe kernel stages rows of at most 128 values)
-  const bool probe = probe_eligible(h) && R <= kProbeMaxR && probe_pivot_count(n) <= cap && Dp <= 128;
+  const bool probe = probe_eligible(h) && R <= kProbeMaxR && Dp <= 128;
   if (probe) {
     // one filter pass from the probed thresholds
     HORA_TRY(ensure_pivots(h, L, s));
@@ -1640,8 +1663,7 @@ __global__ void scatter_keys_kernel(const uint64_t *src, int k, const int *list,
 
 bool exact_tc_eligible(const hora_index *h, int k) {
   return h->exact_tc && h->precision == HORA_PREC_FP32 && h->metric == M_L2 && h->n >= kProbeMinRows &&
-         round_up((int64_t)h->dim, 64) / 64 <= 2 && k <= kExactTcMaxK &&
-         probe_pivot_count(h->n) <= (int)round_up(std::max(h->cand_cap, 2 * k), 128);
+         round_up((int64_t)h->dim, 64) / 64 <= 2 && k <= kExactTcMaxK;
 }
 
 int exact_tc_prepare(hora_index *h, cudaStream_t s) {

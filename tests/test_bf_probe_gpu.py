@@ -88,11 +88,11 @@ def test_probe_overflow_with_duplicates(hora, oracle, gpu):
     assert d1[3, 0] == oracle.metric(q[3], base[rows[0]], 3)
 
 
-def test_small_candidate_capacity_keeps_chunked(hora, gpu):
-    """The pivot pass writes one key per pivot into each query's candidate
-    list: with a capacity below the pivot count (410 pivots for 420,000 rows
-    against 384 slots) the probe stays off; with the default it is on, and
-    both answers agree."""
+def test_small_candidate_capacity(hora, gpu):
+    """The pivot pass keeps only each query's nearest pivot (no per-pivot
+    keys), so a candidate capacity below the pivot count (410 pivots for
+    420,000 rows against 256 slots) still runs the probed schedule; the
+    small capacity then overflows into rescans, and both answers agree."""
     from hora_gb300 import synth
     base = synth.mixture(420_000, 16, 256, stream=43)
     q = synth.mixture(300, 16, 256, stream=44)
@@ -101,7 +101,7 @@ def test_small_candidate_capacity_keeps_chunked(hora, gpu):
     assert info1["last_threshold_probe"] == 1
     ix.set_option(hora.Option.CAND_CAP, 256)
     ids2, d2, info2 = run(hora, ix, q, 20, 1)
-    assert info2["last_threshold_probe"] == 0
+    assert info2["last_threshold_probe"] in (1, 2)
     np.testing.assert_array_equal(ids1, ids2)
     np.testing.assert_array_equal(d1, d2)
 
