@@ -638,6 +638,7 @@ __global__ void group_scan_kernel(const int64_t *cnt, int C, int G, int64_t *pai
 }
 
 constexpr int kAdcThreads = 512;
+static_assert(kAdcThreads % 128 == 0, "the code-major LUT build fixes m per thread");
 constexpr int kAdcChunk = 2048;  // code rows scored per selection round
 
 // G sums over subspaces of LUT[m][code[m]] (one per query of the group),
@@ -697,29 +698,49 @@ __device__ __forceinline__ void adc_row_g(const uint8_t *code, const float *lut,
 }
 
 // The same sums for a 32-subspace code row already in registers (two
-// 16-byte words), K = 256.
+// 16-byte words), K = 256, from a LUT laid out code-major (entry (m, j) at
+// j * 32 + m: for 16-byte entries the bank group is m mod 8).  Lane l
+// starts its row sk = l mod 8 steps late: at step s it adds subspace s - sk,
+// so the eight lanes of a quarter warp read eight different m, one bank
+// group each, and every 16-byte gather is conflict-free; each lane still adds
+// its subspaces in order 0..31 (bit-identical sums).  The code row is
+// shifted by sk bytes once, so that step s reads byte s of it.
 template <int G>
-__device__ __forceinline__ void adc_row32_g(const uint4 w0, const uint4 w1, const float *lut, float (&d)[G]) {
+__device__ __forceinline__ void adc_row32_skew_g(const uint4 w0, const uint4 w1, const float *lut, int sk,
+                                                 float (&d)[G]) {
 #pragma unroll
   for (int g = 0; g < G; ++g) d[g] = 0.0f;
+  const uint32_t c[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+  // B = the 32 code bytes moved up by sk bytes (10 words, zero filled)
+  const int q = sk >> 2, r = 8 * (sk & 3);
+  uint32_t B[10];
 #pragma unroll
-  for (int m = 0; m < 32; ++m) {
-    const uint4 w = m < 16 ? w0 : w1;
-    const int t = m & 15;
-    const uint32_t wt = t < 4 ? w.x : t < 8 ? w.y : t < 12 ? w.z : w.w;
-    const int e = m * 256 + (int)((wt >> (8 * (t & 3))) & 255u);
-    if (G == 4) {
-      const float4 v = reinterpret_cast<const float4 *>(lut)[e];
-      d[0] = __fadd_rn(d[0], v.x);
-      d[1 % G] = __fadd_rn(d[1 % G], v.y);
-      d[2 % G] = __fadd_rn(d[2 % G], v.z);
-      d[3 % G] = __fadd_rn(d[3 % G], v.w);
-    } else if (G == 2) {
-      const float2 v = reinterpret_cast<const float2 *>(lut)[e];
-      d[0] = __fadd_rn(d[0], v.x);
-      d[1 % G] = __fadd_rn(d[1 % G], v.y);
-    } else {
-      d[0] = __fadd_rn(d[0], lut[e]);
+  for (int i = 0; i < 10; ++i) {
+    const uint32_t a0 = i - 1 >= 0 && i - 1 < 8 ? c[i - 1] : 0u, a1 = i < 8 ? c[i] : 0u;
+    const uint32_t b0 = i - 2 >= 0 && i - 2 < 8 ? c[i - 2] : 0u;
+    const uint32_t s0 = __funnelshift_l(a0, a1, r);  // q = 0: (c[i] << r) | (c[i-1] >> (32 - r))
+    const uint32_t s1 = __funnelshift_l(b0, a0, r);  // q = 1: one word further up
+    B[i] = q ? s1 : s0;
+  }
+#pragma unroll
+  for (int st = 0; st < 39; ++st) {
+    const int m = st - sk;
+    if ((unsigned)m < 32u) {
+      const int j = (int)((B[st >> 2] >> (8 * (st & 3))) & 255u);
+      const int e = j * 32 + m;
+      if (G == 4) {
+        const float4 v = reinterpret_cast<const float4 *>(lut)[e];
+        d[0] = __fadd_rn(d[0], v.x);
+        d[1 % G] = __fadd_rn(d[1 % G], v.y);
+        d[2 % G] = __fadd_rn(d[2 % G], v.z);
+        d[3 % G] = __fadd_rn(d[3 % G], v.w);
+      } else if (G == 2) {
+        const float2 v = reinterpret_cast<const float2 *>(lut)[e];
+        d[0] = __fadd_rn(d[0], v.x);
+        d[1 % G] = __fadd_rn(d[1 % G], v.y);
+      } else {
+        d[0] = __fadd_rn(d[0], lut[e]);
+      }
     }
   }
 }
@@ -741,23 +762,79 @@ __device__ __forceinline__ void lut_store_g(float *lut, int e, const float (&acc
 
 template <int G, int MT, int DMC>
 __device__ __forceinline__ void lut_build_g(const float *book, const float *zq, int dz, const int *sbs,
-                                            const int *sls, int MK, int kbits, int dm, float *lut) {
-  if (DMC == 4) {
-    // every subspace spans 4 dimensions starting at a multiple of 4: the
-    // residual slice of each query is one aligned 16-byte load
+                                            const int *sls, int M, int K, int kbits, int dm, bool tr,
+                                            float *lut) {
+  // work item i computes entry (m, j) into LUT slot m K + j (m-major), or
+  // with tr (M = 32, K = 256) into slot j 32 + m (code-major); then the 32
+  // items of a warp cover 8 consecutive m x 4 consecutive j, so its codeword
+  // loads are 8 runs of 64 bytes and each quarter warp stores 8 consecutive
+  // slots (conflict-free)
+  const int MK = M * K;
+  auto entry_of = [&](int i, int &m, int &j, int &slot) {
+    if (tr) {
+      m = (i & 7) | (((i >> 5) & 3) << 3);
+      j = ((i >> 3) & 3) | ((i >> 7) << 2);
+      slot = j * 32 + m;
+    } else {
+      m = i >> kbits;
+      j = i & (K - 1);
+      slot = i;
+    }
+  };
+  if (DMC == 4 && tr) {
+    // every subspace spans 4 dimensions starting at a multiple of 4, and with
+    // the code-major mapping (blockDim a multiple of 128) a thread's items all
+    // share one m: its queries' residual slices are loaded once
     const float4 *b4 = reinterpret_cast<const float4 *>(book);
-    for (int e0 = threadIdx.x; e0 < MK; e0 += 8 * blockDim.x) {
+    const int m = (threadIdx.x & 7) | (((threadIdx.x >> 5) & 3) << 3);
+    float4 z[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) z[g] = *reinterpret_cast<const float4 *>(zq + g * dz + sbs[m]);
+    for (int i0 = threadIdx.x; i0 < MK; i0 += 8 * blockDim.x) {
       float4 cv[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const int e = e0 + u * blockDim.x;
-        if (e < MK) cv[u] = __ldg(b4 + e);
+        const int i = i0 + u * blockDim.x;
+        if (i < MK) cv[u] = __ldg(b4 + m * K + (((i >> 3) & 3) | ((i >> 7) << 2)));
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const int e = e0 + u * blockDim.x;
-        if (e < MK) {
-          const int zo = sbs[e >> kbits];
+        const int i = i0 + u * blockDim.x;
+        if (i < MK) {
+          float acc[G];
+#pragma unroll
+          for (int g = 0; g < G; ++g) {
+            float a = dist_op<MT>(0.0f, z[g].x, cv[u].x);
+            a = dist_op<MT>(a, z[g].y, cv[u].y);
+            a = dist_op<MT>(a, z[g].z, cv[u].z);
+            acc[g] = dist_op<MT>(a, z[g].w, cv[u].w);
+          }
+          lut_store_g<G, MT>(lut, (((i >> 3) & 3) | ((i >> 7) << 2)) * 32 + m, acc);
+        }
+      }
+    }
+  } else if (DMC == 4) {
+    // every subspace spans 4 dimensions starting at a multiple of 4: the
+    // residual slice of each query is one aligned 16-byte load
+    const float4 *b4 = reinterpret_cast<const float4 *>(book);
+    for (int i0 = threadIdx.x; i0 < MK; i0 += 8 * blockDim.x) {
+      float4 cv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + u * blockDim.x;
+        if (i < MK) {
+          int m, j, slot;
+          entry_of(i, m, j, slot);
+          cv[u] = __ldg(b4 + m * K + j);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + u * blockDim.x;
+        if (i < MK) {
+          int m, j, slot;
+          entry_of(i, m, j, slot);
+          const int zo = sbs[m];
           float acc[G];
 #pragma unroll
           for (int g = 0; g < G; ++g) {
@@ -767,14 +844,16 @@ __device__ __forceinline__ void lut_build_g(const float *book, const float *zq, 
             a = dist_op<MT>(a, z.z, cv[u].z);
             acc[g] = dist_op<MT>(a, z.w, cv[u].w);
           }
-          lut_store_g<G, MT>(lut, e, acc);
+          lut_store_g<G, MT>(lut, slot, acc);
         }
       }
     }
   } else {
-    for (int e = threadIdx.x; e < MK; e += blockDim.x) {
-      const int m = e >> kbits, len = sls[m];
-      const float *cj = book + (int64_t)e * dm;
+    for (int i = threadIdx.x; i < MK; i += blockDim.x) {
+      int m, j, slot;
+      entry_of(i, m, j, slot);
+      const int len = sls[m];
+      const float *cj = book + (int64_t)(m * K + j) * dm;
       float acc[G];
 #pragma unroll
       for (int g = 0; g < G; ++g) {
@@ -783,7 +862,7 @@ __device__ __forceinline__ void lut_build_g(const float *book, const float *zq, 
         for (int t = 0; t < len; ++t) a = dist_op<MT>(a, z[t], __ldg(cj + t));
         acc[g] = a;
       }
-      lut_store_g<G, MT>(lut, e, acc);
+      lut_store_g<G, MT>(lut, slot, acc);
     }
   }
 }
@@ -1064,14 +1143,16 @@ __global__ void __launch_bounds__(kAdcThreads, 1) adc_group_kernel(
     }
     __syncthreads();
     const float *book = books + (int64_t)c * M * K * dm;
+    // 32-byte code rows and 256 centroids: the skewed scan reads a code-major LUT
+    const bool tr = VB == 16 && M == 32 && K == 256;
     if (mt == M_L2 && aligned4)
-      lut_build_g<G, M_L2, 4>(book, zq, dz, sbs, sls, M * K, kbits, dm, lut);
+      lut_build_g<G, M_L2, 4>(book, zq, dz, sbs, sls, M, K, kbits, dm, tr, lut);
     else if (mt == M_L2)
-      lut_build_g<G, M_L2, 0>(book, zq, dz, sbs, sls, M * K, kbits, dm, lut);
+      lut_build_g<G, M_L2, 0>(book, zq, dz, sbs, sls, M, K, kbits, dm, tr, lut);
     else if (mt == M_L1)
-      lut_build_g<G, M_L1, 0>(book, zq, dz, sbs, sls, M * K, kbits, dm, lut);
+      lut_build_g<G, M_L1, 0>(book, zq, dz, sbs, sls, M, K, kbits, dm, tr, lut);
     else
-      lut_build_g<G, M_IP, 0>(book, zq, dz, sbs, sls, M * K, kbits, dm, lut);
+      lut_build_g<G, M_IP, 0>(book, zq, dz, sbs, sls, M, K, kbits, dm, tr, lut);
     const uint8_t *lcodes = codes + lrow * M;
     int held = 0;
     for (int64_t c0 = 0; c0 < L; c0 += kAdcChunk) {
@@ -1117,7 +1198,7 @@ __global__ void __launch_bounds__(kAdcThreads, 1) adc_group_kernel(
             nrow = items[lrow + c0 + in];
           }
           float d[G];
-          adc_row32_g<G>(w0, w1, lut, d);
+          adc_row32_skew_g<G>(w0, w1, lut, threadIdx.x & 7, d);
           crow[i] = row;
 #pragma unroll
           for (int g = 0; g < G; ++g) {
