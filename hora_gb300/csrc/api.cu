@@ -568,6 +568,8 @@ int hora_idx_info(const hora_index *h, char *buf, uint64_t cap) {
   s += ",\"last_search_ms\":" + std::to_string(h->last_ms.load());
   s += ",\"last_overflow_rescans\":" + std::to_string(h->last_retries.load());
   s += ",\"last_threshold_probe\":" + std::to_string(h->last_probe.load());
+  s += ",\"last_overflow_queries\":" + std::to_string(h->last_overflow_queries.load());
+  s += ",\"last_short_lists\":" + std::to_string(h->last_short_lists.load());
   s += ",\"last_fallback_queries\":" + std::to_string(h->last_fallback.load());
   if (h->kind != HORA_INDEX_BRUTE_FORCE) {
     std::string iv;

@@ -225,14 +225,16 @@ int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint
 constexpr int kRrMaxWarps = 8, kRrSlab = 64;
 // With count, query q's list holds min(count[q], R) keys (the rest of its R
 // slots are neither read nor written); in and outk may be the same buffer.
+// With order, CTA b takes query order[b] (a permutation of the queries):
+// queries whose candidates share rows run side by side and meet them in L2.
 template <int MT>
 __global__ void __launch_bounds__(kRrMaxWarps * 32) rerank_exact_kernel(
     const float *Q, int64_t ld, const float *X, int64_t dim, const float *qnorm, const float *xnorm,
-    const uint64_t *in, int R, const uint32_t *count, uint64_t *outk) {
+    const uint64_t *in, int R, const uint32_t *count, const uint32_t *order, uint64_t *outk) {
   extern __shared__ float rr_smem[];  // per warp a 32 x (kRrSlab + 1) tile, then the query row
   const int nw = blockDim.x >> 5;
   float *qs = rr_smem + nw * 32 * (kRrSlab + 1);
-  const int64_t q = blockIdx.x;
+  const int64_t q = order ? (int64_t)order[blockIdx.x] : (int64_t)blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int64_t t = threadIdx.x; t < ld; t += blockDim.x) qs[t] = Q[q * ld + t];
   __syncthreads();
@@ -287,7 +289,7 @@ __global__ void __launch_bounds__(kRrMaxWarps * 32) rerank_exact_kernel(
 
 int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, int64_t dim,
                         const float *qnorm, const float *xnorm, const uint64_t *in, int64_t nq,
-                        int R, uint64_t *out, cudaStream_t s, const uint32_t *count) {
+                        int R, uint64_t *out, cudaStream_t s, const uint32_t *count, const uint32_t *order) {
   if (nq <= 0) return HORA_OK;
   if (ld % 4) return fail(HORA_EINVAL, "rerank: pitch not a multiple of 4");
   ProfScope ps("rerank_exact", s);
@@ -302,10 +304,10 @@ int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, 
   HORA_SMEM_ATTR(rerank_exact_kernel<M_IP>, qb);
   HORA_SMEM_ATTR(rerank_exact_kernel<M_COS>, qb);
   switch (metric) {
-    case M_L2: rerank_exact_kernel<M_L2><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, out); break;
-    case M_L1: rerank_exact_kernel<M_L1><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, out); break;
-    case M_IP: rerank_exact_kernel<M_IP><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, out); break;
-    case M_COS: rerank_exact_kernel<M_COS><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, out); break;
+    case M_L2: rerank_exact_kernel<M_L2><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, order, out); break;
+    case M_L1: rerank_exact_kernel<M_L1><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, order, out); break;
+    case M_IP: rerank_exact_kernel<M_IP><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, order, out); break;
+    case M_COS: rerank_exact_kernel<M_COS><<<g, T, qb, s>>>(Q, ld, X, dim, qnorm, xnorm, in, R, count, order, out); break;
     default: return fail(HORA_EMETRIC, "unknown method");
   }
   HORA_LAUNCHED();

@@ -63,6 +63,15 @@ constexpr int kLpHitBytes = kLpHitBuf * kLpEpiThreads * 8;
 // the MMA descriptors read), then for BF16 Euclidean the two 8-column halves
 // of the norm block (256 rows x 16 bytes each, unswizzled).  One bulk copy
 // moves a whole tile into a ring stage; rows past n are zero.
+// Base rows gathered into a tile image of the base's layout and precision
+// (converted by the same kernels, so every value equals the base image's),
+// with the per-row values the scan's drain reads (exact squared norms, e4m3
+// scales, norms); padding rows are zero.
+struct RowImage {
+  DevBuf tiles, xsq, xscale, xnorm;
+  int64_t rows = 0;  // a multiple of the tile
+};
+
 struct LowpState {
   int prec = 0, metric = 0;
   int64_t n = 0, Dp = 0;
@@ -80,6 +89,13 @@ struct LowpState {
   DevBuf ctiles;   // the pivots' BF16 tile image (the BF16 base's layout, also for an FP8 base)
   int64_t ctile_bytes = 0;
   int cnkb = 0;    // the pivot image's 128-byte K blocks
+  // the members' image: cluster c's first min(members, kProbeMaxMembers)
+  // rows from image row moff[c] (a multiple of the tile)
+  RowImage members;
+  DevBuf moff;
+  // the sample image: base rows floor(frac(j phi) n), j = 1, 2, ... (any
+  // prefix spread over the base), for wide R-best lists
+  RowImage sample;
   // BF16 Euclidean: the largest |x - bf16(x)| over the rows (1 f32, rounded
   // up), the rows' share of the certified exact search's error bound
   DevBuf dxmax;
@@ -105,6 +121,14 @@ struct LpParams {
   int dense_hits;  // hit-dense launch: the warp-converged staging (stage_hits)
   int tpc;         // base tiles per CTA (lp_tiles_per_cta)
   const float *tau0;  // per query starting distance threshold (filter mode), or null
+  // work items instead of the (query block, row chunk) grid: CTA b takes
+  // items[b] = {first query row, query rows, first image row (a multiple of
+  // the tile), columns}, for b < *n_items
+  const int4 *items;
+  const int *n_items;
+  // TILE_DIST: distances out_dist[query row * ldo + column]
+  float *out_dist;
+  int64_t ldo;
 };
 
 // BF16 Euclidean folds the row norm into the MMA: one extra K = 16 step
@@ -197,6 +221,25 @@ __device__ __forceinline__ void flush_hits(const DrainCtx &c, int &nb) {
   for (int i = 0; i < nb; ++i, ++slot)
     if (slot < (uint32_t)c.cap) out[slot] = c.hb[i * kLpEpiThreads];
   nb = 0;
+}
+
+// TILE_DIST: a slice's 32 distances to the query's output row (orow is
+// indexed by image row; 16-byte stores for a whole slice: the row's
+// columns start a multiple of 32 into a 16-byte aligned row).
+template <int MT, bool RAW>
+__device__ __forceinline__ void store_dist(const uint32_t (&v)[32], const DrainCtx &c, float *orow) {
+  float *o = orow + c.rt;
+  if (c.rt + 32 <= c.r_end) {
+#pragma unroll
+    for (int j = 0; j < 32; j += 4)
+      *reinterpret_cast<float4 *>(o + j) =
+          make_float4(drain_dist<MT, TILE_DIST, RAW>(v[j], c.qa), drain_dist<MT, TILE_DIST, RAW>(v[j + 1], c.qa),
+                      drain_dist<MT, TILE_DIST, RAW>(v[j + 2], c.qa), drain_dist<MT, TILE_DIST, RAW>(v[j + 3], c.qa));
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+      if (c.rt + j < c.r_end) o[j] = drain_dist<MT, TILE_DIST, RAW>(v[j], c.qa);
+  }
 }
 
 template <int MT, int MODE, bool RAW>
@@ -313,10 +356,23 @@ __global__ void __launch_bounds__(kLpThreads, 1)
   volatile int *abort = reinterpret_cast<volatile int *>(done + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t q0 = (int64_t)blockIdx.x * kLpBM;
-  const int64_t row0 = p.r_begin + (int64_t)blockIdx.y * kLpBN * p.tpc;
-  const int64_t rows_here = p.r_end - row0;
-  const int T = (int)std::min<int64_t>(p.tpc, (rows_here + kLpBN - 1) / kLpBN);
+  int64_t q0, row0, r_end;
+  int T, nqv;  // tiles, query rows of the block
+  if (p.items) {
+    if ((int)blockIdx.x >= *p.n_items) return;  // the grid is an upper bound
+    const int4 it = p.items[blockIdx.x];
+    q0 = it.x;
+    nqv = it.y;
+    row0 = it.z;
+    r_end = row0 + it.w;
+    T = (it.w + kLpBN - 1) / kLpBN;
+  } else {
+    q0 = (int64_t)blockIdx.x * kLpBM;
+    nqv = kLpBM;
+    row0 = p.r_begin + (int64_t)blockIdx.y * kLpBN * p.tpc;
+    r_end = p.r_end;
+    T = (int)std::min<int64_t>(p.tpc, (r_end - row0 + kLpBN - 1) / kLpBN);
+  }
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -436,7 +492,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     const int h = (warp - 2) >> 2;    // column quarter (32 columns)
     const int m = g * 32 + lane;      // query row in the tile
     const int64_t qrow = q0 + m;
-    const int64_t qid = qrow < p.nq ? (p.qmap ? p.qmap[qrow] : qrow) : -1;
+    const int64_t qid = qrow < p.nq && m < nqv ? (p.qmap ? p.qmap[qrow] : qrow) : -1;
     float qa = 0.0f, qs = 1.0f;
     if (qid >= 0) {
       if (MT == M_L2) qa = p.qsq[qid];
@@ -473,7 +529,8 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     }
     uint64_t *hbuf = reinterpret_cast<uint64_t *>(bars + kLpBarSlots);
     uint64_t amin = kEmptyKey;  // TILE_ARGMIN: this thread's smallest key so far
-    DrainCtx c{p.cand, p.count, hbuf + (threadIdx.x - 64), qid, 0, p.r_begin, p.r_end, p.cap, qa, tau_d, tau_r};
+    DrainCtx c{p.cand, p.count, hbuf + (threadIdx.x - 64), qid, 0, p.r_begin, r_end, p.cap, qa, tau_d, tau_r};
+    float *orow = MODE == TILE_DIST && qid >= 0 ? p.out_dist + qrow * p.ldo - row0 : nullptr;
     int nb = 0;  // keys staged in this thread's column
     for (int t = 0; t < T; ++t) {
       const int b = t % kLpNB, jb = t / kLpNB;
@@ -493,8 +550,8 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       if (!FAST) {
         const int64_t r = c.rt + lane;
         const float *va = MT == M_L2 ? p.xsq : (MT == M_COS ? p.xnorm : nullptr);
-        if (va) xa = r < p.r_end ? __ldg(va + r) : 0.0f;
-        if (PREC == HORA_PREC_FP8) xs = r < p.r_end ? __ldg(p.xscale + r) : 0.0f;
+        if (va) xa = r < r_end ? __ldg(va + r) : 0.0f;
+        if (PREC == HORA_PREC_FP8) xs = r < r_end ? __ldg(p.xscale + r) : 0.0f;
       }
       uint32_t v[32];
       tc::tmem_ld32(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + (h * kLpSlices + sl) * 32), v);
@@ -525,6 +582,8 @@ __global__ void __launch_bounds__(kLpThreads, 1)
           }
         } else if constexpr (MODE == TILE_DENSE) {
           if (qid >= 0) drain_mask<MT, MODE, true>(v, 0xffffffffu, c, nb);
+        } else if constexpr (MODE == TILE_DIST) {
+          if (qid >= 0) store_dist<MT, true>(v, c, orow);
         } else {
           // the slice's extreme decides whether any column can hit; the
           // hit mask is built only then (padded query rows never hit)
@@ -573,8 +632,12 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         v[j] = __float_as_uint(d);
         hits |= (uint32_t)(d <= tau_d) << j;
       }
-      if (MODE == TILE_DENSE) hits = 0xffffffffu;
-      if (qid >= 0 && hits) drain_mask<MT, MODE, false>(v, hits, c, nb);
+      if constexpr (MODE == TILE_DIST) {
+        if (qid >= 0) store_dist<MT, false>(v, c, orow);
+      } else {
+        if (MODE == TILE_DENSE) hits = 0xffffffffu;
+        if (qid >= 0 && hits) drain_mask<MT, MODE, false>(v, hits, c, nb);
+      }
       }
     }
     if (qid >= 0 && nb > 0) flush_hits(c, nb);
@@ -667,229 +730,196 @@ __global__ void gather_rows_u8_kernel(const uint8_t *src, int64_t row_bytes, con
   for (int64_t t = threadIdx.x; t < row_bytes; t += blockDim.x) dst[r * row_bytes + t] = s[t];
 }
 
-// ---- starting thresholds from pivot clusters (BF16 Euclidean) ---------------------------
+// ---- starting thresholds ------------------------------------------------------------
 // With a threshold that starts at the R-th key of the rows scanned so far,
 // the chunked schedule keeps about R x ln(n / first chunk) rows per query
 // (~1,500 on 1M rows, R = 132), and the drain's hit handling is the largest
 // cost of the scan after the MMAs.  A base of at least kProbeMinRows rows
-// therefore keeps ~n / 1,024 pivot clusters (a few Lloyd steps from evenly
-// spaced rows).  Before the scan every query goes to its nearest pivot and
-// is scored against up to kProbeMaxMembers rows of that cluster with the
-// scan's own arithmetic (BF16 operands, exact products, f32 sums, the
-// folded norm).  Its starting threshold is the R-th of those distances plus
-// a bound on what the different summation order can change; one filter pass
-// over the base then keeps every row at or below it.  A query that kept at
-// least R rows has its R-best set complete: R rows at or below the
-// threshold put its R-th key there, and every key up to that one was kept.
-// A query that kept fewer (the bound did not hold, or its cluster had fewer
-// than R members) is answered again by the chunked schedule.
+// therefore gives every query a starting threshold before one filter pass
+// over the whole base.  A query that kept at least R rows has its R-best set
+// complete: R rows at or below the threshold put its R-th key there, and
+// every key up to that one was kept.  A query that kept fewer is answered
+// again by the chunked schedule.  So the threshold only decides the cost.
+//
+// Up to R = kProbeClusterMaxR the threshold is a bound.  The base keeps
+// ~n / 1,024 pivot clusters (a few Lloyd steps from evenly spaced rows;
+// clusters below kProbeMinCluster members dissolved, empty ones dropped).
+// Every query goes to its nearest pivot in the index's own metric (a BF16
+// pass over the pivots' image: Euclidean with the norm folded in,
+// CosineSimilarity on unit pivots, DotProduct ascending +<q, c>) and is
+// scored against up to kProbeMaxMembers rows of that cluster by the scan
+// kernel itself: the members' rows are kept as a second tile image (each
+// cluster's first kProbeMaxMembers members, every cluster starting on a
+// tile, converted exactly as the base's image), the queries are gathered in
+// pivot order, and one CTA per (pivot, up to 128 of its queries) writes the
+// keys of those members (TILE_DIST): the same operands, MMAs and key formula
+// as the scan.  The threshold is the R-th of those keys plus a bound
+// covering any difference in summation order; a cluster holds at least
+// kProbeMinCluster >= R rows, so no list comes out short.
+//
+// Wider lists (up to kProbeMaxR) take a sampled threshold instead
+// (sample_threshold): the R best rows of a large base are often thin tails
+// of many clusters, so the R-th key of one cluster's members lies far above
+// the base's R-th key.
 constexpr int64_t kProbeRowsPerPivot = 1024;
 constexpr int64_t kProbeMinRows = 65536;
-constexpr int kProbeMaxMembers = 1024;  // members a query is scored against
-constexpr int kProbeMaxR = 256;         // widest R-best list the probe serves
+constexpr int kProbeMaxMembers = 1024;  // members of a cluster a query is scored against
+constexpr int kProbeClusterMaxR = 256;  // widest R-best list with a cluster threshold
+constexpr int kProbeMaxR = 4096;        // widest R-best list with a sampled threshold
 constexpr int kExactTcMaxK = 256;       // largest k of the certified exact search
 constexpr int kProbeMinCluster = 256;   // smaller clusters are dissolved at the end
 constexpr int kProbeReseed = 128;       // Lloyd steps re-seed clusters below this
 constexpr int kProbeLloyd = 6;
-constexpr int kProbeQ = 32;       // queries per pass of a probe CTA
-constexpr int kProbeRows = 128;   // member rows per shared-memory tile
-constexpr int kProbePitch = 132;  // f32 pitch of a staged row (spreads the banks)
-constexpr int kProbeSmem = (kProbeQ + kProbeRows) * kProbePitch * 4 + kProbeMaxMembers * 12;
+constexpr int64_t kProbeSampleRows = 262144;  // rows of the sample image at most
+static_assert(kProbeMinCluster >= kProbeClusterMaxR, "a cluster must hold the widest clustered R-best list");
 
-__device__ __forceinline__ void bf16x8_to_f32(const uint4 &v, float *out) {
-  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    out[2 * i] = __uint_as_float(w[i] << 16);
-    out[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
-  }
-}
-
-// The 16 e4m3 values of a 16-byte chunk as f32 (through the library's
-// FP8 -> half conversion, exact).
-__device__ __forceinline__ void e4m3x16_to_f32(const uint4 &v, float *out) {
-  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    const __nv_fp8_storage_t b = (__nv_fp8_storage_t)((w[i >> 2] >> (8 * (i & 3))) & 0xffu);
-    out[i] = __half2float(__half(__nv_cvt_fp8_to_halfraw(b, __NV_E4M3)));
-  }
-}
-
-// Elements per 16-byte chunk of a row: 8 BF16 values or 16 e4m3 values.
-template <bool FP8>
-__device__ __forceinline__ void chunk_to_f32(const uint4 &v, float *out) {
-  if (FP8) e4m3x16_to_f32(v, out); else bf16x8_to_f32(v, out);
-}
-
-// The 16-byte chunks of member rows mt.. (kProbeRows of them) that thread t
-// stages: chunk i = t + 256 u is row i / nch, chunk i % nch.
-__device__ __forceinline__ void probe_load_tile(uint4 (&buf)[8], const uint32_t *ids, int mt, int L, int nch, int t,
-                                                const uint8_t *tiles, int64_t tile_bytes) {
-#pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    const int i = t + 256 * u, j = i / nch, ch = i % nch;
-    buf[u] = make_uint4(0u, 0u, 0u, 0u);
-    if (i < kProbeRows * nch && mt + j < L) {
-      const uint32_t r = ids[mt + j];
-      const int rr = (int)(r % kLpBN), kb = ch >> 3, cc = ch & 7;
-      buf[u] = *reinterpret_cast<const uint4 *>(tiles + (int64_t)(r / kLpBN) * tile_bytes + kb * (kLpBN * 128) +
-                                                rr * 128 + ((cc ^ (rr & 7)) * 16));
-    }
-  }
-}
-
-// One CTA per work item: up to kProbeQ of one pivot's queries against its
-// first kProbeMaxMembers member rows, read from the tile image.  Thread (qg, rg)
-// of the 8 x 32 layout scores queries qg + 8i against rows rg + 32j, the
-// products summed over ascending dimensions with one f32 FMA each, then the
-// scan's distance formed from the sum: BF16 (norm folded) qsq - 2 (sum +
-// (-|x|^2 / 2)); FP8 (per-row scales) qsq + |x|^2 - 2 sum (qscale xscale).
-template <bool FP8>
-__global__ void __launch_bounds__(256) probe_dist_kernel(const uint8_t *tiles, int64_t tile_bytes,
-                                                         const float *xsq, const float *xscale,
-                                                         const int64_t *coff, const uint32_t *cmem,
-                                                         const uint8_t *lq, const float *lqscale,
-                                                         int64_t Dp, const float *qsq, const int64_t *qoff,
-                                                         const uint32_t *qmem, const int *item_off, int C,
-                                                         float *pdist) {
-  extern __shared__ __align__(16) float psm[];
-  float *qs = psm;                           // kProbeQ x kProbePitch
-  float *xs = qs + kProbeQ * kProbePitch;    // kProbeRows x kProbePitch
-  float *xh = xs + kProbeRows * kProbePitch;                       // per member: -|x|^2 / 2 (FP8: |x|^2)
-  float *xc = xh + kProbeMaxMembers;                               // per member: its scale (FP8)
-  uint32_t *ids = reinterpret_cast<uint32_t *>(xc + kProbeMaxMembers);  // per member: its row
-  constexpr int kPer = FP8 ? 16 : 8;  // elements per 16-byte chunk
-  constexpr int esz = FP8 ? 1 : 2;
-  // work item blockIdx.x: batch (item - item_off[c]) of pivot c's queries
-  const int b = blockIdx.x;
-  if (b >= item_off[C]) return;
-  int lo = 0, hi = C;  // the last c with item_off[c] <= b
+// Row i of the members' image: the base row of member i - moff[c] of the
+// cluster c whose image rows hold i, or none (0xffffffff) past its first
+// min(members, kProbeMaxMembers) members.
+__global__ void member_rows_kernel(const int64_t *coff, const uint32_t *cmem, const int64_t *moff, int C,
+                                   int64_t nimg, uint32_t *mrow) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nimg) return;
+  int lo = 0, hi = C;  // the last c with moff[c] <= i
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
-    if (item_off[mid] <= b) lo = mid; else hi = mid;
+    if (moff[mid] <= i) lo = mid; else hi = mid;
   }
-  const int c = lo;
-  const int64_t q_lo = qoff[c], nqc = qoff[c + 1] - q_lo;
-  const int64_t m_lo = coff[c];
-  const int L = (int)(coff[c + 1] - m_lo < kProbeMaxMembers ? coff[c + 1] - m_lo : kProbeMaxMembers);
-  const int t = threadIdx.x, qg = t & 7, rg = t >> 3;
-  const int D = (int)Dp, nch = D / kPer;
-  {
-    const int64_t qb = (int64_t)(b - item_off[c]) * kProbeQ;
-    const int nb = (int)(nqc - qb < kProbeQ ? nqc - qb : kProbeQ);
-    const int ni = (nb + 7) >> 3;  // query slots in use per thread (CTA-uniform)
-    for (int j = t; j < L; j += 256) {
-      const uint32_t r = cmem[m_lo + j];
-      ids[j] = r;
-      xh[j] = FP8 ? xsq[r] : -0.5f * xsq[r];
-      xc[j] = FP8 ? xscale[r] : 1.0f;
+  const int64_t j = i - moff[lo], cnt = coff[lo + 1] - coff[lo];
+  mrow[i] = j < cnt && j < kProbeMaxMembers ? cmem[coff[lo] + j] : 0xffffffffu;
+}
+
+// Sample image rows: j < m holds base row floor(frac((j + 1) phi) n) (phi
+// the golden ratio: every prefix is spread evenly over the rows), the rest
+// padding.
+__global__ void sample_rows_kernel(int64_t n, int64_t m, int64_t ns, uint32_t *rowmap) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ns) return;
+  if (j >= m) {
+    rowmap[j] = 0xffffffffu;
+    return;
+  }
+  const double f = (double)(j + 1) * 0.6180339887498949;
+  const int64_t r = (int64_t)((f - floor(f)) * (double)n);
+  rowmap[j] = (uint32_t)(r < n ? r : n - 1);
+}
+
+// FP32 rows (pitch ld) and per-row values of the members' image rows (zero
+// for padding rows); any output may be null.
+__global__ void gather_members_kernel(const float *X, int64_t ld, const uint32_t *mrow, int64_t nimg,
+                                      const double *sq64, const float *xsq, const float *xnorm, float *rows,
+                                      double *sq64_out, float *xsq_out, float *xnorm_out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nimg * ld) return;
+  const int64_t r = i / ld, t = i % ld;
+  const uint32_t b = mrow[r];
+  rows[i] = b == 0xffffffffu ? 0.0f : X[(int64_t)b * ld + t];
+  if (t == 0) {
+    if (sq64_out) sq64_out[r] = b == 0xffffffffu ? 0.0 : sq64[b];
+    if (xsq_out) xsq_out[r] = b == 0xffffffffu ? 0.0f : xsq[b];
+    if (xnorm_out) xnorm_out[r] = b == 0xffffffffu ? 0.0f : xnorm[b];
+  }
+}
+
+// Probe work items, one CTA of 1,024 threads (C <= 4,096): pivot c with
+// pairs qoff[c]..qoff[c+1] (in pivot order) owns ceil(pairs / 128) items
+// {first pair, pairs, first image row moff[c], min(members, kProbeMaxMembers)}.
+__global__ void probe_items_kernel(const int64_t *qoff, const int64_t *coff, const int64_t *moff, int C,
+                                   int4 *items, int *n_items) {
+  __shared__ int part[1024];
+  const int t = threadIdx.x, per = (C + 1023) / 1024;
+  const int lo = min(C, t * per), hi = min(C, lo + per);
+  int s = 0;
+  for (int c = lo; c < hi; ++c) s += (int)((qoff[c + 1] - qoff[c] + kLpBM - 1) / kLpBM);
+  part[t] = s;
+  __syncthreads();
+  if (t == 0) {
+    int run = 0;
+    for (int i = 0; i < 1024; ++i) {
+      const int v = part[i];
+      part[i] = run;
+      run += v;
     }
-    for (int i = t; i < kProbeQ * nch; i += 256) {
-      const int qi = i / nch, ch = i % nch;
-      float f[16];
-#pragma unroll
-      for (int e = 0; e < kPer; ++e) f[e] = 0.0f;
-      if (qi < nb) {
-        const uint32_t qid = qmem[q_lo + qb + qi];
-        chunk_to_f32<FP8>(*reinterpret_cast<const uint4 *>(lq + ((int64_t)qid * Dp + ch * kPer) * esz), f);
-      }
-      float4 *dst = reinterpret_cast<float4 *>(qs + qi * kProbePitch + ch * kPer);
-#pragma unroll
-      for (int e = 0; e < kPer / 4; ++e) dst[e] = make_float4(f[4 * e], f[4 * e + 1], f[4 * e + 2], f[4 * e + 3]);
-    }
-    __syncthreads();  // member rows and queries staged
-    // a tile's 16-byte chunks in registers: the next tile's loads are in
-    // flight while the current one is scored
-    uint4 buf[8];
-    probe_load_tile(buf, ids, 0, L, nch, t, tiles, tile_bytes);
-    for (int mt = 0; mt < L; mt += kProbeRows) {
-      if (mt > 0) __syncthreads();  // the previous tile consumed
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int i = t + 256 * u, j = i / nch, ch = i % nch;
-        if (i < kProbeRows * nch) {
-          float f[16];
-          chunk_to_f32<FP8>(buf[u], f);
-          float4 *dst = reinterpret_cast<float4 *>(xs + j * kProbePitch + ch * kPer);
-#pragma unroll
-          for (int e = 0; e < kPer / 4; ++e) dst[e] = make_float4(f[4 * e], f[4 * e + 1], f[4 * e + 2], f[4 * e + 3]);
-        }
-      }
-      __syncthreads();
-      if (mt + kProbeRows < L) probe_load_tile(buf, ids, mt + kProbeRows, L, nch, t, tiles, tile_bytes);
-      float acc[4][4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
-#pragma unroll 2
-      for (int d = 0; d < D; d += 4) {
-        float4 xv[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) xv[j] = *reinterpret_cast<const float4 *>(xs + (rg + 32 * j) * kProbePitch + d);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          if (i < ni) {
-            const float4 qv = *reinterpret_cast<const float4 *>(qs + (qg + 8 * i) * kProbePitch + d);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              acc[i][j] = fmaf(qv.x, xv[j].x, acc[i][j]);
-              acc[i][j] = fmaf(qv.y, xv[j].y, acc[i][j]);
-              acc[i][j] = fmaf(qv.z, xv[j].z, acc[i][j]);
-              acc[i][j] = fmaf(qv.w, xv[j].w, acc[i][j]);
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int qi = qg + 8 * i;
-        if (i >= ni || qi >= nb) continue;
-        const uint32_t qid = qmem[q_lo + qb + qi];
-        const float qa = qsq[qid];
-        const float qsc = FP8 ? lqscale[qid] : 1.0f;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int m = mt + rg + 32 * j;
-          if (m < L)
-            pdist[(int64_t)qid * kProbeMaxMembers + m] =
-                FP8 ? fmaf(-2.0f, acc[i][j] * (qsc * xc[m]), qa + xh[m]) : fmaf(-2.0f, acc[i][j] + xh[m], qa);
-        }
-      }
+    *n_items = run;
+  }
+  __syncthreads();
+  int run = part[t];
+  for (int c = lo; c < hi; ++c) {
+    const int64_t cnt = coff[c + 1] - coff[c];
+    const int cols = (int)(cnt < kProbeMaxMembers ? cnt : kProbeMaxMembers);
+    for (int64_t q = qoff[c]; q < qoff[c + 1]; q += kLpBM) {
+      const int nb = (int)(qoff[c + 1] - q < kLpBM ? qoff[c + 1] - q : kLpBM);
+      items[run++] = make_int4((int)q, nb, (int)moff[c], cols);
     }
   }
 }
 
-// One warp per query: the R-th smallest probe distance by a 32-step bitwise
-// descent over the ordered encoding, plus the summation-order bound
-// 1e-4 (|q|^2 + max |x|^2).  Both sums add the same exact BF16 products
-// (<= |q||x| + |x|^2 / 2 in magnitude, <= |q|^2 / 2 + max|x|^2) in f32; each
-// is within 144 x 2^-24 of that magnitude, so the distances (2 x the sum)
-// differ by less than 3.5e-5 of it.  A cluster with fewer than R members
-// gives -FLT_MAX: the scan keeps nothing and the query is rescheduled.
-__global__ void probe_select_kernel(const uint64_t *pkeys, const int64_t *coff, const float *pdist,
-                                    const float *qsq, const float *xsqmax, int64_t nq, int R,
-                                    const float *slack, float *tau) {
+// The inverse of a permutation: pos_of[perm[i]] = i.
+__global__ void inverse_kernel(const uint32_t *perm, int64_t n, uint32_t *pos_of) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) pos_of[perm[i]] = (uint32_t)i;
+}
+
+// The summation-order bound added to a probed threshold.  The probe and the
+// scan add the same exact products (BF16 x BF16, or e4m3 x e4m3 before the
+// scales) in f32 in different orders; each sum is within (Dp + 16) 2^-24 of
+// the sum of the products' magnitudes.  Euclidean (norm folded: <= |q||x| +
+// |x|^2 / 2 <= |q|^2 / 2 + max|x|^2) and DotProduct (<= |q||x|) keys are 2 x
+// or 1 x such a sum: they differ by less than 3.5e-5 (|q|^2 + max|x|^2),
+// and 1e-4 of it is taken.  CosineSimilarity keys are a sum of unit rows'
+// products (or one divided by |q||x|): at most 1 in magnitude, 2e-4 taken.
+__device__ __forceinline__ float probe_bound(int metric, float qsq, float xsqmax) {
+  return metric == M_COS ? 2e-4f : 1e-4f * (qsq + xsqmax);
+}
+
+// The probed threshold from the upper bound a of the R-th key (ordered
+// bits): the bound above, and for the certified exact search its slack (and
+// a relative 2^-20 against the rounding of these f32 additions).
+__device__ __forceinline__ float probe_tau(uint32_t a, int metric, float qsq, float xsqmax, const float *slack,
+                                           int64_t q) {
+  float t = ord2f(a) + probe_bound(metric, qsq, xsqmax);
+  if (slack) t = t + slack[q] + 0x1p-20f * fabsf(t + slack[q]);
+  return t;
+}
+
+// The descent stops kSelectSkip bits short of the R-th value's ordered
+// encoding and rounds up: an upper bound within 2^-(23 - kSelectSkip) of
+// it, which is all a threshold needs.
+constexpr int kSelectSkip = 12;
+
+// Members of the cluster of pivot key pk scored for a query (0 for an
+// empty key).
+__device__ __forceinline__ int probe_members(uint64_t pk, const int64_t *coff, int C) {
+  const uint32_t c = key_row(pk);
+  if (pk == kEmptyKey || c >= (uint32_t)C) return 0;
+  const int64_t L = coff[c + 1] - coff[c];
+  return (int)(L < kProbeMaxMembers ? L : kProbeMaxMembers);
+}
+
+// One cluster per query, one warp per query: the R-th smallest probe key
+// by a bitwise descent over the ordered encoding, plus probe_bound.  The
+// keys of pair (q, p) are row pos_of[q P + p] of pdist.  A cluster with
+// fewer than R members gives -FLT_MAX: the scan keeps nothing and the query
+// is rescheduled.
+__global__ void probe_select_kernel(const uint64_t *pkeys, const int64_t *coff, int C, const float *pdist,
+                                    const uint32_t *pos_of, const float *qsq, const float *xsqmax, int metric,
+                                    int64_t nq, int R, const float *slack, float *tau) {
   const int64_t q = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (q >= nq) return;
-  const uint32_t c = key_row(pkeys[q]);
-  const int L = (int)(coff[c + 1] - coff[c] < kProbeMaxMembers ? coff[c + 1] - coff[c] : kProbeMaxMembers);
+  const int L = probe_members(pkeys[q], coff, C);
   if (L < R) {
     if (lane == 0) tau[q] = -FLT_MAX;
     return;
   }
+  const float *pq = pdist + (int64_t)pos_of[q] * kProbeMaxMembers;
   uint32_t v[kProbeMaxMembers / 32];
 #pragma unroll
   for (int i = 0; i < kProbeMaxMembers / 32; ++i) {
     const int m = lane + 32 * i;
-    v[i] = m < L ? f2ord(pdist[q * kProbeMaxMembers + m]) : 0xffffffffu;
+    v[i] = m < L ? f2ord(pq[m]) : 0xffffffffu;
   }
-  // the largest a with fewer than R values below it is the R-th smallest;
-  // the descent stops kSelectSkip bits short and rounds up (an upper bound
-  // within 2^-(23 - kSelectSkip) of the value, which is all a threshold needs)
-  constexpr int kSelectSkip = 12;
+  // the largest a with fewer than R values below it is the R-th smallest
   uint32_t a = 0;
   for (int b = 31; b >= kSelectSkip; --b) {
     const uint32_t tt = a | (1u << b);
@@ -900,40 +930,25 @@ __global__ void probe_select_kernel(const uint64_t *pkeys, const int64_t *coff, 
     for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     if (cnt < R) a = tt;
   }
-  if (lane == 0) {
-    float t = ord2f(a | ((1u << kSelectSkip) - 1)) + 1e-4f * (qsq[q] + *xsqmax);
-    // the certified exact search widens it by its error bound (and by a
-    // relative 2^-20 against the rounding of these f32 additions)
-    if (slack) t = t + slack[q] + 0x1p-20f * fabsf(t + slack[q]);
-    tau[q] = t;
-  }
+  if (lane == 0) tau[q] = probe_tau(a | ((1u << kSelectSkip) - 1), metric, qsq[q], *xsqmax, slack, q);
 }
 
-// Probe work items: pivot c owns ceil(queries / kProbeQ) of them, from
-// item_off[c] (C + 1 offsets; one CTA of 1,024 threads, C <= 4,096).
-__global__ void probe_items_kernel(const int64_t *qoff, int C, int *item_off) {
-  __shared__ int part[1024];
-  const int t = threadIdx.x, per = (C + 1023) / 1024;
-  const int lo = min(C, t * per), hi = min(C, lo + per);
-  int s = 0;
-  for (int c = lo; c < hi; ++c) s += (int)((qoff[c + 1] - qoff[c] + kProbeQ - 1) / kProbeQ);
-  part[t] = s;
-  __syncthreads();
-  if (t == 0) {
-    int run = 0;
-    for (int i = 0; i < 1024; ++i) {
-      const int v = part[i];
-      part[i] = run;
-      run += v;
-    }
-    item_off[C] = run;
-  }
-  __syncthreads();
-  int run = part[t];
-  for (int c = lo; c < hi; ++c) {
-    item_off[c] = run;
-    run += (int)((qoff[c + 1] - qoff[c] + kProbeQ - 1) / kProbeQ);
-  }
+// A query left without a pivot key (no finite distance to any pivot) takes
+// the last pivot: any cluster gives a valid threshold, and every query is
+// bucketed, so the buckets order all of them.
+__global__ void fill_empty_pivot_kernel(uint64_t *pk, int64_t n, int C) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && pk[i] == kEmptyKey) pk[i] = make_key(__int_as_float(0x7f800000), (uint32_t)(C - 1));
+}
+
+// A query's threshold from the j-th key of its sorted sample list (first:
+// set, +inf when the list is shorter; else lowered when the key exists).
+__global__ void sample_tau_kernel(const uint64_t *best, int rs, int j, int64_t nq, bool first, float *tau) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const uint64_t kk = best[q * rs + (j - 1)];
+  const float t = kk == kEmptyKey ? __int_as_float(0x7f800000) : key_dist(kk);
+  tau[q] = first ? t : fminf(tau[q], t);
 }
 
 // Re-seeds centre dst[i] with base row cmem[src[i]] (all ld columns).
@@ -950,6 +965,33 @@ __global__ void reseed_kernel(const float *X, int64_t ld, const uint32_t *cmem, 
 __global__ void short_lists_kernel(const uint64_t *best, int R, int64_t nq, int *n, int *list) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < nq && best[q * R + (R - 1)] == kEmptyKey) list[atomicAdd(n, 1)] = (int)q;
+}
+
+// The windowed rerank's candidates: query q's keys (R slots of best) whose
+// distance is at most the k-th smallest key's plus slack[q] (and a relative
+// 2^-20 against the rounding of that f32 addition), moved to the front of
+// its R slots of out, their number to count[q].  One warp per query.
+__global__ void rerank_window_kernel(const uint64_t *best, int R, const uint64_t *kth, int k, const float *slack,
+                                     int64_t nq, uint64_t *out, uint32_t *count) {
+  const int64_t q = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  const uint64_t tk = kth[q * k + (k - 1)];
+  float w = __int_as_float(0x7f800000);
+  if (tk != kEmptyKey) {
+    const float t = key_dist(tk) + slack[q];
+    w = t + 0x1p-20f * fabsf(t);
+  }
+  uint32_t n = 0;
+  for (int i0 = 0; i0 < R; i0 += 32) {
+    const int i = i0 + lane;
+    const uint64_t key = i < R ? best[q * R + i] : kEmptyKey;
+    const bool keep = key != kEmptyKey && key_dist(key) <= w;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) out[q * R + n + __popc(m & ((1u << lane) - 1u))] = key;
+    n += __popc(m);
+  }
+  if (lane == 0) count[q] = n;
 }
 
 // Empties the R-best lists of the listed queries.
@@ -1071,6 +1113,43 @@ static int launch_lp(int prec, int metric, int mode, const CUtensorMap &ta, cons
                                 : launch_lp2<HORA_PREC_FP8>(metric, mode, ta, q, s);
 }
 
+// The pivot pass of the probed schedule: BF16 over the pivots' image, in
+// the index's metric, each query's nearest pivot (argmin mode).
+static int launch_pivot_pass(int metric, const CUtensorMap &ta, const LpParams &p, cudaStream_t s) {
+  switch (metric) {
+    case M_L2: return launch_lp3<HORA_PREC_BF16, M_L2, TILE_ARGMIN>(ta, p, s);
+    case M_IP: return launch_lp3<HORA_PREC_BF16, M_IP, TILE_ARGMIN>(ta, p, s);
+    case M_COS: return launch_lp3<HORA_PREC_BF16, M_COS, TILE_ARGMIN>(ta, p, s);
+  }
+  return fail(HORA_EMETRIC, "no tensor-core form for this metric");
+}
+
+// The probe's keys: the scan kernel over the members' image in TILE_DIST
+// mode, one CTA per work item (the grid an upper bound on their number).
+template <int PREC, int MT>
+static int launch_probe_items3(const CUtensorMap &ta, const LpParams &p, int max_items, cudaStream_t s) {
+  const int smem = lp_smem_bytes(p.nkb, p.stages, PREC == HORA_PREC_BF16 && MT == M_L2);
+  HORA_SMEM_ATTR((lowp_tile_kernel<PREC, MT, TILE_DIST>), smem);
+  if (max_items <= 0) return HORA_OK;
+  lowp_tile_kernel<PREC, MT, TILE_DIST><<<(unsigned)max_items, kLpThreads, smem, s>>>(ta, p);
+  HORA_LAUNCHED();
+  return HORA_OK;
+}
+
+static int launch_probe_items(int prec, int metric, const CUtensorMap &ta, const LpParams &p, int max_items,
+                              cudaStream_t s) {
+  const bool bf = prec == HORA_PREC_BF16;
+  switch (metric) {
+    case M_L2: return bf ? launch_probe_items3<HORA_PREC_BF16, M_L2>(ta, p, max_items, s)
+                         : launch_probe_items3<HORA_PREC_FP8, M_L2>(ta, p, max_items, s);
+    case M_IP: return bf ? launch_probe_items3<HORA_PREC_BF16, M_IP>(ta, p, max_items, s)
+                         : launch_probe_items3<HORA_PREC_FP8, M_IP>(ta, p, max_items, s);
+    case M_COS: return bf ? launch_probe_items3<HORA_PREC_BF16, M_COS>(ta, p, max_items, s)
+                          : launch_probe_items3<HORA_PREC_FP8, M_COS>(ta, p, max_items, s);
+  }
+  return fail(HORA_EMETRIC, "no tensor-core form for this metric");
+}
+
 // The tile image from a row-major copy (n x row_bytes) and, for BF16
 // Euclidean, the n x 32-byte norm block: one thread per 16-byte chunk.
 __global__ void tile_image_kernel(const uint8_t *rows, int64_t n, int64_t row_bytes, int nkb,
@@ -1160,8 +1239,81 @@ static int probe_pivot_count(int64_t n) {
 }
 
 static bool probe_eligible(const hora_index *h) {
-  return h->bf_probe && (h->precision == HORA_PREC_BF16 || h->precision == HORA_PREC_FP8) && h->metric == M_L2 &&
-         h->n >= kProbeMinRows;
+  return h->bf_probe && (h->precision == HORA_PREC_BF16 || h->precision == HORA_PREC_FP8) &&
+         (h->metric == M_L2 || h->metric == M_IP || h->metric == M_COS) && h->n >= kProbeMinRows;
+}
+
+// A row image (see RowImage) of nimg rows (a multiple of the tile): image
+// row i holds base row rowmap[i] (device array; 0xffffffff: padding).
+static int build_row_image(hora_index *h, const LowpState &L, const uint32_t *rowmap, int64_t nimg, RowImage &out,
+                           cudaStream_t s) {
+  const int prec = L.prec;
+  const int64_t ld = h->ld, Dp = L.Dp;
+  const int nkb = (int)(Dp / (prec == HORA_PREC_BF16 ? 64 : 128));
+  const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
+  const bool fold = prec == HORA_PREC_BF16 && h->metric == M_L2, cos = h->metric == M_COS;
+  const int64_t ntiles = nimg / kLpBN;
+  DevBuf rowsf, sq64, rows, normblk;  // staging, freed on return
+  HORA_TRY(rowsf.reserve(sizeof(float) * nimg * ld));
+  HORA_TRY(sq64.reserve(sizeof(double) * nimg));
+  HORA_TRY(rows.reserve(nimg * Dp * esz));
+  HORA_TRY(out.xsq.reserve(sizeof(float) * nimg));
+  if (prec == HORA_PREC_FP8) HORA_TRY(out.xscale.reserve(sizeof(float) * nimg));
+  if (cos) HORA_TRY(out.xnorm.reserve(sizeof(float) * nimg));
+  if (fold) HORA_TRY(normblk.reserve(nimg * 16 * 2));
+  HORA_TRY(out.tiles.reserve(ntiles * L.tile_bytes));
+  gather_members_kernel<<<(unsigned)ceil_div(nimg * ld, 256), 256, 0, s>>>(
+      h->base.as<float>(), ld, rowmap, nimg, h->xsq64.as<double>(), L.xsq.as<float>(),
+      cos ? h->xnorm.as<float>() : nullptr, rowsf.as<float>(), sq64.as<double>(), out.xsq.as<float>(),
+      cos ? out.xnorm.as<float>() : nullptr);
+  HORA_LAUNCHED();
+  if (prec == HORA_PREC_BF16) {
+    to_bf16_kernel<<<(unsigned)ceil_div(nimg * Dp, 256), 256, 0, s>>>(rowsf.as<float>(), nimg, ld, h->dim, Dp,
+                                                                      cos ? sq64.as<double>() : nullptr,
+                                                                      rows.as<__nv_bfloat16>());
+    HORA_LAUNCHED();
+    if (fold) {
+      norm_block_kernel<<<(unsigned)ceil_div(nimg, 256), 256, 0, s>>>(sq64.as<double>(), nimg,
+                                                                       normblk.as<__nv_bfloat16>());
+      HORA_LAUNCHED();
+    }
+  } else {
+    to_e4m3_kernel<<<(unsigned)ceil_div(nimg, 8), 256, 0, s>>>(rowsf.as<float>(), nimg, ld, h->dim, Dp,
+                                                               rows.as<uint8_t>(), out.xscale.as<float>());
+    HORA_LAUNCHED();
+  }
+  const int64_t chunks = ntiles * kLpBN * (nkb * 8 + (fold ? 2 : 0));
+  tile_image_kernel<<<(unsigned)ceil_div(chunks, 256), 256, 0, s>>>(rows.as<uint8_t>(), nimg, Dp * esz, nkb,
+                                                                    fold ? normblk.as<uint8_t>() : nullptr,
+                                                                    L.tile_bytes, ntiles, out.tiles.as<uint8_t>());
+  HORA_LAUNCHED();
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  out.rows = nimg;
+  return HORA_OK;
+}
+
+// The members' image of the L.pc pivot clusters (member offsets off, C + 1
+// of them) and the sample image (see LowpState).
+static int build_probe_images(hora_index *h, LowpState &L, const std::vector<int64_t> &off, cudaStream_t s) {
+  const int C = L.pc;
+  std::vector<int64_t> moff(C + 1, 0);
+  for (int c = 0; c < C; ++c)
+    moff[c + 1] = moff[c] + round_up(std::min<int64_t>(off[c + 1] - off[c], kProbeMaxMembers), kLpBN);
+  const int64_t nimg = moff[C];
+  const int64_t ns = round_up(std::min<int64_t>(h->n, kProbeSampleRows), kLpBN);
+  DevBuf rowmap;
+  HORA_TRY(rowmap.reserve(sizeof(uint32_t) * std::max(nimg, ns)));
+  HORA_TRY(L.moff.reserve(sizeof(int64_t) * (C + 1)));
+  HORA_CUDA_TRY(cudaMemcpyAsync(L.moff.ptr, moff.data(), sizeof(int64_t) * (C + 1), cudaMemcpyHostToDevice, s));
+  member_rows_kernel<<<(unsigned)ceil_div(nimg, 256), 256, 0, s>>>(L.coff.as<int64_t>(), L.cmem.as<uint32_t>(),
+                                                                   L.moff.as<int64_t>(), C, nimg,
+                                                                   rowmap.as<uint32_t>());
+  HORA_LAUNCHED();
+  HORA_TRY(build_row_image(h, L, rowmap.as<uint32_t>(), nimg, L.members, s));
+  sample_rows_kernel<<<(unsigned)ceil_div(ns, 256), 256, 0, s>>>(h->n, std::min<int64_t>(h->n, kProbeSampleRows), ns,
+                                                                 rowmap.as<uint32_t>());
+  HORA_LAUNCHED();
+  return build_row_image(h, L, rowmap.as<uint32_t>(), ns, L.sample, s);
 }
 
 // Pivot clusters of the base (exact FP32 nearest-pivot assignment): evenly
@@ -1243,56 +1395,168 @@ static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
       HORA_CUDA_TRY(cudaStreamSynchronize(s));  // the host plan is reused next step
     }
   }
+  // pivots left without members (the dissolved ones, and any that lost
+  // every row in the last assignment) are dropped, so that no metric's pivot
+  // pass can pick an empty cluster: the member ranges stay as they are
+  int Cn = 0;
+  std::vector<int64_t> off;  // the kept clusters' member offsets
+  {
+    std::vector<float> hc((size_t)C * ld);
+    HORA_CUDA_TRY(cudaMemcpyAsync(h_cnt.data(), cnt.ptr, sizeof(int64_t) * C, cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaMemcpyAsync(h_off.data(), L.coff.ptr, sizeof(int64_t) * (C + 1), cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaMemcpyAsync(hc.data(), L.centers.ptr, sizeof(float) * C * ld, cudaMemcpyDeviceToHost, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int c = 0; c < C; ++c) {
+      if (h_cnt[c] == 0) continue;
+      if (Cn != c) std::copy(hc.begin() + (size_t)c * ld, hc.begin() + (size_t)(c + 1) * ld, hc.begin() + (size_t)Cn * ld);
+      off.push_back(h_off[c]);
+      ++Cn;
+    }
+    off.push_back(h_off[C]);
+    HORA_CUDA_TRY(cudaMemcpyAsync(L.centers.ptr, hc.data(), sizeof(float) * Cn * ld, cudaMemcpyHostToDevice, s));
+    HORA_CUDA_TRY(cudaMemcpyAsync(L.coff.ptr, off.data(), sizeof(int64_t) * (Cn + 1), cudaMemcpyHostToDevice, s));
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));  // the host copies are freed on return
+  }
   HORA_CUDA_TRY(cudaMemsetAsync(L.xsqmax.ptr, 0, sizeof(float), s));
   max_nonneg_kernel<<<152, 256, 0, s>>>(L.xsq.as<float>(), n, L.xsqmax.as<unsigned>());
   HORA_LAUNCHED();
-  // the pivots' tile image (BF16 rows and folded norms, like the base's)
-  const int64_t Dp = round_up((int64_t)h->dim, 64);  // BF16, whatever the base's precision
+  // the pivots' tile image in BF16 whatever the base's precision, laid out
+  // like a BF16 base of the index's metric: folded norms for Euclidean,
+  // unit rows for CosineSimilarity
+  const bool fold = h->metric == M_L2;
+  const int64_t Dp = round_up((int64_t)h->dim, 64);
   const int nkb = (int)(Dp / 64);
   L.cnkb = nkb;
-  L.ctile_bytes = (int64_t)nkb * kLpBN * 128 + kNormBytesB;
-  const int64_t ctiles = ceil_div((int64_t)C, (int64_t)kLpBN);
+  L.ctile_bytes = (int64_t)nkb * kLpBN * 128 + (fold ? kNormBytesB : 0);
+  const int64_t ctiles = ceil_div((int64_t)Cn, (int64_t)kLpBN);
   DevBuf crow, cnorm, csq;
-  HORA_TRY(crow.reserve(sizeof(__nv_bfloat16) * C * Dp));
-  HORA_TRY(cnorm.reserve(sizeof(__nv_bfloat16) * C * 16));
-  HORA_TRY(csq.reserve(sizeof(double) * C));
+  HORA_TRY(crow.reserve(sizeof(__nv_bfloat16) * Cn * Dp));
+  HORA_TRY(cnorm.reserve(sizeof(__nv_bfloat16) * Cn * 16));
+  HORA_TRY(csq.reserve(sizeof(double) * Cn));
   HORA_TRY(L.ctiles.reserve(ctiles * L.ctile_bytes));
-  HORA_TRY(launch_row_norms(L.centers.as<float>(), C, ld, h->dim, nullptr, csq.as<double>(), s));
-  to_bf16_kernel<<<ceil_div((int64_t)C * Dp, 256), 256, 0, s>>>(L.centers.as<float>(), C, ld, h->dim, Dp, nullptr,
-                                                                crow.as<__nv_bfloat16>());
+  HORA_TRY(launch_row_norms(L.centers.as<float>(), Cn, ld, h->dim, nullptr, csq.as<double>(), s));
+  to_bf16_kernel<<<ceil_div((int64_t)Cn * Dp, 256), 256, 0, s>>>(L.centers.as<float>(), Cn, ld, h->dim, Dp,
+                                                                 h->metric == M_COS ? csq.as<double>() : nullptr,
+                                                                 crow.as<__nv_bfloat16>());
   HORA_LAUNCHED();
-  norm_block_kernel<<<ceil_div((int64_t)C, 256), 256, 0, s>>>(csq.as<double>(), C, cnorm.as<__nv_bfloat16>());
-  HORA_LAUNCHED();
+  if (fold) {
+    norm_block_kernel<<<ceil_div((int64_t)Cn, 256), 256, 0, s>>>(csq.as<double>(), Cn, cnorm.as<__nv_bfloat16>());
+    HORA_LAUNCHED();
+  }
   tile_image_kernel<<<ceil_div(ctiles * kLpBN * (nkb * 8 + 2), 256), 256, 0, s>>>(
-      crow.as<uint8_t>(), C, Dp * 2, nkb, cnorm.as<uint8_t>(), L.ctile_bytes, ctiles, L.ctiles.as<uint8_t>());
+      crow.as<uint8_t>(), Cn, Dp * 2, nkb, fold ? cnorm.as<uint8_t>() : nullptr, L.ctile_bytes, ctiles,
+      L.ctiles.as<uint8_t>());
   HORA_LAUNCHED();
   HORA_CUDA_TRY(cudaStreamSynchronize(s));  // the temporaries are freed on return
-  L.pc = C;
+  L.pc = Cn;
+  return build_probe_images(h, L, off, s);
+}
+
+// The sampled threshold of a wide R-best list (see the note on starting
+// thresholds) into ws.ptau.  The first ms rows of the sample image are an
+// even sample of the base: where r = R ms / n of them are expected below
+// the base's R-th key, the rs-th smallest sample key, rs = r + 3 sqrt(r) + 1,
+// has about R rs / r base rows below it, and at least R with high
+// probability.  The sample is scanned by the scan kernel in two chunks with
+// the search's own queries: the first s1 = 2,048 rows densely (their rs
+// smallest keys, sorted), then the rest in filter mode from the k1-th of
+// those keys (the same rule with r1 = R s1 / n: a loose threshold, often
+// already well below the members' bound), merged into the same list; the
+// threshold is its rs-th key (or the k1-th when the list stays shorter).
+// Not a bound: a query that keeps fewer than R rows is answered by the
+// chunked schedule.  *used is false when the sample would hold fewer than 16
+// expected rows below the R-th key (a quarter of the base at most).
+static int sample_threshold(hora_index *h, LowpState &L, int prec, int64_t nq, int R, SearchWorkspace &ws,
+                            const CUtensorMap &ta, const LpParams &lp, cudaStream_t s, bool *used) {
+  *used = false;
+  const int64_t n = h->n;
+  const int64_t lim = std::min<int64_t>(std::min<int64_t>(n, kProbeSampleRows), n / 4) / kLpBN * kLpBN;
+  const int64_t ms = std::min<int64_t>(lim, round_up(ceil_div((int64_t)128 * n, (int64_t)R), kLpBN));
+  const double r = (double)R * (double)ms / (double)n;
+  if (r < 16.0) return HORA_OK;
+  const int rs = (int)std::ceil(r + 3.0 * std::sqrt(r)) + 1;
+  const int64_t s1 = std::min<int64_t>(ms, 2048);
+  const double r1 = (double)R * (double)s1 / (double)n;
+  const int k1 = std::min(rs, (int)std::ceil(r1 + 3.0 * std::sqrt(r1)) + 1);
+  const int caps = (int)round_up(std::max<int64_t>(s1, 4 * rs), 128);
+  int64_t nres = 1024;
+  while (nres < nq) nres <<= 1;
+  HORA_TRY(ws.ptau.reserve(sizeof(float) * nres));
+  const int64_t lb = round_up(nq * rs, 32);  // the candidates start 256-byte aligned
+  HORA_TRY(ws.sbuf.reserve(sizeof(uint64_t) * (lb + nq * caps) + sizeof(uint32_t) * nq + nq + 64));
+  uint64_t *sbest = ws.sbuf.as<uint64_t>(), *scand = sbest + lb;
+  uint32_t *scount = reinterpret_cast<uint32_t *>(scand + nq * caps), *sovc = scount + nq;
+  uint8_t *sflags = reinterpret_cast<uint8_t *>(sovc + 4);
+  float *tau = ws.ptau.as<float>();
+  HORA_CUDA_TRY(cudaMemsetAsync(sbest, 0xff, sizeof(uint64_t) * nq * rs, s));
+  HORA_CUDA_TRY(cudaMemsetAsync(scount, 0, sizeof(uint32_t) * (nq + 4) + nq, s));
+  LpParams u = lp;
+  u.tiles = L.sample.tiles.as<uint8_t>();
+  u.xsq = L.sample.xsq.as<float>();
+  u.xscale = L.sample.xscale.as<float>();
+  u.xnorm = L.sample.xnorm.as<float>();
+  u.nq = nq;
+  u.qmap = nullptr;
+  u.dense_hits = 0;
+  u.best = sbest;
+  u.k = rs;
+  u.cand = scand;
+  u.cap = caps;
+  u.count = scount;
+  u.items = nullptr;
+  auto scan = [&](int mode) -> int {
+    ProfScope ps("probe_sample", s);
+    return prec == HORA_PREC_BF16 ? launch_lp2<HORA_PREC_BF16>(h->metric, mode, ta, u, s)
+                                  : launch_lp2<HORA_PREC_FP8>(h->metric, mode, ta, u, s);
+  };
+  u.r_begin = 0;
+  u.r_end = s1;
+  u.tpc = lp_tiles_per_cta(nq, s1);
+  u.tau0 = nullptr;
+  HORA_TRY(scan(TILE_DENSE));
+  HORA_TRY(launch_merge_topk(sbest, rs, scand, nullptr, caps, (int)s1, nullptr, nq, sflags, sovc, s, true));
+  sample_tau_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(sbest, rs, k1, nq, true, tau);
+  HORA_LAUNCHED();
+  if (ms > s1) {
+    u.r_begin = s1;
+    u.r_end = ms;
+    u.tpc = lp_tiles_per_cta(nq, ms - s1);
+    u.tau0 = tau;
+    HORA_TRY(scan(TILE_FILTER));
+    HORA_TRY(launch_merge_topk(sbest, rs, scand, scount, caps, 0, nullptr, nq, sflags, sovc, s, false));
+    sample_tau_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(sbest, rs, rs, nq, false, tau);
+    HORA_LAUNCHED();
+  }
+  *used = true;
   return HORA_OK;
 }
 
 // Starting thresholds of nq staged queries (ws.q f32, ws.lq, ws.lqsq) into
-// ws.ptau.  lp carries the search's scan parameters; the pivot pass keeps
-// each query's nearest pivot key in ws.pkeys.
-// ta16: the queries' BF16 tile map (the pivot pass runs in BF16 whatever
-// the base's precision); the probe scores members in the base's precision
-// (prec), from ws.lq (and ws.lqscale for FP8).
+// ws.ptau, for R-best lists up to kProbeClusterMaxR wide.  lp carries the
+// search's scan parameters; the pivot pass keeps each query's nearest pivot
+// key in ws.pkeys.  ta16: the queries' BF16 tile map for the pivot pass (it
+// runs in BF16 whatever the base's precision, in the index's metric: unit
+// queries for CosineSimilarity); the probe scores members in the base's
+// precision (prec) and metric, from ws.lq (and ws.lqscale for FP8).
+// *order (when given) receives the queries in order of their nearest pivot.
 static int probe_thresholds(hora_index *h, LowpState &L, int prec, int64_t nq, int R, int64_t Dp,
                             SearchWorkspace &ws, const CUtensorMap &ta16, const LpParams &lp, cudaStream_t s,
-                            const float *slack = nullptr) {
+                            const float *slack = nullptr, const uint32_t **order = nullptr) {
   const int C = L.pc;
   // sized for a power of two of at least 1,024 queries: a serving slot whose
   // batches vary reallocates (and with that waits for the device) rarely
   int64_t nres = 1024;
   while (nres < nq) nres <<= 1;
   HORA_TRY(ws.pkeys.reserve(sizeof(uint64_t) * nres));
-  HORA_TRY(ws.poff.reserve(sizeof(int64_t) * (C + 1) + sizeof(int) * (C + 1)));
+  HORA_TRY(ws.poff.reserve(sizeof(int64_t) * (C + 1)));
   HORA_TRY(ws.pmem.reserve(sizeof(uint32_t) * nres));
   HORA_TRY(ws.pdist.reserve(sizeof(float) * nres * kProbeMaxMembers));
-  HORA_TRY(ws.ptau.reserve(sizeof(float) * nres));
+  HORA_TRY(ws.ptau.reserve(sizeof(float) * nres + sizeof(uint32_t) * nres));  // thresholds, then positions
   int64_t *qoff = ws.poff.as<int64_t>();
-  int *item_off = reinterpret_cast<int *>(qoff + C + 1);
-  // nearest pivot: the tensor-core scan over the pivots in dense mode, then the best key
+  uint32_t *pmem = ws.pmem.as<uint32_t>(), *pos_of = ws.ptau.as<uint32_t>() + nres;
+  // nearest pivot: the tensor-core scan over the pivots' image, each drain
+  // thread's smallest key combined by a 64-bit atomic minimum per query (no
+  // per-pivot keys written)
   LpParams a = lp;
   a.tiles = L.ctiles.as<uint8_t>();
   a.r_begin = 0;
@@ -1301,39 +1565,56 @@ static int probe_thresholds(hora_index *h, LowpState &L, int prec, int64_t nq, i
   a.tau0 = nullptr;
   a.dense_hits = 0;
   a.nkb = L.cnkb;
-  a.stages = lp_stages(L.cnkb, true);
-  // each drain thread's smallest key, combined by a 64-bit atomic minimum
-  // per query (no per-pivot keys written)
-  a.best = ws.pkeys.as<uint64_t>();
-  HORA_CUDA_TRY(cudaMemsetAsync(ws.pkeys.ptr, 0xff, sizeof(uint64_t) * nq, s));
-  HORA_TRY((launch_lp3<HORA_PREC_BF16, M_L2, TILE_ARGMIN>(ta16, a, s)));
-  HORA_TRY(sort_labels(ws.pkeys.as<uint64_t>(), nullptr, nq, C, ws.pblk, ws.pcnt, qoff, ws.pmem.as<uint32_t>(), s));
-  const bool fp8 = prec == HORA_PREC_FP8;
-  if (fp8)
-    HORA_SMEM_ATTR(probe_dist_kernel<true>, kProbeSmem);
-  else
-    HORA_SMEM_ATTR(probe_dist_kernel<false>, kProbeSmem);
+  a.stages = lp_stages(L.cnkb, h->metric == M_L2);
+  uint64_t *pk = ws.pkeys.as<uint64_t>();
+  a.best = pk;
+  HORA_CUDA_TRY(cudaMemsetAsync(pk, 0xff, sizeof(uint64_t) * nq, s));
+  HORA_TRY(launch_pivot_pass(h->metric, ta16, a, s));
+  fill_empty_pivot_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(pk, nq, C);
+  HORA_LAUNCHED();
+  // queries bucketed by pivot: position i of the pivot order holds query pmem[i]
+  HORA_TRY(sort_labels(pk, nullptr, nq, C, ws.pblk, ws.pcnt, qoff, pmem, s));
+  if (order) *order = pmem;
+  const int mt = h->metric;
   {
+    // the queries gathered in pivot order, one work item per (pivot, up to
+    // 128 of its queries), the members' keys by the scan kernel
     ProfScope ps("probe_scores", s);
-    probe_items_kernel<<<1, 1024, 0, s>>>(qoff, C, item_off);
+    const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
+    const int64_t max_items = C + ceil_div(nq, (int64_t)kLpBM);
+    const int64_t qb = round_up(nq * Dp * esz, 16);
+    HORA_TRY(ws.pqg.reserve(qb + sizeof(int4) * max_items + 16));
+    int4 *items = reinterpret_cast<int4 *>(ws.pqg.as<uint8_t>() + qb);
+    int *n_items = reinterpret_cast<int *>(items + max_items);
+    inverse_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(pmem, nq, pos_of);
     HORA_LAUNCHED();
-    const unsigned grid = (unsigned)(C + ceil_div(nq, (int64_t)kProbeQ));
-    if (fp8)
-      probe_dist_kernel<true><<<grid, 256, kProbeSmem, s>>>(
-          L.tiles.as<uint8_t>(), L.tile_bytes, L.xsq.as<float>(), L.xscale.as<float>(), L.coff.as<int64_t>(),
-          L.cmem.as<uint32_t>(), ws.lq.as<uint8_t>(), ws.lqscale.as<float>(), Dp, ws.lqsq.as<float>(), qoff,
-          ws.pmem.as<uint32_t>(), item_off, C, ws.pdist.as<float>());
-    else
-      probe_dist_kernel<false><<<grid, 256, kProbeSmem, s>>>(
-          L.tiles.as<uint8_t>(), L.tile_bytes, L.xsq.as<float>(), nullptr, L.coff.as<int64_t>(),
-          L.cmem.as<uint32_t>(), ws.lq.as<uint8_t>(), nullptr, Dp, ws.lqsq.as<float>(), qoff,
-          ws.pmem.as<uint32_t>(), item_off, C, ws.pdist.as<float>());
+    gather_rows_u8_kernel<<<(unsigned)nq, 128, 0, s>>>(ws.lq.as<uint8_t>(), Dp * esz,
+                                                        reinterpret_cast<const int *>(pmem), nq,
+                                                        ws.pqg.as<uint8_t>());
     HORA_LAUNCHED();
+    probe_items_kernel<<<1, 1024, 0, s>>>(qoff, L.coff.as<int64_t>(), L.moff.as<int64_t>(), C, items, n_items);
+    HORA_LAUNCHED();
+    CUtensorMap tq;
+    HORA_TRY(make_tmap(&tq, ws.pqg.ptr, prec, Dp, nq, kLpBM));
+    LpParams t = lp;
+    t.tiles = L.members.tiles.as<uint8_t>();
+    t.xsq = L.members.xsq.as<float>();
+    t.xscale = L.members.xscale.as<float>();
+    t.xnorm = L.members.xnorm.as<float>();
+    t.nq = nq;
+    t.qmap = reinterpret_cast<const int *>(pmem);
+    t.tau0 = nullptr;
+    t.dense_hits = 0;
+    t.items = items;
+    t.n_items = n_items;
+    t.out_dist = ws.pdist.as<float>();
+    t.ldo = kProbeMaxMembers;
+    HORA_TRY(launch_probe_items(prec, mt, tq, t, (int)max_items, s));
   }
   ProfScope ps("probe_select", s);
-  probe_select_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(
-      ws.pkeys.as<uint64_t>(), L.coff.as<int64_t>(), ws.pdist.as<float>(), ws.lqsq.as<float>(),
-      L.xsqmax.as<float>(), nq, R, slack, ws.ptau.as<float>());
+  probe_select_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(pk, L.coff.as<int64_t>(), C, ws.pdist.as<float>(),
+                                                                pos_of, ws.lqsq.as<float>(), L.xsqmax.as<float>(),
+                                                                mt, nq, R, slack, ws.ptau.as<float>());
   HORA_LAUNCHED();
   return HORA_OK;
 }
@@ -1346,6 +1627,12 @@ int lowp_prepare(hora_index *h, cudaStream_t s) {
   return HORA_OK;
 }
 
+int lowp_probe_kind(const hora_index *h, int R) {
+  const int64_t kbe = h->precision == HORA_PREC_BF16 ? 64 : 128;
+  if (!probe_eligible(h) || R > kProbeMaxR || round_up((int64_t)h->dim, kbe) / kbe > 2) return 0;
+  return R <= kProbeClusterMaxR ? 1 : 2;
+}
+
 int lowp_rerank_width(const hora_index *h, int k) {
   const int64_t kbe = h->precision == HORA_PREC_BF16 ? 64 : 128;
   if (h->metric == M_L1 || round_up((int64_t)h->dim, kbe) / kbe > 2) return 0;  // the exact path answers
@@ -1354,6 +1641,10 @@ int lowp_rerank_width(const hora_index *h, int k) {
   R = std::max(R, k);
   return (int)std::min<int64_t>(R, std::max<int64_t>(h->n, k));
 }
+
+__global__ void exact_tc_slack_kernel(const float *Q, int64_t nq, int64_t ld, int64_t dim, int64_t Dp,
+                                      const double *qsq64, const float *dxmax, const float *xsqmax,
+                                      float *slack);
 
 int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
                      cudaStream_t s) {
@@ -1376,6 +1667,8 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   if (R > 4096) return fail(HORA_ECAP, "rerank width must be <= 4096");
   int cap = std::max(h->cand_cap, 2 * R);
   cap = (int)round_up(cap, 128);
+  // the overflow rescans' merge holds the list and the candidates in shared memory
+  while (cap > 2 * R && merge_smem_bytes(R, cap) > 200 * 1024) cap -= 128;
   const int stages = lp_stages(nkb, prec == HORA_PREC_BF16 && h->metric == M_L2);
   const int64_t esz = prec == HORA_PREC_BF16 ? 2 : 1;
 
@@ -1484,22 +1777,29 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     return make_tmap(tg, ws.lqgather.ptr, prec, Dp, nl, kLpBM);
   };
   int *lerr = ws.lerr.as<int>();  // [0] a pipeline wait timed out, [1] short lists after the probed pass
-  // (the probe kernel stages rows of at most 128 values)
-  const bool probe = probe_eligible(h) && R <= kProbeMaxR && Dp <= 128;
-  if (probe) {
-    // one filter pass from the probed thresholds
+  const uint32_t *rr_order = nullptr;  // the rerank's query order (clusters: by nearest pivot)
+  bool probe = false;                  // a starting threshold per query
+  if (probe_eligible(h) && R > kProbeClusterMaxR && R <= kProbeMaxR) {
+    HORA_TRY(ensure_pivots(h, L, s));
+    HORA_TRY(sample_threshold(h, L, prec, nq, R, ws, ta, p, s, &probe));
+  } else if (probe_eligible(h) && R <= kProbeClusterMaxR) {
+    probe = true;
     HORA_TRY(ensure_pivots(h, L, s));
     CUtensorMap ta16 = ta;
     if (prec == HORA_PREC_FP8) {
-      // the pivot pass reads the queries in BF16
+      // the pivot pass reads the queries in BF16 (unit rows for CosineSimilarity)
       const int64_t Dp16 = round_up((int64_t)h->dim, 64);
       HORA_TRY(ws.lq16.reserve(std::max<int64_t>(nq, 1) * Dp16 * 2));
-      to_bf16_kernel<<<ceil_div(nq * Dp16, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp16, nullptr,
+      to_bf16_kernel<<<ceil_div(nq * Dp16, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp16,
+                                                               h->metric == M_COS ? qsq64 : nullptr,
                                                                ws.lq16.as<__nv_bfloat16>());
       HORA_LAUNCHED();
       HORA_TRY(make_tmap(&ta16, ws.lq16.ptr, HORA_PREC_BF16, Dp16, nq, kLpBM));
     }
-    HORA_TRY(probe_thresholds(h, L, prec, nq, R, Dp, ws, ta16, p, s));
+    HORA_TRY(probe_thresholds(h, L, prec, nq, R, Dp, ws, ta16, p, s, nullptr, &rr_order));
+  }
+  if (probe) {
+    // one filter pass from the starting thresholds
     p.tau0 = ws.ptau.as<float>();
     p.dense_hits = 0;
     for (int64_t lo = 0; lo < n; lo += max_chunk) {
@@ -1518,10 +1818,41 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   // the host learns whether a candidate list overflowed or came out short
   // (rare), so the stream runs on without a round trip, and redone after
   HORA_TRY(ws.tmp.reserve(sizeof(uint64_t) * nq * R));
+  // A wide BF16 Euclidean list is reranked only where the exact k best can
+  // lie: with eps(q) the certified bound on |scan key - exact distance| (the
+  // exact search's, see exact_tc_slack_kernel), k candidates have exact
+  // distances at most T + eps (T the k-th smallest scan key of the list),
+  // so a candidate whose scan key exceeds T + 2 eps is beaten by k others
+  // and cannot be among the k best: the result equals the rerank of all R.
+  const bool window = prec == HORA_PREC_BF16 && h->metric == M_L2 && L.pc > 0 && R >= 512 && R >= 4 * k;
+  uint64_t *wkth = nullptr;
+  uint32_t *wcount = nullptr;
+  if (window) {
+    HORA_TRY(ws.xslack.reserve(sizeof(float) * nq));
+    HORA_TRY(ws.rwin.reserve(sizeof(uint64_t) * nq * k + sizeof(uint32_t) * nq));
+    wkth = ws.rwin.as<uint64_t>();
+    wcount = reinterpret_cast<uint32_t *>(wkth + nq * k);
+    exact_tc_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, qsq64,
+                                                          L.dxmax.as<float>(), L.xsqmax.as<float>(),
+                                                          ws.xslack.as<float>());
+    HORA_LAUNCHED();
+  }
   auto finish = [&]() -> int {
+    if (window) {
+      HORA_CUDA_TRY(cudaMemsetAsync(wkth, 0xff, sizeof(uint64_t) * nq * k, s));
+      HORA_TRY(launch_merge_topk(wkth, k, bestR, nullptr, R, R, nullptr, nq, flags, ovc, s, false));
+      rerank_window_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(bestR, R, wkth, k, ws.xslack.as<float>(), nq,
+                                                                     ws.tmp.as<uint64_t>(), wcount);
+      HORA_LAUNCHED();
+      HORA_TRY(launch_rerank_exact(h->metric, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim,
+                                   ws.qnorm.as<float>(), h->xnorm.as<float>(), ws.tmp.as<uint64_t>(), nq, R,
+                                   ws.tmp.as<uint64_t>(), s, wcount, rr_order));
+      HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
+      return launch_merge_topk(d_best, k, ws.tmp.as<uint64_t>(), wcount, R, 0, nullptr, nq, flags, ovc, s);
+    }
     HORA_TRY(launch_rerank_exact(h->metric, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim,
                                  ws.qnorm.as<float>(), h->xnorm.as<float>(), bestR, nq, R,
-                                 ws.tmp.as<uint64_t>(), s));
+                                 ws.tmp.as<uint64_t>(), s, nullptr, rr_order));
     HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
     return launch_merge_topk(d_best, k, ws.tmp.as<uint64_t>(), nullptr, R, R, nullptr, nq, flags, ovc, s);
   };
@@ -1537,18 +1868,21 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   };
   HORA_TRY(status());
   h->last_probe = probe ? 1 : 0;
-  bool redo = false;
+  h->last_short_lists = hs[1];
+  h->last_overflow_queries = h_ovc;
+  std::vector<int> redo;  // queries whose R-best lists were redone
   if (hs[1] > 0) {
     // lists the probed pass left short: the chunked schedule answers them
     h->last_probe = 2;
     const int64_t nl = hs[1];
+    redo.resize(nl);
+    HORA_CUDA_TRY(cudaMemcpyAsync(redo.data(), ws.qlist.ptr, sizeof(int) * nl, cudaMemcpyDeviceToHost, s));
     clear_lists_kernel<<<(unsigned)ceil_div(nl * R, 256), 256, 0, s>>>(bestR, R, ws.qlist.as<int>(), nl);
     HORA_LAUNCHED();
     CUtensorMap tg;
     HORA_TRY(gather(nl, &tg));
     HORA_TRY(chunked(tg, nl, ws.qlist.as<int>()));
     HORA_TRY(status());
-    redo = true;
   }
   // overflow rescans over gathered query rows, against the R-th key of the
   // list so far (for a probed list that key is already at or below its
@@ -1563,6 +1897,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     for (int64_t q = 0; q < nq; ++q)
       if (ws.h_flags[q]) list.push_back((int)q);
     const int64_t nl = (int64_t)list.size();
+    redo.insert(redo.end(), list.begin(), list.end());
     HORA_CUDA_TRY(cudaMemcpyAsync(ws.qlist.ptr, list.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, s));
     HORA_CUDA_TRY(cudaMemsetAsync(flags, 0, nq, s));
     HORA_CUDA_TRY(cudaMemsetAsync(ovc, 0, sizeof(uint32_t), s));
@@ -1581,10 +1916,24 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
       HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, ws.qlist.as<int>(), nl, flags, ovc, s));
     }
     HORA_TRY(status());
-    redo = true;
   }
   h->last_retries = rounds;
-  if (redo) HORA_TRY(finish());
+  if (!redo.empty()) {
+    // the exact rerank and the k best again, for the redone queries only
+    std::sort(redo.begin(), redo.end());
+    redo.erase(std::unique(redo.begin(), redo.end()), redo.end());
+    const int64_t nl = (int64_t)redo.size();
+    const int *ql = ws.qlist.as<int>();
+    HORA_CUDA_TRY(cudaMemcpyAsync(ws.qlist.ptr, redo.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, s));
+    HORA_TRY(launch_rerank_exact(h->metric, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim,
+                                 ws.qnorm.as<float>(), h->xnorm.as<float>(), bestR, nl, R, ws.tmp.as<uint64_t>(), s,
+                                 nullptr, reinterpret_cast<const uint32_t *>(ql)));
+    clear_lists_kernel<<<(unsigned)ceil_div(nl * k, 256), 256, 0, s>>>(d_best, k, ql, nl);
+    HORA_LAUNCHED();
+    HORA_TRY(launch_merge_topk(d_best, k, ws.tmp.as<uint64_t>(), nullptr, R, R, ql, nl, flags, ovc, s));
+    // the host vector is read by the copy above before it goes out of scope
+    HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  }
   return HORA_OK;
 }
 
@@ -1601,8 +1950,8 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
 //   the f32 roundings of |x|^2 / 2, |q|^2 and the final FMA            (C)
 //   the reference's own f32 sum, (dim + 4) 2^-23 (|q| + max|x|)^2     (E)
 //   eps = 2 A + 2 B + C + E.
-// The probe (probe_dist_kernel, same products, another f32 order, within
-// delta = 1e-4 (|q|^2 + max|x|^2) of the scan) puts a query's k-th smallest
+// The probe (the scan kernel on the members' image: the scan's own values,
+// and delta = 1e-4 (|q|^2 + max|x|^2) added regardless) puts a query's k-th smallest
 // probe value t among its pivot cluster's members.  k rows then have r <= t
 // + delta + eps, so the exact k-th distance is at most that, and every row
 // of the exact top k has s <= t + delta + 2 eps: the filter pass from that

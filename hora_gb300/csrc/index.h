@@ -60,6 +60,9 @@ struct hora_index {
   std::atomic<int> last_retries{0};
   // BF16 starting-threshold probe: 0 not used, 1 answered, 2 fell back to the chunked schedule
   std::atomic<int> last_probe{0};
+  // low-precision search: queries whose candidate list overflowed its
+  // capacity (before the rescans), queries the probed pass left short
+  std::atomic<int64_t> last_overflow_queries{0}, last_short_lists{0};
   // certified exact search: queries the last search handed to the CUDA-core scan
   std::atomic<int64_t> last_fallback{0};
   std::atomic<double> last_ms{0.0};
@@ -94,6 +97,9 @@ int lowp_prepare(hora_index *h, cudaStream_t s);
 // Candidates a low-precision search keeps for its exact rerank (0 when the
 // exact path answers: Manhattan, or dimensions beyond the resident tile).
 int lowp_rerank_width(const hora_index *h, int k);
+// The starting threshold a low-precision search of an R-best list takes: 0
+// none (the chunked schedule), 1 the cluster probe, 2 the sampled threshold.
+int lowp_probe_kind(const hora_index *h, int R);
 // Exact FP32 Euclidean search with the BF16 tensor-core scan as a certified
 // filter (bf_lowp.cu): whether it answers a k-NN search on this index, its
 // lazily built state, the search itself.

@@ -52,9 +52,11 @@ int launch_check_finite(const float *X, int64_t n, int64_t ld, int64_t dim, uint
 // Exact FP32 distances (reference op order) for R candidate rows per query:
 // in = approximate keys (row in the low word), out = exact keys.  With
 // count, query q has min(count[q], R) keys in its R slots (in may be out).
+// With order (a permutation of the nq queries), they are taken in that order.
 int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, int64_t dim,
                         const float *qnorm, const float *xnorm, const uint64_t *in, int64_t nq,
-                        int R, uint64_t *out, cudaStream_t s, const uint32_t *count = nullptr);
+                        int R, uint64_t *out, cudaStream_t s, const uint32_t *count = nullptr,
+                        const uint32_t *order = nullptr);
 
 // ---- selection (topk.cu) ------------------------------------------------------
 // Merges each query's candidates into its sorted k-best key list (dedup by
@@ -91,6 +93,9 @@ struct SearchWorkspace {
   // BF16 starting thresholds: query -> pivot keys, queries bucketed by pivot,
   // probe distances (queries x members), thresholds
   DevBuf pkeys, poff, pmem, pblk, pcnt, pdist, ptau;
+  DevBuf pqg;    // the probe's queries in pivot order and its work items
+  DevBuf sbuf;   // wide lists: the sample pass's lists, candidates, counts and flags
+  DevBuf rwin;   // windowed rerank: each query's k best approximate keys, then its kept counts
   // learned nprobe
   DevBuf feats, pred, npq;
   // certified tensor-core exact search: per-query threshold slack, one empty
@@ -109,7 +114,7 @@ struct SearchWorkspace {
                            &out_dist, &rows, &keys2, &tmp, &coarse, &probes, &pair_cnt, &pair_off, &pair_q,
                            &pair_c, &pair_slot, &ivf_cand, &best_r, &tmp_keys, &adc_next, &adc_gmap, &lq,
                            &lqsq, &lqscale, &lqgather, &lerr, &lq16, &pkeys, &poff, &pmem, &pblk, &pcnt, &pdist,
-                           &ptau, &feats, &pred, &npq, &xslack, &xempty, &xlist, &xq, &xkeys, &d_status};
+                           &ptau, &pqg, &sbuf, &rwin, &feats, &pred, &npq, &xslack, &xempty, &xlist, &xq, &xkeys, &d_status};
     size_t b = 0;
     for (const DevBuf *d : all) b += d->bytes;
     return b;

@@ -118,7 +118,8 @@ __global__ void coarse_init_kernel(const float *X, int64_t ld, int64_t n, int64_
 }
 
 // Stable counting sort of n labels in [0, C): block histograms, per-label
-// block prefix, then an in-order warp scatter inside each block.
+// block prefix, then an in-order warp scatter inside each block.  An item
+// whose label is outside [0, C) (an empty key) is left out of every bucket.
 constexpr int kSortBlock = 1024;
 
 __global__ void label_hist_kernel(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
@@ -129,7 +130,7 @@ __global__ void label_hist_kernel(const uint64_t *keys, const uint32_t *labels, 
   int64_t lo = (int64_t)blockIdx.x * kSortBlock;
   for (int64_t i = lo + threadIdx.x; i < min(n, lo + kSortBlock); i += blockDim.x) {
     uint32_t l = keys ? key_row(keys[i]) : labels[i];
-    atomicAdd(&hist[l], 1u);
+    if (l < (uint32_t)C) atomicAdd(&hist[l], 1u);
   }
   __syncthreads();
   for (int c = threadIdx.x; c < C; c += blockDim.x) block_counts[(int64_t)blockIdx.x * C + c] = hist[c];
@@ -188,8 +189,8 @@ __global__ void label_scatter_kernel(const uint64_t *keys, const uint32_t *label
   int64_t hi = min(n, lo + kSortBlock);
   for (int64_t base = lo; base < hi; base += 32) {
     int64_t i = base + lane;
-    bool ok = i < hi;
-    uint32_t l = ok ? (keys ? key_row(keys[i]) : labels[i]) : 0xffffffffu;
+    uint32_t l = i < hi ? (keys ? key_row(keys[i]) : labels[i]) : 0xffffffffu;
+    const bool ok = l < (uint32_t)C;
     unsigned peers = __match_any_sync(0xffffffffu, l);
     unsigned lower = peers & ((1u << lane) - 1u);
     uint32_t r0 = ok ? rank[l] : 0;

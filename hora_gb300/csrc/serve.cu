@@ -92,9 +92,13 @@ static size_t request_bytes(const hora_index *h, uint64_t nq, uint64_t k) {
     const int R = std::max<int>((int)k, lowp_rerank_width(h, (int)k));
     const size_t cap = (size_t)round_up(std::max(h->cand_cap, 2 * R), 128);
     per_q += Dp * 2 + cap * 8 + (size_t)R * 16 + 64;
-    const size_t C = 4096;                                  // pivots at most
-    const size_t nres = std::max<size_t>(1024, nq);         // probe buffers: a power of two >= 1,024
-    fixed += 2 * nres * (8 + 4 + 4 + 1024 * 4) + C * 64;
+    // starting thresholds: per query (a power of two >= 1,024 of them) the
+    // pivot key, bucket slot, member keys, threshold, position, query copy
+    // and share of a work item (4,096 pivots at most); for wide lists the
+    // sample pass's list and candidates (at most 165 + 2,048 keys)
+    const size_t nres = std::max<size_t>(1024, nq);
+    fixed += 2 * nres * (8 + 4 + 1024 * 4 + 4 + 4 + Dp + 1) + (size_t)4097 * 48;
+    if (lowp_probe_kind(h, R) == 2) per_q += 8 * (165 + 2048 + 32) + 8;
   } else {
     const size_t C = h->ivf.n_kmeans_center;
     size_t pmax = std::max<size_t>(32, std::max<size_t>(h->ivf.search_n_center, (size_t)h->nprobe_max));
