@@ -683,7 +683,10 @@ def run_ours(a, dist: Dist):
         roof["traffic"] = SCAN_TRAFFIC_BYTES_PER_STEP * a.steps \
             if name == "bf16_tc_scan" and head == "bf16r132" and not a.small and nq == 10000 else None
         roof["traffic_unit"] = "bytes per timed region (dram__bytes_read.sum + dram__bytes_write.sum)"
-        roof["algorithmic_bytes"] = (n * (DIM * 2 + 32)) * a.steps if name == "bf16_tc_scan" else None
+        # per base row the image bytes a pass reads: BF16 rows and norm block,
+        # or e4m3 rows plus the per-row scale and squared norm the drain reads
+        roof["algorithmic_bytes"] = (n * (DIM * 2 + 32)) * a.steps if name == "bf16_tc_scan" else (
+            (n * (DIM + 8)) * a.steps if name == "fp8_tc_scan" else None)
         roof["share_of_step"] = ms / (t_dev * 1e3)
 
     extras = run_form_extras(a, H, ix, base, q, dq, exact, prec, head_rerank) \
@@ -714,7 +717,7 @@ def run_ours(a, dist: Dist):
             "value": value, "unit": "queries/s", "n_gpus": dist.world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_max / a.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": {"fp32": "f32", "bf16": "bf16", "fp8": "e4m3"}[head[:4]],
+            "dtype": "f32" if head.startswith("fp32") else ("bf16" if head.startswith("bf16") else "e4m3"),
             "data": "synthetic (seeded gaussian mixture; ann-benchmarks sets unavailable offline)",
             "config": {"workload": WORKLOAD if not a.small else "small check", "n": n, "dim": DIM,
                        "queries": nq, "k": K, "form": head, "rerank": head_rerank or "default",

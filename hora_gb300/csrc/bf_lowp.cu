@@ -68,7 +68,7 @@ constexpr int kLpHitBytes = kLpHitBuf * kLpEpiThreads * 8;
 // with the per-row values the scan's drain reads (exact squared norms, e4m3
 // scales, norms); padding rows are zero.
 struct RowImage {
-  DevBuf tiles, xsq, xscale, xnorm;
+  DevBuf tiles, xsq, xscale, xnorm, gmeta;
   int64_t rows = 0;  // a multiple of the tile
 };
 
@@ -79,6 +79,7 @@ struct LowpState {
   int64_t tile_bytes = 0;
   DevBuf xsq;      // n f32 exact squared norms
   DevBuf xscale;   // n f32 (e4m3 per-row scale)
+  DevBuf gmeta;    // e4m3: per 32 rows the filter's bound inputs (see group_meta_kernel)
   // BF16 Euclidean on at least kProbeMinRows rows: pivot clusters of the base
   // (see ensure_pivots), built on first use
   int pc = 0;      // pivots (0: not built)
@@ -96,8 +97,8 @@ struct LowpState {
   // the sample image: base rows floor(frac(j phi) n), j = 1, 2, ... (any
   // prefix spread over the base), for wide R-best lists
   RowImage sample;
-  // BF16 Euclidean: the largest |x - bf16(x)| over the rows (1 f32, rounded
-  // up), the rows' share of the certified exact search's error bound
+  // BF16 Euclidean and DotProduct: the largest |x - bf16(x)| over the rows
+  // (1 f32, rounded up), the rows' share of the certified error bounds
   DevBuf dxmax;
 };
 
@@ -129,6 +130,9 @@ struct LpParams {
   // TILE_DIST: distances out_dist[query row * ldo + column]
   float *out_dist;
   int64_t ldo;
+  // FP8 filter: per 32 image rows {min |x|^2, min scale, max scale, 0}, or
+  // null (see group_meta_kernel)
+  const float4 *gmeta;
 };
 
 // BF16 Euclidean folds the row norm into the MMA: one extra K = 16 step
@@ -534,6 +538,15 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     int nb = 0;  // keys staged in this thread's column
     for (int t = 0; t < T; ++t) {
       const int b = t % kLpNB, jb = t / kLpNB;
+      // e4m3 filter: this warp's two slices' bound inputs, loaded while the
+      // MMAs of the tile run
+      static_assert(kLpSlices == 2, "two slices per drain warp and tile");
+      float4 gm0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), gm1 = gm0;
+      if (!FAST && MODE == TILE_FILTER && (MT == M_L2 || MT == M_IP) && p.gmeta) {
+        const int64_t g0 = (row0 + (int64_t)t * kLpBN + h * kLpSlices * 32) >> 5;
+        gm0 = __ldg(p.gmeta + g0);
+        gm1 = __ldg(p.gmeta + g0 + 1);
+      }
       const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full + b, jb & 1, abort));
       if (!ok) break;
       tc::fence_after_sync();
@@ -545,14 +558,6 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       // slice's hit handling wait here for the others
       __syncwarp();
       c.rt = row0 + (int64_t)t * kLpBN + (h * kLpSlices + sl) * 32;
-      // generic forms: this lane's row factor, broadcast by shuffle below
-      float xa = 0.0f, xs = 1.0f;
-      if (!FAST) {
-        const int64_t r = c.rt + lane;
-        const float *va = MT == M_L2 ? p.xsq : (MT == M_COS ? p.xnorm : nullptr);
-        if (va) xa = r < r_end ? __ldg(va + r) : 0.0f;
-        if (PREC == HORA_PREC_FP8) xs = r < r_end ? __ldg(p.xscale + r) : 0.0f;
-      }
       uint32_t v[32];
       tc::tmem_ld32(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + (h * kLpSlices + sl) * 32), v);
       tc::tmem_ld_wait();
@@ -613,6 +618,43 @@ __global__ void __launch_bounds__(kLpThreads, 1)
           }
         }
         continue;
+      }
+      if constexpr (MODE == TILE_FILTER && (MT == M_L2 || MT == M_IP)) {
+        // e4m3 filter on the raw accumulators: from the slice's bound inputs
+        // (smallest squared norm, scale range of its 32 rows) an accumulator
+        // threshold th such that a column whose key clears tau has acc >= th
+        // (Euclidean: qsq + |x|^2 - 2 qs xs acc <= tau needs 2 qs max(xs) acc
+        // >= qsq + min|x|^2 - tau) or acc <= th (DotProduct: qs xs acc <=
+        // tau), loosened by a relative 1e-5 for the f32 roundings.  When the
+        // slice's extreme clears no lane's threshold, the warp skips the
+        // per-column pass; the decision is a warp vote, because that pass
+        // shuffles across all 32 lanes.
+        if (p.gmeta) {
+          const float4 gm = sl == 0 ? gm0 : gm1;
+          float th;
+          if (MT == M_L2) {
+            const float slack = 1e-5f * (fabsf(qa) + fabsf(gm.x) + fabsf(tau_d));
+            th = ((qa + gm.x) - tau_d - slack) / (2.0f * qs * gm.z);
+            th = th > 0.0f ? th * (1.0f - 1e-5f) : -__int_as_float(0x7f800000);  // else every column
+          } else {
+            th = tau_d / (qs * (tau_d >= 0.0f ? gm.y : gm.z));
+            th = th + 1e-5f * fabsf(th) + 1e-30f;
+          }
+          bool maybe = false;
+          if (qid >= 0) {
+            const float ext = slice_extreme<MT == M_IP>(v);
+            maybe = MT == M_L2 ? ext >= th : ext <= th;
+          }
+          if (!__any_sync(0xffffffffu, maybe)) continue;
+        }
+      }
+      // generic forms: this lane's row factor, broadcast by shuffle below
+      float xa = 0.0f, xs = 1.0f;
+      {
+        const int64_t r = c.rt + lane;
+        const float *va = MT == M_L2 ? p.xsq : (MT == M_COS ? p.xnorm : nullptr);
+        if (va) xa = r < r_end ? __ldg(va + r) : 0.0f;
+        if (PREC == HORA_PREC_FP8) xs = r < r_end ? __ldg(p.xscale + r) : 0.0f;
       }
       // finished distances replace the accumulators in place
       uint32_t hits = 0;
@@ -967,6 +1009,55 @@ __global__ void short_lists_kernel(const uint64_t *best, int R, int64_t nq, int 
   if (q < nq && best[q * R + (R - 1)] == kEmptyKey) list[atomicAdd(n, 1)] = (int)q;
 }
 
+// 2 eps(q) per query (rounded up) for the windowed rerank of a BF16 list,
+// eps(q) bounding |scan key - exact distance| for every row (Q the staged
+// f32 query rows):
+//   DotProduct (key +<q~, x~> against the reference's sequential f32 sum):
+//   |<q~, x~> - <q, x>| <= |q~| max|x - x~| + |q - q~| max|x|         (A)
+//   the tensor core's f32 accumulation of Dp exact products,
+//   generously (Dp + 16) 2^-22 |q~| max|x~|                            (B)
+//   the reference's own sum, (dim + 4) 2^-23 |q| max|x|                 (E)
+//   CosineSimilarity (key -<q^, x^> on BF16 unit rows against the
+//   reference's f32 -ab / (sqrt(aa) sqrt(bb))): each unit row is rounded
+//   to f32 then BF16 (relative 2^-9 + 2^-24 per element), so
+//   |<q^, x^> - <u, v>| <= 2^-8 (1 + 2^-8) + 2^-8 for the exact unit
+//   rows u, v                                                           (A)
+//   (Dp + 16) 2^-22 (1 + 2^-8)^2 for the accumulation                   (B)
+//   and (2 dim + 8) 2^-24 for the reference's sums, roots and division  (E)
+//   (zero rows: both keys are 0).
+__global__ void rerank_slack_kernel(const float *Q, int64_t nq, int64_t ld, int64_t dim, int64_t Dp, int metric,
+                                    const double *qsq64, const float *dxmax, const float *xsqmax, float *slack) {
+  const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  double eps;
+  if (metric == M_COS) {
+    if (lane) return;
+    const double u = 0x1p-8;
+    eps = u * (1.0 + u) + u + (double)(Dp + 16) * 0x1p-22 * (1.0 + u) * (1.0 + u) + (double)(2 * dim + 8) * 0x1p-24;
+  } else {
+    double sb = 0.0, sd = 0.0;
+    for (int64_t t = lane; t < dim; t += 32) {
+      const float x = Q[q * ld + t];
+      const double b = (double)__bfloat162float(__float2bfloat16_rn(x));
+      sb += b * b;
+      sd += ((double)x - b) * ((double)x - b);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      sb += __shfl_xor_sync(0xffffffffu, sb, o);
+      sd += __shfl_xor_sync(0xffffffffu, sd, o);
+    }
+    if (lane) return;
+    const double qb = sqrt(sb) * (1.0 + 0x1p-40), dq = sqrt(sd) * (1.0 + 0x1p-40);
+    const double qn = sqrt(qsq64[q]) * (1.0 + 0x1p-40);
+    const double xn = sqrt((double)*xsqmax * (1.0 + 0x1p-22)), dx = (double)*dxmax;
+    const double xb = xn * (1.0 + 0x1p-8) + dx;
+    eps = qb * dx + dq * xn + (double)(Dp + 16) * 0x1p-22 * qb * xb + (double)(dim + 4) * 0x1p-23 * qn * xn;
+  }
+  slack[q] = nextafterf((float)(2.0 * eps * (1.0 + 0x1p-10)), INFINITY);
+}
+
 // The windowed rerank's candidates: query q's keys (R slots of best) whose
 // distance is at most the k-th smallest key's plus slack[q] (and a relative
 // 2^-20 against the rounding of that f32 addition), moved to the front of
@@ -998,6 +1089,26 @@ __global__ void rerank_window_kernel(const uint64_t *best, int R, const uint64_t
 __global__ void clear_lists_kernel(uint64_t *best, int R, const int *list, int64_t nl) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nl * R) best[(int64_t)list[i / R] * R + (i % R)] = kEmptyKey;
+}
+
+// e4m3 filter bound inputs per group of 32 rows, for ngroups groups (every
+// group of the image's tiles; rows past n excluded, a group without rows
+// gets {+inf, +inf, 0, 0}): {min |x|^2, min scale, max scale, 0}.  A column's Euclidean distance
+// qsq + |x|^2 - 2 qscale xscale acc is at least qsq + min|x|^2 - 2 qscale
+// (max scale if the slice's largest acc is positive, else min scale) x that
+// acc; a DotProduct key qscale xscale acc is at least qscale (max scale if
+// the smallest acc is negative, else min scale) x that acc.
+__global__ void group_meta_kernel(const float *xsq, const float *xscale, int64_t n, int64_t ngroups,
+                                  float4 *out) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroups) return;
+  float mq = __int_as_float(0x7f800000), mn = __int_as_float(0x7f800000), mx = 0.0f;
+  for (int64_t r = 32 * g; r < n && r < 32 * g + 32; ++r) {
+    mq = fminf(mq, xsq[r]);
+    mn = fminf(mn, xscale[r]);
+    mx = fmaxf(mx, xscale[r]);
+  }
+  out[g] = make_float4(mq, mn, mx, 0.0f);
 }
 
 // The largest of n non-negative floats (as ordered bits) into *out.
@@ -1059,6 +1170,8 @@ static int make_tmap(CUtensorMap *m, const void *ptr, int prec, int64_t Dp, int6
   return HORA_OK;
 }
 
+// Shared memory of the scan kernel: alignment slack, the query tile (and
+// the fold's A block), the ring, barriers and the hit staging.
 static int lp_smem_bytes(int nkb, int stages, bool fold) {
   return 1024 + nkb * kLpBM * 128 + (fold ? 4096 : 0) +
          stages * (nkb * kLpBN * 128 + (fold ? (int)kNormBytesB : 0)) + kLpBarSlots * 8 + kLpHitBytes;
@@ -1208,6 +1321,9 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
         HORA_TRY(normblk.reserve(std::max<int64_t>(h->n, 1) * 16 * 2));
         norm_block_kernel<<<ceil_div(h->n, 256), 256, 0, s>>>(h->xsq64.as<double>(), h->n,
                                                               normblk.as<__nv_bfloat16>());
+      }
+      if (h->metric != M_COS) {
+        // raw BF16 rows: the largest rounding residual (certified bounds)
         HORA_LAUNCHED();
         HORA_TRY(st->dxmax.reserve(sizeof(float)));
         HORA_CUDA_TRY(cudaMemsetAsync(st->dxmax.ptr, 0, sizeof(float), s));
@@ -1222,6 +1338,13 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
     HORA_LAUNCHED();
     f64_to_f32_kernel<<<ceil_div(h->n, 256), 256, 0, s>>>(h->xsq64.as<double>(), h->n, st->xsq.as<float>());
     HORA_LAUNCHED();
+    if (prec == HORA_PREC_FP8) {
+      const int64_t ng = ntiles * (kLpBN / 32);  // every group of the image's tiles
+      HORA_TRY(st->gmeta.reserve(sizeof(float4) * ng));
+      group_meta_kernel<<<(unsigned)ceil_div(ng, (int64_t)256), 256, 0, s>>>(st->xsq.as<float>(), st->xscale.as<float>(),
+                                                                             h->n, ng, st->gmeta.as<float4>());
+      HORA_LAUNCHED();
+    }
     const int64_t chunks = ntiles * kLpBN * (nkb * 8 + (fold ? 2 : 0));
     tile_image_kernel<<<ceil_div(chunks, 256), 256, 0, s>>>(rows.as<uint8_t>(), h->n, Dp * esz, nkb,
                                                             fold ? normblk.as<uint8_t>() : nullptr,
@@ -1280,6 +1403,10 @@ static int build_row_image(hora_index *h, const LowpState &L, const uint32_t *ro
   } else {
     to_e4m3_kernel<<<(unsigned)ceil_div(nimg, 8), 256, 0, s>>>(rowsf.as<float>(), nimg, ld, h->dim, Dp,
                                                                rows.as<uint8_t>(), out.xscale.as<float>());
+    HORA_LAUNCHED();
+    HORA_TRY(out.gmeta.reserve(sizeof(float4) * (nimg / 32)));
+    group_meta_kernel<<<(unsigned)ceil_div(nimg / 32, (int64_t)256), 256, 0, s>>>(
+        out.xsq.as<float>(), out.xscale.as<float>(), nimg, nimg / 32, out.gmeta.as<float4>());
     HORA_LAUNCHED();
   }
   const int64_t chunks = ntiles * kLpBN * (nkb * 8 + (fold ? 2 : 0));
@@ -1455,9 +1582,9 @@ static int ensure_pivots(hora_index *h, LowpState &L, cudaStream_t s) {
 // The sampled threshold of a wide R-best list (see the note on starting
 // thresholds) into ws.ptau.  The first ms rows of the sample image are an
 // even sample of the base: where r = R ms / n of them are expected below
-// the base's R-th key, the rs-th smallest sample key, rs = r + 3 sqrt(r) + 1,
-// has about R rs / r base rows below it, and at least R with high
-// probability.  The sample is scanned by the scan kernel in two chunks with
+// the base's R-th key, the rs-th smallest sample key, rs = r + 4 sqrt(r) + 2,
+// has about R rs / r base rows below it, and at least R unless the sample
+// count strays 4 standard deviations.  The sample is scanned by the scan kernel in two chunks with
 // the search's own queries: the first s1 = 2,048 rows densely (their rs
 // smallest keys, sorted), then the rest in filter mode from the k1-th of
 // those keys (the same rule with r1 = R s1 / n: a loose threshold, often
@@ -1471,13 +1598,13 @@ static int sample_threshold(hora_index *h, LowpState &L, int prec, int64_t nq, i
   *used = false;
   const int64_t n = h->n;
   const int64_t lim = std::min<int64_t>(std::min<int64_t>(n, kProbeSampleRows), n / 4) / kLpBN * kLpBN;
-  const int64_t ms = std::min<int64_t>(lim, round_up(ceil_div((int64_t)128 * n, (int64_t)R), kLpBN));
+  const int64_t ms = std::min<int64_t>(lim, round_up(ceil_div((int64_t)64 * n, (int64_t)R), kLpBN));
   const double r = (double)R * (double)ms / (double)n;
   if (r < 16.0) return HORA_OK;
-  const int rs = (int)std::ceil(r + 3.0 * std::sqrt(r)) + 1;
+  const int rs = (int)std::ceil(r + 4.0 * std::sqrt(r)) + 2;
   const int64_t s1 = std::min<int64_t>(ms, 2048);
   const double r1 = (double)R * (double)s1 / (double)n;
-  const int k1 = std::min(rs, (int)std::ceil(r1 + 3.0 * std::sqrt(r1)) + 1);
+  const int k1 = std::min(rs, (int)std::ceil(r1 + 4.0 * std::sqrt(r1)) + 2);
   const int caps = (int)round_up(std::max<int64_t>(s1, 4 * rs), 128);
   int64_t nres = 1024;
   while (nres < nq) nres <<= 1;
@@ -1495,6 +1622,7 @@ static int sample_threshold(hora_index *h, LowpState &L, int prec, int64_t nq, i
   u.xsq = L.sample.xsq.as<float>();
   u.xscale = L.sample.xscale.as<float>();
   u.xnorm = L.sample.xnorm.as<float>();
+  u.gmeta = L.sample.gmeta.as<float4>();
   u.nq = nq;
   u.qmap = nullptr;
   u.dense_hits = 0;
@@ -1538,10 +1666,13 @@ static int sample_threshold(hora_index *h, LowpState &L, int prec, int64_t nq, i
 // runs in BF16 whatever the base's precision, in the index's metric: unit
 // queries for CosineSimilarity); the probe scores members in the base's
 // precision (prec) and metric, from ws.lq (and ws.lqscale for FP8).
-// *order (when given) receives the queries in order of their nearest pivot.
+// *order (when given) receives the queries in order of their nearest pivot
+// (ws.pmem), *tq the tile map of their rows gathered in that order (ws.pqg,
+// valid until the next search on this workspace).
 static int probe_thresholds(hora_index *h, LowpState &L, int prec, int64_t nq, int R, int64_t Dp,
                             SearchWorkspace &ws, const CUtensorMap &ta16, const LpParams &lp, cudaStream_t s,
-                            const float *slack = nullptr, const uint32_t **order = nullptr) {
+                            const float *slack = nullptr, const uint32_t **order = nullptr,
+                            CUtensorMap *tq_out = nullptr) {
   const int C = L.pc;
   // sized for a power of two of at least 1,024 queries: a serving slot whose
   // batches vary reallocates (and with that waits for the device) rarely
@@ -1596,6 +1727,7 @@ static int probe_thresholds(hora_index *h, LowpState &L, int prec, int64_t nq, i
     HORA_LAUNCHED();
     CUtensorMap tq;
     HORA_TRY(make_tmap(&tq, ws.pqg.ptr, prec, Dp, nq, kLpBM));
+    if (tq_out) *tq_out = tq;
     LpParams t = lp;
     t.tiles = L.members.tiles.as<uint8_t>();
     t.xsq = L.members.xsq.as<float>();
@@ -1720,6 +1852,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   p.xsq = L.xsq.as<float>();
   p.xscale = L.xscale.as<float>();
   p.xnorm = h->xnorm.as<float>();
+  p.gmeta = L.gmeta.as<float4>();
   p.qsq = ws.lqsq.as<float>();
   p.qscale = ws.lqscale.as<float>();
   p.qnorm = ws.qnorm.as<float>();
@@ -1746,7 +1879,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     c.tpc = lp_tiles_per_cta(nl, c0);
     HORA_TRY(launch_lp(prec, h->metric, TILE_DENSE, tm, L, c, s));
     // bestR is an intermediate list: only its R-th key (the threshold) needs its place
-    HORA_TRY(launch_merge_topk(bestR, R, c.cand, count, cap, (int)c0, qlist, nl, flags, ovc, s, false));
+    HORA_TRY(launch_merge_topk(bestR, R, c.cand, count, cap, (int)c0, qlist, nl, flags, ovc, s, false, true));
     int64_t done = c0;
     while (done < n) {
       // each chunk at most 1.5x the rows scanned so far and at least 2,048
@@ -1763,7 +1896,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
       c.tpc = lp_tiles_per_cta(nl, w);
       c.dense_hits = (double)R * (kLpBN * c.tpc / 4) / (double)done >= 20.0;
       HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, tm, L, c, s));
-      HORA_TRY(launch_merge_topk(bestR, R, c.cand, count, cap, 0, qlist, nl, flags, ovc, s, false));
+      HORA_TRY(launch_merge_topk(bestR, R, c.cand, count, cap, 0, qlist, nl, flags, ovc, s, false, true));
       done += w;
     }
     return HORA_OK;
@@ -1779,6 +1912,8 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   int *lerr = ws.lerr.as<int>();  // [0] a pipeline wait timed out, [1] short lists after the probed pass
   const uint32_t *rr_order = nullptr;  // the rerank's query order (clusters: by nearest pivot)
   bool probe = false;                  // a starting threshold per query
+  CUtensorMap tf = ta;                 // the filter pass's query rows ...
+  const int *fmap = nullptr;           // ... and their query ids (null: in query order)
   if (probe_eligible(h) && R > kProbeClusterMaxR && R <= kProbeMaxR) {
     HORA_TRY(ensure_pivots(h, L, s));
     HORA_TRY(sample_threshold(h, L, prec, nq, R, ws, ta, p, s, &probe));
@@ -1796,17 +1931,22 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
       HORA_LAUNCHED();
       HORA_TRY(make_tmap(&ta16, ws.lq16.ptr, HORA_PREC_BF16, Dp16, nq, kLpBM));
     }
-    HORA_TRY(probe_thresholds(h, L, prec, nq, R, Dp, ws, ta16, p, s, nullptr, &rr_order));
+    HORA_TRY(probe_thresholds(h, L, prec, nq, R, Dp, ws, ta16, p, s, nullptr, &rr_order, &tf));
+    fmap = reinterpret_cast<const int *>(rr_order);
   }
   if (probe) {
-    // one filter pass from the starting thresholds
-    p.tau0 = ws.ptau.as<float>();
-    p.dense_hits = 0;
+    // one filter pass from the starting thresholds; after the cluster probe
+    // over the queries gathered in pivot order, so that a drain warp's 32
+    // query rows share their near rows (the e4m3 slice skip is a warp vote)
+    LpParams f = p;
+    f.qmap = fmap;
+    f.tau0 = ws.ptau.as<float>();
+    f.dense_hits = 0;
     for (int64_t lo = 0; lo < n; lo += max_chunk) {
-      p.r_begin = lo;
-      p.r_end = std::min<int64_t>(n, lo + max_chunk);
-      p.tpc = lp_tiles_per_cta(nq, p.r_end - p.r_begin);
-      HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, ta, L, p, s));
+      f.r_begin = lo;
+      f.r_end = std::min<int64_t>(n, lo + max_chunk);
+      f.tpc = lp_tiles_per_cta(nq, f.r_end - f.r_begin);
+      HORA_TRY(launch_lp(prec, h->metric, TILE_FILTER, tf, L, f, s));
       HORA_TRY(launch_merge_topk(bestR, R, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s, false));
     }
     short_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(bestR, R, nq, lerr + 1, ws.qlist.as<int>());
@@ -1818,13 +1958,14 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   // the host learns whether a candidate list overflowed or came out short
   // (rare), so the stream runs on without a round trip, and redone after
   HORA_TRY(ws.tmp.reserve(sizeof(uint64_t) * nq * R));
-  // A wide BF16 Euclidean list is reranked only where the exact k best can
-  // lie: with eps(q) the certified bound on |scan key - exact distance| (the
-  // exact search's, see exact_tc_slack_kernel), k candidates have exact
+  // A wide BF16 list is reranked only where the exact k best can lie: with
+  // eps(q) a certified bound on |scan key - exact distance| (Euclidean: the
+  // exact search's, see exact_tc_slack_kernel; DotProduct and
+  // CosineSimilarity: rerank_slack_kernel), k candidates have exact
   // distances at most T + eps (T the k-th smallest scan key of the list),
   // so a candidate whose scan key exceeds T + 2 eps is beaten by k others
   // and cannot be among the k best: the result equals the rerank of all R.
-  const bool window = prec == HORA_PREC_BF16 && h->metric == M_L2 && L.pc > 0 && R >= 512 && R >= 4 * k;
+  const bool window = prec == HORA_PREC_BF16 && L.pc > 0 && R >= 512 && R >= 4 * k;
   uint64_t *wkth = nullptr;
   uint32_t *wcount = nullptr;
   if (window) {
@@ -1832,8 +1973,13 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
     HORA_TRY(ws.rwin.reserve(sizeof(uint64_t) * nq * k + sizeof(uint32_t) * nq));
     wkth = ws.rwin.as<uint64_t>();
     wcount = reinterpret_cast<uint32_t *>(wkth + nq * k);
-    exact_tc_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, qsq64,
-                                                          L.dxmax.as<float>(), L.xsqmax.as<float>(),
+    if (h->metric == M_L2)
+      exact_tc_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, qsq64,
+                                                            L.dxmax.as<float>(), L.xsqmax.as<float>(),
+                                                            ws.xslack.as<float>());
+    else
+      rerank_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, h->metric,
+                                                          qsq64, L.dxmax.as<float>(), L.xsqmax.as<float>(),
                                                           ws.xslack.as<float>());
     HORA_LAUNCHED();
   }

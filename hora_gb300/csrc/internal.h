@@ -62,10 +62,12 @@ int launch_rerank_exact(int metric, const float *Q, int64_t ld, const float *X, 
 // Merges each query's candidates into its sorted k-best key list (dedup by
 // key).  dense_n > 0: candidates are the first dense_n slots, count ignored.
 // sorted = false (an intermediate list) may leave the k-1 smallest keys
-// unordered; the k-th (largest) key is always at position k-1.
+// unordered; the k-th (largest) key is always at position k-1.  disjoint:
+// the candidates of listed queries (qlist) are rows their lists do not hold
+// (a new chunk), so no deduplication is needed.
 int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap,
                       int dense_n, const int *qlist, int64_t nlist, uint8_t *ovf_flag,
-                      uint32_t *ovf_counter, cudaStream_t s, bool sorted = true);
+                      uint32_t *ovf_counter, cudaStream_t s, bool sorted = true, bool disjoint = false);
 int merge_smem_bytes(int k, int cap);
 // Sorted keys -> (ids via the id table, distances); empty keys -> NO_ID, +inf.
 int launch_keys_to_results(const uint64_t *keys, int64_t n_keys, const uint64_t *id_table,

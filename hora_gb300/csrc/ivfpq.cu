@@ -881,9 +881,9 @@ constexpr int kSelDigitBits = 11, kSelNB = 1 << kSelDigitBits;
 
 // Every lane of the warp: the bin of a kSelNB-bin histogram whose
 // cumulative count first reaches rem (1 <= rem <= total) and the count below
-// it.  Lane l owns bins [64 l, 64 l + 64), summed in a rotated order
-// (conflict-free banks); the warp then scans the chosen lane's 64 bins
-// together, two per lane.
+// it.  Lane l owns bins [nb l, nb l + nb), nb = kSelNB / 32, summed in a
+// rotated order (conflict-free banks); the warp then scans the chosen lane's
+// nb bins together, two per lane.
 __device__ __forceinline__ void warp_find_bin_all(const uint32_t *hist, uint32_t rem, int &bin,
                                                   uint32_t &below) {
   constexpr int nb = kSelNB / 32;
@@ -901,8 +901,10 @@ __device__ __forceinline__ void warp_find_bin_all(const uint32_t *hist, uint32_t
   const unsigned who = __ballot_sync(0xffffffffu, exc < rem && inc >= rem);
   const int src = who ? __ffs(who) - 1 : 31;
   const uint32_t base = __shfl_sync(0xffffffffu, exc, src);
-  // the chosen lane's 64 bins: bins 2 l, 2 l + 1 of its range on lane l
-  const uint32_t b0 = hist[src * nb + 2 * lane], b1 = hist[src * nb + 2 * lane + 1];
+  // the chosen lane's nb bins: bins 2 l, 2 l + 1 of its range on lane l
+  static_assert(nb % 2 == 0 && nb <= 64, "two bins per lane");
+  const uint32_t b0 = 2 * lane < nb ? hist[src * nb + 2 * lane] : 0u;
+  const uint32_t b1 = 2 * lane + 1 < nb ? hist[src * nb + 2 * lane + 1] : 0u;
   uint32_t pinc = b0 + b1;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -952,7 +954,7 @@ __device__ __forceinline__ void cta_select_group(uint32_t *dk, int stride, uint3
     q[kStCnt] = 0;
   }
   __syncthreads();
-  for (int pass = 0; pass < 8; ++pass) {
+  for (int pass = 0; pass < 2 * (32 + kSelDigitBits - 1) / kSelDigitBits; ++pass) {
 #pragma unroll
     for (int g = 0; g < G; ++g) {
       if (g >= gc) break;

@@ -293,14 +293,15 @@ __device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
 
 template <bool SORTED>
 __global__ void __launch_bounds__(kWmWarps * 32, 3) merge_warp_kernel(
-    uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n, int64_t nq,
-    uint8_t *ovf_flag, uint32_t *ovf_counter) {
+    uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n, const int *qlist,
+    int64_t nq, uint8_t *ovf_flag, uint32_t *ovf_counter) {
   __shared__ uint32_t hist_all[kWmWarps][256];
   __shared__ uint64_t sel_all[kWmWarps][kWmMaxK];
   __shared__ int dig_all[kWmWarps][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t q = (int64_t)blockIdx.x * kWmWarps + warp;
-  if (q >= nq) return;
+  const int64_t qi = (int64_t)blockIdx.x * kWmWarps + warp;
+  if (qi >= nq) return;
+  const int64_t q = qlist ? qlist[qi] : qi;
   uint32_t *hist = hist_all[warp];
   uint64_t *sel = sel_all[warp];
   int *dig = dig_all[warp];
@@ -483,14 +484,14 @@ constexpr int kMbThreads = 256, kMbRegs = 48, kMbMaxK = 4096;
 
 template <bool SORTED>
 __global__ void __launch_bounds__(kMbThreads, 2) merge_block_kernel(
-    uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n,
+    uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap, int dense_n, const int *qlist,
     uint8_t *ovf_flag, uint32_t *ovf_counter) {
   extern __shared__ uint64_t mb_sel[];  // P >= k winners
   __shared__ uint32_t hist[kSelBins];
   __shared__ uint32_t red[3][kMbThreads / 32];
   __shared__ int sc[8];  // [1] bin, [2] below, [3] taken, [4] remaining, [5] at bin
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t q = blockIdx.x;
+  const int64_t q = qlist ? qlist[blockIdx.x] : blockIdx.x;
   uint32_t c = dense_n > 0 ? (uint32_t)dense_n : count[q];
   if (c == 0) return;
   const bool ovf = c > (uint32_t)cap;
@@ -671,24 +672,27 @@ int merge_smem_bytes(int k, int cap) {
 
 int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *count, int cap,
                       int dense_n, const int *qlist, int64_t nlist, uint8_t *ovf_flag,
-                      uint32_t *ovf_counter, cudaStream_t s, bool sorted) {
+                      uint32_t *ovf_counter, cudaStream_t s, bool sorted, bool disjoint) {
   if (nlist <= 0) return HORA_OK;
   HORA_SMEM_ATTR(merge_topk_kernel, 200 * 1024);
   HORA_SMEM_ATTR(merge_select_kernel, 200 * 1024);
   const int cmax = dense_n > 0 ? dense_n : cap;
-  if (!qlist && k <= kWmMaxK) {
+  // a query list takes the radix merges only for candidates disjoint from
+  // the list (the rescans after an overflow re-offer rows: they deduplicate)
+  const bool radix = !qlist || disjoint;
+  if (radix && k <= kWmMaxK) {
     ProfScope ps("topk_merge", s);
     const unsigned grid = (unsigned)ceil_div(nlist, (int64_t)kWmWarps);
     if (sorted)
-      merge_warp_kernel<true><<<grid, kWmWarps * 32, 0, s>>>(best, k, cand, count, cap, dense_n, nlist,
+      merge_warp_kernel<true><<<grid, kWmWarps * 32, 0, s>>>(best, k, cand, count, cap, dense_n, qlist, nlist,
                                                                  ovf_flag, ovf_counter);
     else
-      merge_warp_kernel<false><<<grid, kWmWarps * 32, 0, s>>>(best, k, cand, count, cap, dense_n, nlist,
+      merge_warp_kernel<false><<<grid, kWmWarps * 32, 0, s>>>(best, k, cand, count, cap, dense_n, qlist, nlist,
                                                                   ovf_flag, ovf_counter);
     HORA_LAUNCHED();
     return HORA_OK;
   }
-  if (!qlist && k <= kMbMaxK && cmax + k <= kMbThreads * kMbRegs) {
+  if (radix && k <= kMbMaxK && cmax + k <= kMbThreads * kMbRegs) {
     int P = 1;
     while (P < k) P <<= 1;
     const int smem = P * 8;
@@ -697,10 +701,10 @@ int launch_merge_topk(uint64_t *best, int k, const uint64_t *cand, uint32_t *cou
     ProfScope ps("topk_merge", s);
     if (sorted)
       merge_block_kernel<true><<<(unsigned)nlist, kMbThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
-                                                                      ovf_flag, ovf_counter);
+                                                                      qlist, ovf_flag, ovf_counter);
     else
       merge_block_kernel<false><<<(unsigned)nlist, kMbThreads, smem, s>>>(best, k, cand, count, cap, dense_n,
-                                                                       ovf_flag, ovf_counter);
+                                                                       qlist, ovf_flag, ovf_counter);
     HORA_LAUNCHED();
     return HORA_OK;
   }

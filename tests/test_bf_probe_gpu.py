@@ -71,13 +71,13 @@ def sample_rows(n, m):
 
 def test_short_lists_fall_back(hora, gpu):
     """A base where exactly the sampled rows lie near the queries: for R =
-    4,096 on 65,536 rows the sampled threshold (the 163rd of the first 2,048
-    sample rows' keys) keeps only ~163 rows, every list comes out short, and
+    4,096 on 65,536 rows the sampled threshold (the 98th of the first 1,024
+    sample rows' keys) keeps only ~98 rows, every list comes out short, and
     the chunked schedule answers all of them, with the same result."""
     rng = np.random.default_rng(5)
     n = 65_536
     base = (50.0 + rng.standard_normal((n, 32))).astype(np.float32)
-    near = np.unique(sample_rows(n, 2048))
+    near = np.unique(sample_rows(n, 1024))
     base[near] = rng.standard_normal((near.size, 32)).astype(np.float32)
     q = rng.standard_normal((40, 32)).astype(np.float32)
     ix = build(hora, base, 4096)
@@ -184,16 +184,17 @@ def test_dot_and_cosine_probe_matches_chunked(hora, oracle, gpu, metric, prec, R
         assert d1[qi, 0] == oracle.metric(q[qi], base[int(ids1[qi, 0])], metric)
 
 
-def test_windowed_rerank_equals_full_rerank(hora, oracle, gpu):
-    """A wide BF16 Euclidean list (R = 4,096 for k = 100) is reranked only
-    within T + 2 eps of its k-th scan key (eps the certified bound on scan
-    key vs exact distance); k = 1,100 (R < 4k) reranks all 4,096.  The same
-    R-best set, so the first 100 of the wide answer must equal the windowed
-    one bit for bit, and both the exact FP32 search's distances."""
+@pytest.mark.parametrize("metric", [3, 2, 4])
+def test_windowed_rerank_equals_full_rerank(hora, oracle, gpu, metric):
+    """A wide BF16 list (R = 4,096 for k = 100) is reranked only within
+    T + 2 eps of its k-th scan key (eps the certified bound on scan key vs
+    exact distance, per metric); k = 1,100 (R < 4k) reranks all 4,096.  The
+    same R-best set, so the first 100 of the wide answer must equal the
+    windowed one bit for bit, and both the exact FP32 search's distances."""
     from hora_gb300 import synth
     base = synth.mixture(100_000, 64, 256, stream=49)
     q = synth.mixture(300, 64, 256, stream=50)
-    ix = build(hora, base, 4096)
+    ix = build(hora, base, 4096, metric=metric)
     ids_w, d_w = ix.search_batch(q, 100)
     ids_f, d_f = ix.search_batch(q, 1100)
     np.testing.assert_array_equal(ids_w, ids_f[:, :100])
@@ -202,3 +203,21 @@ def test_windowed_rerank_equals_full_rerank(hora, oracle, gpu):
     ix.set_option(hora.Option.EXACT_TC, 0)
     ids_e, d_e = ix.search_batch(q, 100)
     np.testing.assert_array_equal(d_w, d_e)
+
+
+@pytest.mark.parametrize("metric", [3, 2])
+def test_fp8_wide_list_holds_exact_top_k(hora, gpu, metric):
+    """e4m3 filter passes skip a 32-column slice when a lower bound on its
+    distances (from the slice's extreme accumulator and the rows' smallest
+    squared norm and scale range) clears the threshold.  With a 4,096-wide
+    list the exact 10 best of every query must survive the filter: the
+    answer's distances equal the exact FP32 search's."""
+    from hora_gb300 import synth
+    base = synth.mixture(100_000, 64, 256, stream=51)
+    q = synth.mixture(300, 64, 256, stream=52)
+    ix = build(hora, base, 4096, prec=2, metric=metric)
+    ids8, d8 = ix.search_batch(q, 10)
+    ix.set_option(hora.Option.PRECISION, 0)
+    ix.set_option(hora.Option.EXACT_TC, 0)
+    ids32, d32 = ix.search_batch(q, 10)
+    np.testing.assert_array_equal(d8, d32)
