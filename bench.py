@@ -52,6 +52,9 @@ def args_parse():
                     help="only build the IVF-PQ index of the IVF section and run one search of "
                          "--nq queries at --nprobe (a small case for ncu captures)")
     ap.add_argument("--nprobe", type=int, default=2)
+    ap.add_argument("--ivf-lists", type=int, default=1024, help="coarse lists of the --ivf-profile index")
+    ap.add_argument("--coarse-fp32", action="store_true",
+                    help="--ivf-profile: the FP32 coarse probe (HORA_OPT_EXACT_TC 0) instead of the certified one")
     ap.add_argument("--small", action="store_true", help="tiny workload for a quick check")
     ap.add_argument("--nq", type=int, default=0, help="override the number of queries (profiling)")
     ap.add_argument("--no-ivf", action="store_true", help="skip the IVF-PQ section")
@@ -533,9 +536,11 @@ def run_ivf_profile(a, H, base, q):
     the first 500k items, exact rerank of 100) and one search of the given
     queries at --nprobe."""
     import torch
-    params = H.IVFPQParams(n_sub=32, sub_bits=8, n_kmeans_center=1024, search_n_center=a.nprobe,
+    params = H.IVFPQParams(n_sub=32, sub_bits=8, n_kmeans_center=a.ivf_lists, search_n_center=a.nprobe,
                            train_epoch=a.ivf_epochs)
     ix = H.IVFPQIndex(DIM, params)
+    if a.coarse_fp32:
+        ix.set_option(H.Option.EXACT_TC, 0)
     ix.set_option(H.Option.TRAIN_SIZE, min(500_000, base.shape[0]))
     ix.madd(torch.from_numpy(base).cuda(), None)
     t0 = time.perf_counter()
@@ -553,6 +558,7 @@ def run_ivf_profile(a, H, base, q):
     H._lib.profile(False)
     kern = {k: {"launches": v[0] // 3, "ms": v[1] / 3} for k, v in H._lib.profile_report().items()}
     print(json.dumps({"workload": "IVF-PQ profile case", "queries": q.shape[0], "nprobe": a.nprobe,
+                      "lists": a.ivf_lists, "coarse": "fp32" if a.coarse_fp32 else "default",
                       "build_s": build_s, "first_search_ms": first_ms,
                       "search_ms": json.loads(ix.idx_info())["last_search_ms"], "kernels_per_search": kern}),
           flush=True)

@@ -141,7 +141,7 @@ int stage_queries(hora_index *h, const float *queries, int64_t nq, SearchWorkspa
                                     cudaMemcpyHostToDevice, s));
   float *qn = nullptr;
   double *qsq = nullptr;
-  if (h->metric == M_COS || h->precision != HORA_PREC_FP32 || exact_tc_eligible(h, 1)) {
+  if (h->metric == M_COS || h->precision != HORA_PREC_FP32 || exact_tc_eligible(h, 1) || coarse_tc_eligible(h)) {
     HORA_TRY(ws.qnorm.reserve(sizeof(float) * nq + sizeof(double) * nq + 16));
     qn = ws.qnorm.as<float>();
     qsq = reinterpret_cast<double *>(ws.qnorm.as<char>() + round_up(sizeof(float) * nq, 16));

@@ -534,7 +534,9 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     uint64_t *hbuf = reinterpret_cast<uint64_t *>(bars + kLpBarSlots);
     uint64_t amin = kEmptyKey;  // TILE_ARGMIN: this thread's smallest key so far
     DrainCtx c{p.cand, p.count, hbuf + (threadIdx.x - 64), qid, 0, p.r_begin, r_end, p.cap, qa, tau_d, tau_r};
-    float *orow = MODE == TILE_DIST && qid >= 0 ? p.out_dist + qrow * p.ldo - row0 : nullptr;
+    // TILE_DIST: column = image row - the item's first row (work items) or
+    // the launch's first row
+    float *orow = MODE == TILE_DIST && qid >= 0 ? p.out_dist + qrow * p.ldo - (p.items ? row0 : p.r_begin) : nullptr;
     int nb = 0;  // keys staged in this thread's column
     for (int t = 0; t < T; ++t) {
       const int b = t % kLpNB, jb = t / kLpNB;
@@ -2268,6 +2270,222 @@ int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, 
     HORA_LAUNCHED();
     h->last_retries = retries;
   }
+  return HORA_OK;
+}
+
+
+// ---- the IVF coarse probe, certified on the tensor cores -------------------------------
+// The reference ranks every centre by its exact FP32 distance and probes the
+// pmax nearest (ties to the lower centre).  Here a BF16 pass of the scan
+// kernel (dense distances) over the centres' image gives each query its
+// pmax-th smallest approximate key T; with eps(q) the certified bound on
+// |BF16 key - exact distance| (Euclidean: exact_tc_slack_kernel's, the
+// centres playing the rows; DotProduct and CosineSimilarity:
+// rerank_slack_kernel's), pmax centres have exact distances at most T + eps,
+// so a centre whose approximate key exceeds T + 2 eps is beaten by pmax
+// others and is not probed.  The centres within T + 2 eps are rescored in
+// the reference's op order (the rerank kernel) and the pmax smallest exact
+// keys kept: the FP32 probe's result.
+struct CoarseTc {
+  int metric = 0;
+  int64_t C = 0, Dp = 0;
+  int nkb = 0;
+  DevBuf tiles;     // the centres' BF16 tile image (the scan's layout for the metric)
+  DevBuf dxmax;     // 1 f32: the largest |c - bf16(c)| (Euclidean, DotProduct)
+  DevBuf xsqmax;    // 1 f32: the largest squared centre norm
+};
+
+void coarse_tc_free(CoarseTc *p) { delete p; }
+
+// Below this many lists the FP32 pass is the cheaper (1,024 lists: 0.24 ms
+// per 10k queries against 0.30 ms for the BF16 pass with its rescoring).
+constexpr int64_t kCoarseTcMinLists = 2048;
+
+bool coarse_tc_eligible(const hora_index *h) {
+  return h->exact_tc && h->kind == HORA_INDEX_IVFPQ && (int64_t)h->ivf.n_kmeans_center >= kCoarseTcMinLists &&
+         (h->metric == M_L2 || h->metric == M_IP || h->metric == M_COS) && round_up((int64_t)h->dim, 64) / 64 <= 2;
+}
+
+// A query's candidate centres: those whose approximate distance (row q of
+// dist) is at most the pmax-th smallest approximate key plus slack[q] (and
+// a relative 2^-20 against the rounding of that f32 addition), as keys at
+// the front of its C slots of out, their number to count[q].  One warp per
+// query.
+__global__ void coarse_window_kernel(const float *dist, int64_t C, const uint64_t *kth, int pmax,
+                                     const float *slack, int64_t nq, uint64_t *out, uint32_t *count) {
+  const int64_t q = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  const uint64_t tk = kth[q * pmax + (pmax - 1)];
+  float w = __int_as_float(0x7f800000);
+  if (tk != kEmptyKey) {
+    const float t = key_dist(tk) + slack[q];
+    w = t + 0x1p-20f * fabsf(t);
+  }
+  uint32_t n = 0;
+  for (int64_t c0 = 0; c0 < C; c0 += 32) {
+    const int64_t c = c0 + lane;
+    const float d = c < C ? dist[q * C + c] : __int_as_float(0x7f800000);
+    const bool keep = c < C && d <= w;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) out[q * C + n + __popc(m & ((1u << lane) - 1u))] = make_key(d, (uint32_t)c);
+    n += __popc(m);
+  }
+  if (lane == 0) count[q] = n;
+}
+
+// The exact keys of a query's candidate centres (count[q] of them at the
+// front of its C slots of keys, centre rows in the low words), rescored in
+// the reference's op order (the exact tile kernel's dist_op sequence over
+// the dimensions; the cosine from the dot and the two norms), in place.
+// One warp per query, one candidate per lane at a time.
+template <int MT>
+__global__ void coarse_rescore_kernel(const float *Q, int64_t ld, const float *X, int64_t dim, const float *qnorm,
+                                      const float *xnorm, int64_t nq, int64_t C, const uint32_t *count,
+                                      uint64_t *keys) {
+  const int64_t q = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  const int64_t n = (int64_t)count[q] < C ? (int64_t)count[q] : C;
+  constexpr int OP = MT == M_COS ? M_IP : MT;
+  for (int64_t i = lane; i < n; i += 32) {
+    const uint32_t row = key_row(keys[q * C + i]);
+    const float *qr = Q + q * ld, *xr = X + (int64_t)row * ld;
+    float s = 0.0f;
+    for (int64_t d = 0; d < dim; ++d) s = dist_op<OP>(s, qr[d], xr[d]);
+    if (MT == M_COS) s = cosine_from_dot(s, qnorm[q], xnorm[row]);
+    keys[q * C + i] = make_key(s, row);
+  }
+}
+
+static int ensure_coarse_tc(hora_index *h, const float *centers, int64_t C, cudaStream_t s) {
+  if (h->coarse_tc && h->coarse_tc->C == C && h->coarse_tc->metric == h->metric) return HORA_OK;
+  std::unique_ptr<CoarseTc, CoarseTcDeleter> st(new CoarseTc());
+  st->metric = h->metric;
+  st->C = C;
+  st->Dp = round_up((int64_t)h->dim, 64);
+  st->nkb = (int)(st->Dp / 64);
+  const bool fold = h->metric == M_L2, cos = h->metric == M_COS;
+  const int64_t ld = h->ld, Dp = st->Dp, ntiles = ceil_div(C, (int64_t)kLpBN);
+  const int64_t tile_bytes = (int64_t)st->nkb * kLpBN * 128 + (fold ? kNormBytesB : 0);
+  DevBuf crow, cnb, csq, csqf;  // staging, freed on return
+  HORA_TRY(crow.reserve(sizeof(__nv_bfloat16) * C * Dp));
+  HORA_TRY(cnb.reserve(sizeof(__nv_bfloat16) * C * 16));
+  HORA_TRY(csq.reserve(sizeof(double) * C));
+  HORA_TRY(csqf.reserve(sizeof(float) * C));
+  HORA_TRY(st->tiles.reserve(ntiles * tile_bytes));
+  HORA_TRY(st->dxmax.reserve(sizeof(float)));
+  HORA_TRY(st->xsqmax.reserve(sizeof(float)));
+  HORA_CUDA_TRY(cudaMemsetAsync(st->dxmax.ptr, 0, sizeof(float), s));
+  HORA_CUDA_TRY(cudaMemsetAsync(st->xsqmax.ptr, 0, sizeof(float), s));
+  HORA_TRY(launch_row_norms(centers, C, ld, h->dim, nullptr, csq.as<double>(), s));
+  to_bf16_kernel<<<(unsigned)ceil_div(C * Dp, 256), 256, 0, s>>>(centers, C, ld, h->dim, Dp,
+                                                                 cos ? csq.as<double>() : nullptr,
+                                                                 crow.as<__nv_bfloat16>());
+  HORA_LAUNCHED();
+  if (fold) {
+    norm_block_kernel<<<(unsigned)ceil_div(C, 256), 256, 0, s>>>(csq.as<double>(), C, cnb.as<__nv_bfloat16>());
+    HORA_LAUNCHED();
+  }
+  tile_image_kernel<<<(unsigned)ceil_div(ntiles * kLpBN * (st->nkb * 8 + 2), 256), 256, 0, s>>>(
+      crow.as<uint8_t>(), C, Dp * 2, st->nkb, fold ? cnb.as<uint8_t>() : nullptr, tile_bytes, ntiles,
+      st->tiles.as<uint8_t>());
+  HORA_LAUNCHED();
+  if (!cos) {
+    bf16_residual_max_kernel<<<(unsigned)ceil_div(C, 8), 256, 0, s>>>(centers, C, ld, h->dim,
+                                                                       st->dxmax.as<unsigned>());
+    HORA_LAUNCHED();
+  }
+  f64_to_f32_kernel<<<(unsigned)ceil_div(C, 256), 256, 0, s>>>(csq.as<double>(), C, csqf.as<float>());
+  HORA_LAUNCHED();
+  max_nonneg_kernel<<<152, 256, 0, s>>>(csqf.as<float>(), C, st->xsqmax.as<unsigned>());
+  HORA_LAUNCHED();
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));  // the staging buffers are freed on return
+  h->coarse_tc = std::move(st);
+  return HORA_OK;
+}
+
+int coarse_tc_probe(hora_index *h, const float *centers, const float *cnorm, int64_t C, int64_t nq, int pmax,
+                    SearchWorkspace &ws, float *dist, uint64_t *probes, cudaStream_t s) {
+  if (nq <= 0) return HORA_OK;
+  HORA_TRY(ensure_coarse_tc(h, centers, C, s));
+  const CoarseTc &T = *h->coarse_tc;
+  const int64_t Dp = T.Dp;
+  const bool fold = h->metric == M_L2;
+  HORA_TRY(ws.lq.reserve(nq * Dp * 2));
+  HORA_TRY(ws.lqsq.reserve(sizeof(float) * nq));
+  HORA_TRY(ws.lerr.reserve(16));
+  HORA_TRY(ws.xslack.reserve(sizeof(float) * nq));
+  HORA_TRY(ws.ccand.reserve(sizeof(uint64_t) * nq * C + sizeof(uint32_t) * nq));
+  HORA_TRY(ws.ovf_flag.reserve(nq));
+  HORA_TRY(ws.ovf_counter.reserve(sizeof(uint32_t)));
+  uint64_t *cand = ws.ccand.as<uint64_t>();
+  uint32_t *count = reinterpret_cast<uint32_t *>(cand + nq * C);
+  const double *qsq64 = reinterpret_cast<const double *>(ws.qnorm.as<char>() + round_up(sizeof(float) * nq, 16));
+  {
+    ProfScope ps("coarse_tc", s);
+    to_bf16_kernel<<<(unsigned)ceil_div(nq * Dp, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp,
+                                                                    h->metric == M_COS ? qsq64 : nullptr,
+                                                                    ws.lq.as<__nv_bfloat16>());
+    HORA_LAUNCHED();
+    f64_to_f32_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(qsq64, nq, ws.lqsq.as<float>());
+    HORA_LAUNCHED();
+    HORA_CUDA_TRY(cudaMemsetAsync(ws.lerr.ptr, 0, 16, s));
+    CUtensorMap ta;
+    HORA_TRY(make_tmap(&ta, ws.lq.ptr, HORA_PREC_BF16, Dp, nq, kLpBM));
+    LpParams p{};
+    p.nq = nq;
+    p.nkb = T.nkb;
+    p.stages = lp_stages(T.nkb, fold);
+    p.tiles = T.tiles.as<uint8_t>();
+    p.qsq = ws.lqsq.as<float>();
+    p.qnorm = ws.qnorm.as<float>();
+    p.err = ws.lerr.as<int>();
+    p.r_begin = 0;
+    p.r_end = C;
+    p.tpc = lp_tiles_per_cta(nq, C);
+    p.out_dist = dist;
+    p.ldo = C;
+    if (h->metric == M_L2)
+      HORA_TRY((launch_lp3<HORA_PREC_BF16, M_L2, TILE_DIST>(ta, p, s)));
+    else if (h->metric == M_IP)
+      HORA_TRY((launch_lp3<HORA_PREC_BF16, M_IP, TILE_DIST>(ta, p, s)));
+    else
+      HORA_TRY((launch_lp3<HORA_PREC_BF16, M_COS, TILE_DIST>(ta, p, s)));
+    if (fold)
+      exact_tc_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, qsq64,
+                                                            T.dxmax.as<float>(), T.xsqmax.as<float>(),
+                                                            ws.xslack.as<float>());
+    else
+      rerank_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, h->metric,
+                                                          qsq64, T.dxmax.as<float>(), T.xsqmax.as<float>(),
+                                                          ws.xslack.as<float>());
+    HORA_LAUNCHED();
+  }
+  HORA_TRY(launch_rows_topk(dist, nq, C, C, pmax, probes, s));
+  coarse_window_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(dist, C, probes, pmax, ws.xslack.as<float>(), nq,
+                                                                 cand, count);
+  HORA_LAUNCHED();
+  {
+    const unsigned g = (unsigned)ceil_div(nq, 8);
+    if (h->metric == M_L2)
+      coarse_rescore_kernel<M_L2><<<g, 256, 0, s>>>(ws.q.as<float>(), h->ld, centers, h->dim, ws.qnorm.as<float>(),
+                                                    cnorm, nq, C, count, cand);
+    else if (h->metric == M_IP)
+      coarse_rescore_kernel<M_IP><<<g, 256, 0, s>>>(ws.q.as<float>(), h->ld, centers, h->dim, ws.qnorm.as<float>(),
+                                                    cnorm, nq, C, count, cand);
+    else
+      coarse_rescore_kernel<M_COS><<<g, 256, 0, s>>>(ws.q.as<float>(), h->ld, centers, h->dim, ws.qnorm.as<float>(),
+                                                     cnorm, nq, C, count, cand);
+    HORA_LAUNCHED();
+  }
+  HORA_CUDA_TRY(cudaMemsetAsync(probes, 0xff, sizeof(uint64_t) * nq * pmax, s));
+  HORA_TRY(launch_merge_topk(probes, pmax, cand, count, (int)C, 0, nullptr, nq, ws.ovf_flag.as<uint8_t>(),
+                             ws.ovf_counter.as<uint32_t>(), s, true));
+  int err = 0;
+  HORA_CUDA_TRY(cudaMemcpyAsync(&err, ws.lerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (err) return fail(HORA_ETIMEDOUT, "tensor-core coarse pass: a pipeline wait timed out");
   return HORA_OK;
 }
 

@@ -11,13 +11,16 @@ namespace hora {
 
 struct IvfState;   // ivfpq.cu
 struct LowpState;  // bf_lowp.cu
+struct CoarseTc;   // bf_lowp.cu
 struct NprobeModel;  // nprobe_mlp.cu
 
 void ivf_state_free(IvfState *);
 void lowp_state_free(LowpState *);
+void coarse_tc_free(CoarseTc *);
 void nprobe_model_free(NprobeModel *);
 struct IvfDeleter { void operator()(IvfState *p) const { ivf_state_free(p); } };
 struct LowpDeleter { void operator()(LowpState *p) const { lowp_state_free(p); } };
+struct CoarseTcDeleter { void operator()(CoarseTc *p) const { coarse_tc_free(p); } };
 struct NprobeDeleter { void operator()(NprobeModel *p) const { nprobe_model_free(p); } };
 
 }  // namespace hora
@@ -55,6 +58,8 @@ struct hora_index {
   hora::SearchWorkspace ws;
   std::unique_ptr<hora::IvfState, hora::IvfDeleter> ivfs;
   std::unique_ptr<hora::LowpState, hora::LowpDeleter> lowp;
+  // the IVF centres' BF16 image for the certified coarse probe (bf_lowp.cu)
+  std::unique_ptr<hora::CoarseTc, hora::CoarseTcDeleter> coarse_tc;
   std::unique_ptr<hora::NprobeModel, hora::NprobeDeleter> nprobe;
   // last search diagnostics (written by whichever search finished last)
   std::atomic<int> last_retries{0};
@@ -104,6 +109,13 @@ int lowp_probe_kind(const hora_index *h, int R);
 // filter (bf_lowp.cu): whether it answers a k-NN search on this index, its
 // lazily built state, the search itself.
 bool exact_tc_eligible(const hora_index *h, int k);
+// The IVF coarse probe on the tensor cores (bf_lowp.cu): each query's pmax
+// nearest centres (ascending exact keys, the FP32 probe's result), from a
+// BF16 pass over the centres and an exact rescoring of the centres within
+// the certified error bound of the pmax-th; dist is nq x C scratch.
+bool coarse_tc_eligible(const hora_index *h);
+int coarse_tc_probe(hora_index *h, const float *centers, const float *cnorm, int64_t C, int64_t nq, int pmax,
+                    SearchWorkspace &ws, float *dist, uint64_t *probes, cudaStream_t s);
 int exact_tc_prepare(hora_index *h, cudaStream_t s);
 int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
                          cudaStream_t s);

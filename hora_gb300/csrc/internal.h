@@ -98,6 +98,7 @@ struct SearchWorkspace {
   DevBuf pqg;    // the probe's queries in pivot order and its work items
   DevBuf sbuf;   // wide lists: the sample pass's lists, candidates, counts and flags
   DevBuf rwin;   // windowed rerank: each query's k best approximate keys, then its kept counts
+  DevBuf ccand;  // certified coarse probe: the centres rescored per query, then their counts
   // learned nprobe
   DevBuf feats, pred, npq;
   // certified tensor-core exact search: per-query threshold slack, one empty
@@ -116,7 +117,7 @@ struct SearchWorkspace {
                            &out_dist, &rows, &keys2, &tmp, &coarse, &probes, &pair_cnt, &pair_off, &pair_q,
                            &pair_c, &pair_slot, &ivf_cand, &best_r, &tmp_keys, &adc_next, &adc_gmap, &lq,
                            &lqsq, &lqscale, &lqgather, &lerr, &lq16, &pkeys, &poff, &pmem, &pblk, &pcnt, &pdist,
-                           &ptau, &pqg, &sbuf, &rwin, &feats, &pred, &npq, &xslack, &xempty, &xlist, &xq, &xkeys, &d_status};
+                           &ptau, &pqg, &sbuf, &rwin, &ccand, &feats, &pred, &npq, &xslack, &xempty, &xlist, &xq, &xkeys, &d_status};
     size_t b = 0;
     for (const DevBuf *d : all) b += d->bytes;
     return b;

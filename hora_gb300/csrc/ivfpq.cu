@@ -1563,6 +1563,7 @@ int ivf_build(hora_index *h) {
     HORA_CUDA_TRY(cudaStreamSynchronize(s));
   }
   h->ivfs = std::move(vp);
+  h->coarse_tc.reset();  // the centres' image follows the centres
   return HORA_OK;
 }
 
@@ -1597,6 +1598,7 @@ int ivf_set_codebooks(hora_index *h, const float *centers, const float *codebook
   HORA_TRY(encode_all(h, v, s));
   HORA_CUDA_TRY(cudaStreamSynchronize(s));
   h->ivfs = std::move(vp);
+  h->coarse_tc.reset();  // the centres' image follows the centres
   h->built = true;
   return HORA_OK;
 }
@@ -1660,6 +1662,12 @@ int ivf_probe(hora_index *h, int64_t nq, int pmax, SearchWorkspace &ws, cudaStre
   IvfState &v = *h->ivfs;
   const int C = (int)v.n_list;
   HORA_TRY(ws.coarse.reserve(sizeof(float) * nq * C));
+  if (coarse_tc_eligible(h)) {
+    // the same probes from a BF16 pass and a certified exact rescoring
+    HORA_TRY(ws.probes.reserve(sizeof(uint64_t) * nq * pmax));
+    return coarse_tc_probe(h, v.centers.as<float>(), v.cnorm.as<float>(), C, nq, pmax, ws, ws.coarse.as<float>(),
+                           ws.probes.as<uint64_t>(), s);
+  }
   TileParams p;
   p.Q = ws.q.as<float>();
   p.ldq = h->ld;

@@ -105,6 +105,9 @@ static size_t request_bytes(const hora_index *h, uint64_t nq, uint64_t k) {
     pmax = std::min(pmax, C);
     const size_t R = std::max<size_t>(k, (size_t)h->ivf_rerank);
     per_q += C * 4 + pmax * (8 + 12 + 4) + pmax * R * 8 + R * 16 + 40 * 4 + 16;
+    // the certified coarse probe: the rescored centres and their count, the
+    // BF16 query copy, its f32 squared norm and slack
+    if (coarse_tc_eligible(h)) per_q += C * 8 + 4 + Dp + 8;
     fixed += (C + 1) * 32 + C * 4;
   }
   return per_q * nq + fixed;

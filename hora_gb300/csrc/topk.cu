@@ -883,9 +883,64 @@ __global__ void __launch_bounds__(kWmWarps * 32) rows_select_warp_kernel(const f
   for (int i = lane; i < k; i += 32) out[r * k + i] = i < want ? sel[i] : kEmptyKey;
 }
 
+// Small k (<= K): one warp per row; each lane keeps the K smallest keys
+// (ordered distance bits << 32 | column) of its columns (lane, lane + 32,
+// ...: coalesced reads of any row length) in registers, sorted by insertion;
+// then k rounds of a warp minimum over the lanes' heads, the owner popping
+// its head, write the k smallest keys in ascending order.
+template <int K>
+__global__ void __launch_bounds__(256) rows_topk_small_kernel(const float *D, int64_t rows, int64_t cols,
+                                                              int64_t ldd, int k, uint64_t *out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (r >= rows) return;
+  uint64_t best[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) best[i] = kEmptyKey;
+  for (int64_t c = lane; c < cols; c += 32) {
+    uint64_t key = ((uint64_t)f2ord(D[r * ldd + c]) << 32) | (uint32_t)c;
+    if (key < best[K - 1]) {
+#pragma unroll
+      for (int i = 0; i < K; ++i) {
+        const uint64_t lo = key < best[i] ? key : best[i], hi = key < best[i] ? best[i] : key;
+        best[i] = lo;
+        key = hi;
+      }
+    }
+  }
+  for (int j = 0; j < k; ++j) {
+    uint64_t m = best[0];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const uint64_t y = __shfl_xor_sync(0xffffffffu, m, o);
+      m = y < m ? y : m;
+    }
+    if (lane == 0) out[r * k + j] = m;
+    if (m != kEmptyKey && best[0] == m) {  // keys are distinct: one owner
+#pragma unroll
+      for (int i = 0; i < K - 1; ++i) best[i] = best[i + 1];
+      best[K - 1] = kEmptyKey;
+    }
+  }
+}
+
 int launch_rows_topk(const float *D, int64_t rows, int64_t cols, int64_t ldd, int k,
                      uint64_t *out, cudaStream_t s) {
   if (rows <= 0) return HORA_OK;
+  if (k <= 16) {
+    ProfScope ps("rows_topk", s);
+    const unsigned g = (unsigned)ceil_div(rows, (int64_t)8);
+    if (k <= 2)
+      rows_topk_small_kernel<2><<<g, 256, 0, s>>>(D, rows, cols, ldd, k, out);
+    else if (k <= 4)
+      rows_topk_small_kernel<4><<<g, 256, 0, s>>>(D, rows, cols, ldd, k, out);
+    else if (k <= 8)
+      rows_topk_small_kernel<8><<<g, 256, 0, s>>>(D, rows, cols, ldd, k, out);
+    else
+      rows_topk_small_kernel<16><<<g, 256, 0, s>>>(D, rows, cols, ldd, k, out);
+    HORA_LAUNCHED();
+    return HORA_OK;
+  }
   if (k <= kWmMaxK && cols <= 32 * kWmRegs) {
     ProfScope ps("rows_topk", s);
     rows_select_warp_kernel<<<(unsigned)ceil_div(rows, (int64_t)kWmWarps), kWmWarps * 32, 0, s>>>(

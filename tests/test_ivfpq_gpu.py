@@ -191,3 +191,26 @@ def test_full_size_config(hora, oracle, gpu):
     ids, _ = ix.search_batch(q, 10, nprobe=64)
     rr = np.mean([len(set(a) & set(b)) / 10 for a, b in zip(ids.astype(np.int64), ei)])
     assert rr >= 0.95, rr
+
+
+@pytest.mark.parametrize("metric", [3, 2, 4])
+def test_coarse_probe_on_tensor_cores_equals_fp32(hora, gpu, metric):
+    """With at least 2,048 lists the coarse probe is a BF16 pass plus the
+    exact rescoring of the centres within the certified bound of the
+    pmax-th; it returns the FP32 probe's lists: the searches with it (the
+    default) and without it (EXACT_TC 0) agree bit for bit, at several
+    nprobe."""
+    from hora_gb300 import synth
+    X = synth.mixture(120_000, 64, 512, stream=71)
+    q = synth.mixture(400, 64, 512, stream=72)
+    ix = hora.IVFPQIndex(64, hora.IVFPQParams(n_sub=16, sub_bits=8, n_kmeans_center=2048,
+                                              search_n_center=4, train_epoch=3))
+    ix.madd(X, None)
+    ix.build(hora.Metric(metric))
+    for nprobe in (1, 4, 37):
+        ix.set_option(hora.Option.EXACT_TC, 1)
+        ids1, d1 = ix.search_batch(q, 10, nprobe=nprobe)
+        ix.set_option(hora.Option.EXACT_TC, 0)
+        ids0, d0 = ix.search_batch(q, 10, nprobe=nprobe)
+        np.testing.assert_array_equal(ids1, ids0, err_msg=f"nprobe {nprobe}")
+        np.testing.assert_array_equal(d1, d0, err_msg=f"nprobe {nprobe}")
