@@ -125,15 +125,23 @@ typedef enum {
   HORA_OPT_NPROBE_PHASE1 = 11, /* learned nprobe: lists probed before the model
                                   reads its features (0..64, default 4; fixed at
                                   training) */
-  HORA_OPT_BF_PROBE = 12,      /* BF16 Euclidean brute force on >= 65,536 rows:
-                                  start each query's scan from a threshold probed
-                                  in its nearest pivot cluster (default 1; 0 =
-                                  chunked schedule only; same results either way) */
+  HORA_OPT_BF_PROBE = 12,      /* BF16 / FP8 brute force (Euclidean, DotProduct,
+                                  CosineSimilarity) on >= 65,536 rows: start each
+                                  query's scan from a threshold, probed in its
+                                  nearest pivot cluster (R-best lists up to 256)
+                                  or taken from an even sample of the base (wider
+                                  lists, up to 4,096), then one pass over the base
+                                  (default 1; 0 = chunked schedule only; same
+                                  results either way) */
   HORA_OPT_EXACT_TC = 13       /* exact FP32 Euclidean brute force on >= 65,536
                                   rows, k <= 256: the BF16 tensor-core scan as a
                                   filter certified by a rounding-error bound, then
-                                  every kept row rescored exactly (default 1; 0 =
-                                  the CUDA-core scan; same results either way) */
+                                  every kept row rescored exactly; and the coarse
+                                  probe of an IVF-PQ index of >= 2,048 lists: a
+                                  BF16 pass, then the centres within the bound of
+                                  the nprobe-th rescored exactly (default 1; 0 =
+                                  the CUDA-core FP32 passes; same results either
+                                  way) */
 } hora_option;
 
 typedef struct hora_index hora_index;
