@@ -543,10 +543,14 @@ def run_ivf_profile(a, H, base, q):
         ix.set_option(H.Option.EXACT_TC, 0)
     ix.set_option(H.Option.TRAIN_SIZE, min(500_000, base.shape[0]))
     ix.madd(torch.from_numpy(base).cuda(), None)
+    H._lib.profile_report()
+    H._lib.profile(True)
     t0 = time.perf_counter()
     ix.build(H.Metric.Euclidean)
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
+    H._lib.profile(False)
+    build_kern = {k: {"launches": v[0], "ms": v[1]} for k, v in H._lib.profile_report().items()}
     ix.set_option(H.Option.IVF_RERANK, 100)
     ix.search_batch(q, 10)
     first_ms = json.loads(ix.idx_info())["last_search_ms"]
@@ -559,7 +563,7 @@ def run_ivf_profile(a, H, base, q):
     kern = {k: {"launches": v[0] // 3, "ms": v[1] / 3} for k, v in H._lib.profile_report().items()}
     print(json.dumps({"workload": "IVF-PQ profile case", "queries": q.shape[0], "nprobe": a.nprobe,
                       "lists": a.ivf_lists, "coarse": "fp32" if a.coarse_fp32 else "default",
-                      "build_s": build_s, "first_search_ms": first_ms,
+                      "build_s": build_s, "build_kernels": build_kern, "first_search_ms": first_ms,
                       "search_ms": json.loads(ix.idx_info())["last_search_ms"], "kernels_per_search": kern}),
           flush=True)
 

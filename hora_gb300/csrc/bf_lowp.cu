@@ -2358,26 +2358,26 @@ __global__ void coarse_rescore_kernel(const float *Q, int64_t ld, const float *X
   }
 }
 
-static int ensure_coarse_tc(hora_index *h, const float *centers, int64_t C, cudaStream_t s) {
-  if (h->coarse_tc && h->coarse_tc->C == C && h->coarse_tc->metric == h->metric) return HORA_OK;
-  std::unique_ptr<CoarseTc, CoarseTcDeleter> st(new CoarseTc());
-  st->metric = h->metric;
-  st->C = C;
-  st->Dp = round_up((int64_t)h->dim, 64);
-  st->nkb = (int)(st->Dp / 64);
+// The BF16 image of C centres (pitch h->ld) for the index's metric and
+// their bound inputs (see CoarseTc), into st.
+static int build_centre_image(hora_index *h, const float *centers, int64_t C, CoarseTc &st, cudaStream_t s) {
+  st.metric = h->metric;
+  st.C = C;
+  st.Dp = round_up((int64_t)h->dim, 64);
+  st.nkb = (int)(st.Dp / 64);
   const bool fold = h->metric == M_L2, cos = h->metric == M_COS;
-  const int64_t ld = h->ld, Dp = st->Dp, ntiles = ceil_div(C, (int64_t)kLpBN);
-  const int64_t tile_bytes = (int64_t)st->nkb * kLpBN * 128 + (fold ? kNormBytesB : 0);
+  const int64_t ld = h->ld, Dp = st.Dp, ntiles = ceil_div(C, (int64_t)kLpBN);
+  const int64_t tile_bytes = (int64_t)st.nkb * kLpBN * 128 + (fold ? kNormBytesB : 0);
   DevBuf crow, cnb, csq, csqf;  // staging, freed on return
   HORA_TRY(crow.reserve(sizeof(__nv_bfloat16) * C * Dp));
   HORA_TRY(cnb.reserve(sizeof(__nv_bfloat16) * C * 16));
   HORA_TRY(csq.reserve(sizeof(double) * C));
   HORA_TRY(csqf.reserve(sizeof(float) * C));
-  HORA_TRY(st->tiles.reserve(ntiles * tile_bytes));
-  HORA_TRY(st->dxmax.reserve(sizeof(float)));
-  HORA_TRY(st->xsqmax.reserve(sizeof(float)));
-  HORA_CUDA_TRY(cudaMemsetAsync(st->dxmax.ptr, 0, sizeof(float), s));
-  HORA_CUDA_TRY(cudaMemsetAsync(st->xsqmax.ptr, 0, sizeof(float), s));
+  HORA_TRY(st.tiles.reserve(ntiles * tile_bytes));
+  HORA_TRY(st.dxmax.reserve(sizeof(float)));
+  HORA_TRY(st.xsqmax.reserve(sizeof(float)));
+  HORA_CUDA_TRY(cudaMemsetAsync(st.dxmax.ptr, 0, sizeof(float), s));
+  HORA_CUDA_TRY(cudaMemsetAsync(st.xsqmax.ptr, 0, sizeof(float), s));
   HORA_TRY(launch_row_norms(centers, C, ld, h->dim, nullptr, csq.as<double>(), s));
   to_bf16_kernel<<<(unsigned)ceil_div(C * Dp, 256), 256, 0, s>>>(centers, C, ld, h->dim, Dp,
                                                                  cos ? csq.as<double>() : nullptr,
@@ -2387,21 +2387,67 @@ static int ensure_coarse_tc(hora_index *h, const float *centers, int64_t C, cuda
     norm_block_kernel<<<(unsigned)ceil_div(C, 256), 256, 0, s>>>(csq.as<double>(), C, cnb.as<__nv_bfloat16>());
     HORA_LAUNCHED();
   }
-  tile_image_kernel<<<(unsigned)ceil_div(ntiles * kLpBN * (st->nkb * 8 + 2), 256), 256, 0, s>>>(
-      crow.as<uint8_t>(), C, Dp * 2, st->nkb, fold ? cnb.as<uint8_t>() : nullptr, tile_bytes, ntiles,
-      st->tiles.as<uint8_t>());
+  tile_image_kernel<<<(unsigned)ceil_div(ntiles * kLpBN * (st.nkb * 8 + 2), 256), 256, 0, s>>>(
+      crow.as<uint8_t>(), C, Dp * 2, st.nkb, fold ? cnb.as<uint8_t>() : nullptr, tile_bytes, ntiles,
+      st.tiles.as<uint8_t>());
   HORA_LAUNCHED();
   if (!cos) {
     bf16_residual_max_kernel<<<(unsigned)ceil_div(C, 8), 256, 0, s>>>(centers, C, ld, h->dim,
-                                                                       st->dxmax.as<unsigned>());
+                                                                       st.dxmax.as<unsigned>());
     HORA_LAUNCHED();
   }
   f64_to_f32_kernel<<<(unsigned)ceil_div(C, 256), 256, 0, s>>>(csq.as<double>(), C, csqf.as<float>());
   HORA_LAUNCHED();
-  max_nonneg_kernel<<<152, 256, 0, s>>>(csqf.as<float>(), C, st->xsqmax.as<unsigned>());
+  max_nonneg_kernel<<<152, 256, 0, s>>>(csqf.as<float>(), C, st.xsqmax.as<unsigned>());
   HORA_LAUNCHED();
   HORA_CUDA_TRY(cudaStreamSynchronize(s));  // the staging buffers are freed on return
+  return HORA_OK;
+}
+
+static int ensure_coarse_tc(hora_index *h, const float *centers, int64_t C, cudaStream_t s) {
+  if (h->coarse_tc && h->coarse_tc->C == C && h->coarse_tc->metric == h->metric) return HORA_OK;
+  std::unique_ptr<CoarseTc, CoarseTcDeleter> st(new CoarseTc());
+  HORA_TRY(build_centre_image(h, centers, C, *st, s));
   h->coarse_tc = std::move(st);
+  return HORA_OK;
+}
+
+// The BF16 distance pass of nq staged query rows (BF16 copy lq, pitch Dp;
+// f32 squared norms qsq and norms qnorm) over a centre image: dist[q * C +
+// c], the scan kernel's key for the metric.
+static int centre_dist_pass(hora_index *h, const CoarseTc &T, const void *lq, int64_t nq, const float *qsq,
+                            const float *qnorm, int *err, float *dist, cudaStream_t s) {
+  CUtensorMap ta;
+  HORA_TRY(make_tmap(&ta, lq, HORA_PREC_BF16, T.Dp, nq, kLpBM));
+  LpParams p{};
+  p.nq = nq;
+  p.nkb = T.nkb;
+  p.stages = lp_stages(T.nkb, h->metric == M_L2);
+  p.tiles = T.tiles.as<uint8_t>();
+  p.qsq = qsq;
+  p.qnorm = qnorm;
+  p.err = err;
+  p.r_begin = 0;
+  p.r_end = T.C;
+  p.tpc = lp_tiles_per_cta(nq, T.C);
+  p.out_dist = dist;
+  p.ldo = T.C;
+  if (h->metric == M_L2) return launch_lp3<HORA_PREC_BF16, M_L2, TILE_DIST>(ta, p, s);
+  if (h->metric == M_IP) return launch_lp3<HORA_PREC_BF16, M_IP, TILE_DIST>(ta, p, s);
+  return launch_lp3<HORA_PREC_BF16, M_COS, TILE_DIST>(ta, p, s);
+}
+
+// 2 eps per query row of Q (pitch ld; f64 squared norms qsq64) against the
+// centres of T (see rerank_slack_kernel / exact_tc_slack_kernel).
+static int centre_slack(hora_index *h, const CoarseTc &T, const float *Q, int64_t nq, const double *qsq64,
+                        float *slack, cudaStream_t s) {
+  if (h->metric == M_L2)
+    exact_tc_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(Q, nq, h->ld, h->dim, T.Dp, qsq64, T.dxmax.as<float>(),
+                                                          T.xsqmax.as<float>(), slack);
+  else
+    rerank_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(Q, nq, h->ld, h->dim, T.Dp, h->metric, qsq64,
+                                                        T.dxmax.as<float>(), T.xsqmax.as<float>(), slack);
+  HORA_LAUNCHED();
   return HORA_OK;
 }
 
@@ -2411,7 +2457,6 @@ int coarse_tc_probe(hora_index *h, const float *centers, const float *cnorm, int
   HORA_TRY(ensure_coarse_tc(h, centers, C, s));
   const CoarseTc &T = *h->coarse_tc;
   const int64_t Dp = T.Dp;
-  const bool fold = h->metric == M_L2;
   HORA_TRY(ws.lq.reserve(nq * Dp * 2));
   HORA_TRY(ws.lqsq.reserve(sizeof(float) * nq));
   HORA_TRY(ws.lerr.reserve(16));
@@ -2431,36 +2476,9 @@ int coarse_tc_probe(hora_index *h, const float *centers, const float *cnorm, int
     f64_to_f32_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(qsq64, nq, ws.lqsq.as<float>());
     HORA_LAUNCHED();
     HORA_CUDA_TRY(cudaMemsetAsync(ws.lerr.ptr, 0, 16, s));
-    CUtensorMap ta;
-    HORA_TRY(make_tmap(&ta, ws.lq.ptr, HORA_PREC_BF16, Dp, nq, kLpBM));
-    LpParams p{};
-    p.nq = nq;
-    p.nkb = T.nkb;
-    p.stages = lp_stages(T.nkb, fold);
-    p.tiles = T.tiles.as<uint8_t>();
-    p.qsq = ws.lqsq.as<float>();
-    p.qnorm = ws.qnorm.as<float>();
-    p.err = ws.lerr.as<int>();
-    p.r_begin = 0;
-    p.r_end = C;
-    p.tpc = lp_tiles_per_cta(nq, C);
-    p.out_dist = dist;
-    p.ldo = C;
-    if (h->metric == M_L2)
-      HORA_TRY((launch_lp3<HORA_PREC_BF16, M_L2, TILE_DIST>(ta, p, s)));
-    else if (h->metric == M_IP)
-      HORA_TRY((launch_lp3<HORA_PREC_BF16, M_IP, TILE_DIST>(ta, p, s)));
-    else
-      HORA_TRY((launch_lp3<HORA_PREC_BF16, M_COS, TILE_DIST>(ta, p, s)));
-    if (fold)
-      exact_tc_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, qsq64,
-                                                            T.dxmax.as<float>(), T.xsqmax.as<float>(),
-                                                            ws.xslack.as<float>());
-    else
-      rerank_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, h->metric,
-                                                          qsq64, T.dxmax.as<float>(), T.xsqmax.as<float>(),
-                                                          ws.xslack.as<float>());
-    HORA_LAUNCHED();
+    HORA_TRY(centre_dist_pass(h, T, ws.lq.ptr, nq, ws.lqsq.as<float>(), ws.qnorm.as<float>(), ws.lerr.as<int>(),
+                              dist, s));
+    HORA_TRY(centre_slack(h, T, ws.q.as<float>(), nq, qsq64, ws.xslack.as<float>(), s));
   }
   HORA_TRY(launch_rows_topk(dist, nq, C, C, pmax, probes, s));
   coarse_window_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(dist, C, probes, pmax, ws.xslack.as<float>(), nq,
@@ -2486,6 +2504,121 @@ int coarse_tc_probe(hora_index *h, const float *centers, const float *cnorm, int
   HORA_CUDA_TRY(cudaMemcpyAsync(&err, ws.lerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
   HORA_CUDA_TRY(cudaStreamSynchronize(s));
   if (err) return fail(HORA_ETIMEDOUT, "tensor-core coarse pass: a pipeline wait timed out");
+  return HORA_OK;
+}
+
+// ---- certified nearest-centre assignment (coarse k-means) -------------------------------
+// Kmeans::search_data's argmin (kmeans.rs:127-148: the exact FP32 distance,
+// ties to the lower centre) of many items, on the tensor cores: the BF16
+// pass of the scan kernel over the centres' image gives each item its two
+// smallest approximate keys s1 <= s2; with eps the certified bound on
+// |approximate key - exact distance| (the rerank window's, the items playing
+// the queries), s2 - s1 > 2 eps puts the exact distance of s1's centre below
+// every other centre's, so it is the exact argmin, strictly.  The other
+// items (near ties) take the exact FP32 pass.
+struct TcAssign {
+  int64_t T = 0;
+  const float *X = nullptr;  // the items, pitch h->ld: base rows 0 .. T
+  DevBuf lq, lqsq;           // their BF16 copy and f32 squared norms
+  DevBuf slack, dist, top2, list, cnt;
+  CoarseTc img;
+};
+
+void tc_assign_free(TcAssign *p) { delete p; }
+
+static bool tc_assign_eligible(const hora_index *h, int64_t T) {
+  return h->exact_tc && T >= kProbeMinRows && (h->metric == M_L2 || h->metric == M_IP || h->metric == M_COS) &&
+         round_up((int64_t)h->dim, 64) / 64 <= 2;
+}
+
+// Item i: its approximate argmin key when the runner-up lies beyond the
+// bound, else listed for the exact pass.
+__global__ void assign_certify_kernel(const uint64_t *top2, const float *slack, int64_t n, uint64_t *keys,
+                                      int *list, uint32_t *cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t k1 = top2[2 * i], k2 = top2[2 * i + 1];
+  bool sure = k1 != kEmptyKey;
+  if (sure && k2 != kEmptyKey) {
+    const float t = key_dist(k1) + slack[i];
+    sure = key_dist(k2) > t + 0x1p-20f * fabsf(t);
+  }
+  if (sure)
+    keys[i] = k1;
+  else
+    list[atomicAdd(cnt, 1u)] = (int)i;
+}
+
+int tc_assign_prepare(hora_index *h, const float *X, int64_t T, std::unique_ptr<TcAssign, TcAssignDeleter> *out,
+                      cudaStream_t s) {
+  out->reset();
+  if (!tc_assign_eligible(h, T)) return HORA_OK;
+  HORA_TRY(ensure_norms(h, s));
+  std::unique_ptr<TcAssign, TcAssignDeleter> a(new TcAssign());
+  a->T = T;
+  a->X = X;
+  const int64_t Dp = round_up((int64_t)h->dim, 64);
+  HORA_TRY(a->lq.reserve(T * Dp * 2));
+  HORA_TRY(a->lqsq.reserve(sizeof(float) * T));
+  to_bf16_kernel<<<(unsigned)ceil_div(T * Dp, 256), 256, 0, s>>>(X, T, h->ld, h->dim, Dp,
+                                                                 h->metric == M_COS ? h->xsq64.as<double>() : nullptr,
+                                                                 a->lq.as<__nv_bfloat16>());
+  HORA_LAUNCHED();
+  f64_to_f32_kernel<<<(unsigned)ceil_div(T, 256), 256, 0, s>>>(h->xsq64.as<double>(), T, a->lqsq.as<float>());
+  HORA_LAUNCHED();
+  *out = std::move(a);
+  return HORA_OK;
+}
+
+int tc_assign(hora_index *h, TcAssign &a, const float *centers, const float *cnorm, int64_t C, uint64_t *keys,
+              cudaStream_t s) {
+  const int64_t T = a.T;
+  HORA_TRY(build_centre_image(h, centers, C, a.img, s));
+  const int64_t Dp = a.img.Dp;
+  // distance rows of up to 256 MB per chunk
+  const int64_t chunk = std::max<int64_t>(1024, std::min<int64_t>(65536, ((int64_t)1 << 26) / C / 128 * 128));
+  HORA_TRY(a.slack.reserve(sizeof(float) * T));
+  HORA_TRY(a.top2.reserve(sizeof(uint64_t) * 2 * T));
+  HORA_TRY(a.list.reserve(sizeof(int) * T));
+  HORA_TRY(a.cnt.reserve(16));
+  HORA_TRY(a.dist.reserve(sizeof(float) * chunk * C));
+  int *err = reinterpret_cast<int *>(a.cnt.as<uint32_t>() + 1);
+  HORA_CUDA_TRY(cudaMemsetAsync(a.cnt.ptr, 0, 16, s));
+  {
+    ProfScope ps("assign_tc", s);
+    HORA_TRY(centre_slack(h, a.img, a.X, T, h->xsq64.as<double>(), a.slack.as<float>(), s));
+    for (int64_t lo = 0; lo < T; lo += chunk) {
+      const int64_t nc = std::min<int64_t>(chunk, T - lo);
+      HORA_TRY(centre_dist_pass(h, a.img, a.lq.as<uint8_t>() + lo * Dp * 2, nc, a.lqsq.as<float>() + lo,
+                                h->metric == M_COS ? h->xnorm.as<float>() + lo : nullptr, err, a.dist.as<float>(),
+                                s));
+      HORA_TRY(launch_rows_topk(a.dist.as<float>(), nc, C, C, 2, a.top2.as<uint64_t>() + 2 * lo, s));
+    }
+    assign_certify_kernel<<<(unsigned)ceil_div(T, 256), 256, 0, s>>>(a.top2.as<uint64_t>(), a.slack.as<float>(), T,
+                                                                      keys, a.list.as<int>(), a.cnt.as<uint32_t>());
+    HORA_LAUNCHED();
+  }
+  uint32_t hc[2] = {0, 0};
+  HORA_CUDA_TRY(cudaMemcpyAsync(hc, a.cnt.ptr, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  HORA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hc[1]) return fail(HORA_ETIMEDOUT, "tensor-core assignment: a pipeline wait timed out");
+  if (hc[0] > 0) {
+    // the near ties: the exact FP32 pass
+    TileParams p;
+    p.Q = a.X;
+    p.ldq = h->ld;
+    p.nq = hc[0];
+    p.qmap = a.list.as<int>();
+    p.X = centers;
+    p.ldx = h->ld;
+    p.r_begin = 0;
+    p.r_end = C;
+    p.ld = h->ld;
+    p.qnorm = h->xnorm.as<float>();
+    p.xnorm = cnorm;
+    p.out_key = keys;
+    HORA_TRY(launch_dist_tile(h->metric, TILE_ARGMIN, p, s));
+  }
   return HORA_OK;
 }
 
