@@ -2507,119 +2507,4 @@ int coarse_tc_probe(hora_index *h, const float *centers, const float *cnorm, int
   return HORA_OK;
 }
 
-// ---- certified nearest-centre assignment (coarse k-means) -------------------------------
-// Kmeans::search_data's argmin (kmeans.rs:127-148: the exact FP32 distance,
-// ties to the lower centre) of many items, on the tensor cores: the BF16
-// pass of the scan kernel over the centres' image gives each item its two
-// smallest approximate keys s1 <= s2; with eps the certified bound on
-// |approximate key - exact distance| (the rerank window's, the items playing
-// the queries), s2 - s1 > 2 eps puts the exact distance of s1's centre below
-// every other centre's, so it is the exact argmin, strictly.  The other
-// items (near ties) take the exact FP32 pass.
-struct TcAssign {
-  int64_t T = 0;
-  const float *X = nullptr;  // the items, pitch h->ld: base rows 0 .. T
-  DevBuf lq, lqsq;           // their BF16 copy and f32 squared norms
-  DevBuf slack, dist, top2, list, cnt;
-  CoarseTc img;
-};
-
-void tc_assign_free(TcAssign *p) { delete p; }
-
-static bool tc_assign_eligible(const hora_index *h, int64_t T) {
-  return h->exact_tc && T >= kProbeMinRows && (h->metric == M_L2 || h->metric == M_IP || h->metric == M_COS) &&
-         round_up((int64_t)h->dim, 64) / 64 <= 2;
-}
-
-// Item i: its approximate argmin key when the runner-up lies beyond the
-// bound, else listed for the exact pass.
-__global__ void assign_certify_kernel(const uint64_t *top2, const float *slack, int64_t n, uint64_t *keys,
-                                      int *list, uint32_t *cnt) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint64_t k1 = top2[2 * i], k2 = top2[2 * i + 1];
-  bool sure = k1 != kEmptyKey;
-  if (sure && k2 != kEmptyKey) {
-    const float t = key_dist(k1) + slack[i];
-    sure = key_dist(k2) > t + 0x1p-20f * fabsf(t);
-  }
-  if (sure)
-    keys[i] = k1;
-  else
-    list[atomicAdd(cnt, 1u)] = (int)i;
-}
-
-int tc_assign_prepare(hora_index *h, const float *X, int64_t T, std::unique_ptr<TcAssign, TcAssignDeleter> *out,
-                      cudaStream_t s) {
-  out->reset();
-  if (!tc_assign_eligible(h, T)) return HORA_OK;
-  HORA_TRY(ensure_norms(h, s));
-  std::unique_ptr<TcAssign, TcAssignDeleter> a(new TcAssign());
-  a->T = T;
-  a->X = X;
-  const int64_t Dp = round_up((int64_t)h->dim, 64);
-  HORA_TRY(a->lq.reserve(T * Dp * 2));
-  HORA_TRY(a->lqsq.reserve(sizeof(float) * T));
-  to_bf16_kernel<<<(unsigned)ceil_div(T * Dp, 256), 256, 0, s>>>(X, T, h->ld, h->dim, Dp,
-                                                                 h->metric == M_COS ? h->xsq64.as<double>() : nullptr,
-                                                                 a->lq.as<__nv_bfloat16>());
-  HORA_LAUNCHED();
-  f64_to_f32_kernel<<<(unsigned)ceil_div(T, 256), 256, 0, s>>>(h->xsq64.as<double>(), T, a->lqsq.as<float>());
-  HORA_LAUNCHED();
-  *out = std::move(a);
-  return HORA_OK;
-}
-
-int tc_assign(hora_index *h, TcAssign &a, const float *centers, const float *cnorm, int64_t C, uint64_t *keys,
-              cudaStream_t s) {
-  const int64_t T = a.T;
-  HORA_TRY(build_centre_image(h, centers, C, a.img, s));
-  const int64_t Dp = a.img.Dp;
-  // distance rows of up to 256 MB per chunk
-  const int64_t chunk = std::max<int64_t>(1024, std::min<int64_t>(65536, ((int64_t)1 << 26) / C / 128 * 128));
-  HORA_TRY(a.slack.reserve(sizeof(float) * T));
-  HORA_TRY(a.top2.reserve(sizeof(uint64_t) * 2 * T));
-  HORA_TRY(a.list.reserve(sizeof(int) * T));
-  HORA_TRY(a.cnt.reserve(16));
-  HORA_TRY(a.dist.reserve(sizeof(float) * chunk * C));
-  int *err = reinterpret_cast<int *>(a.cnt.as<uint32_t>() + 1);
-  HORA_CUDA_TRY(cudaMemsetAsync(a.cnt.ptr, 0, 16, s));
-  {
-    ProfScope ps("assign_tc", s);
-    HORA_TRY(centre_slack(h, a.img, a.X, T, h->xsq64.as<double>(), a.slack.as<float>(), s));
-    for (int64_t lo = 0; lo < T; lo += chunk) {
-      const int64_t nc = std::min<int64_t>(chunk, T - lo);
-      HORA_TRY(centre_dist_pass(h, a.img, a.lq.as<uint8_t>() + lo * Dp * 2, nc, a.lqsq.as<float>() + lo,
-                                h->metric == M_COS ? h->xnorm.as<float>() + lo : nullptr, err, a.dist.as<float>(),
-                                s));
-      HORA_TRY(launch_rows_topk(a.dist.as<float>(), nc, C, C, 2, a.top2.as<uint64_t>() + 2 * lo, s));
-    }
-    assign_certify_kernel<<<(unsigned)ceil_div(T, 256), 256, 0, s>>>(a.top2.as<uint64_t>(), a.slack.as<float>(), T,
-                                                                      keys, a.list.as<int>(), a.cnt.as<uint32_t>());
-    HORA_LAUNCHED();
-  }
-  uint32_t hc[2] = {0, 0};
-  HORA_CUDA_TRY(cudaMemcpyAsync(hc, a.cnt.ptr, sizeof(hc), cudaMemcpyDeviceToHost, s));
-  HORA_CUDA_TRY(cudaStreamSynchronize(s));
-  if (hc[1]) return fail(HORA_ETIMEDOUT, "tensor-core assignment: a pipeline wait timed out");
-  if (hc[0] > 0) {
-    // the near ties: the exact FP32 pass
-    TileParams p;
-    p.Q = a.X;
-    p.ldq = h->ld;
-    p.nq = hc[0];
-    p.qmap = a.list.as<int>();
-    p.X = centers;
-    p.ldx = h->ld;
-    p.r_begin = 0;
-    p.r_end = C;
-    p.ld = h->ld;
-    p.qnorm = h->xnorm.as<float>();
-    p.xnorm = cnorm;
-    p.out_key = keys;
-    HORA_TRY(launch_dist_tile(h->metric, TILE_ARGMIN, p, s));
-  }
-  return HORA_OK;
-}
-
 }  // namespace hora

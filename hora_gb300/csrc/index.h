@@ -12,18 +12,15 @@ namespace hora {
 struct IvfState;   // ivfpq.cu
 struct LowpState;  // bf_lowp.cu
 struct CoarseTc;   // bf_lowp.cu
-struct TcAssign;   // bf_lowp.cu
 struct NprobeModel;  // nprobe_mlp.cu
 
 void ivf_state_free(IvfState *);
 void lowp_state_free(LowpState *);
 void coarse_tc_free(CoarseTc *);
-void tc_assign_free(TcAssign *);
 void nprobe_model_free(NprobeModel *);
 struct IvfDeleter { void operator()(IvfState *p) const { ivf_state_free(p); } };
 struct LowpDeleter { void operator()(LowpState *p) const { lowp_state_free(p); } };
 struct CoarseTcDeleter { void operator()(CoarseTc *p) const { coarse_tc_free(p); } };
-struct TcAssignDeleter { void operator()(TcAssign *p) const { tc_assign_free(p); } };
 struct NprobeDeleter { void operator()(NprobeModel *p) const { nprobe_model_free(p); } };
 
 }  // namespace hora
@@ -119,15 +116,6 @@ bool exact_tc_eligible(const hora_index *h, int k);
 bool coarse_tc_eligible(const hora_index *h);
 int coarse_tc_probe(hora_index *h, const float *centers, const float *cnorm, int64_t C, int64_t nq, int pmax,
                     SearchWorkspace &ws, float *dist, uint64_t *probes, cudaStream_t s);
-// Nearest-centre assignment of T items on the tensor cores (bf_lowp.cu):
-// prepare keeps the items' BF16 copy (out stays null when the FP32 pass
-// serves: fewer than 65,536 items, Manhattan, wide rows, HORA_OPT_EXACT_TC
-// 0); assign writes keys[i] with item i's nearest centre (the exact FP32
-// argmin, ties to the lower centre) in the low word.
-int tc_assign_prepare(hora_index *h, const float *X, int64_t T, std::unique_ptr<TcAssign, TcAssignDeleter> *out,
-                      cudaStream_t s);
-int tc_assign(hora_index *h, TcAssign &a, const float *centers, const float *cnorm, int64_t C, uint64_t *keys,
-              cudaStream_t s);
 int exact_tc_prepare(hora_index *h, cudaStream_t s);
 int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
                          cudaStream_t s);

@@ -1394,25 +1394,19 @@ static int assign_lists(hora_index *h, IvfState &v, DevBuf &keys, DevBuf &blk, D
     HORA_TRY(launch_row_norms(v.centers.as<float>(), v.n_list, h->ld, h->dim, v.cnorm.as<float>(), nullptr, s));
     HORA_TRY(ensure_norms(h, s));
   }
-  std::unique_ptr<TcAssign, TcAssignDeleter> tca;
-  HORA_TRY(tc_assign_prepare(h, h->base.as<float>(), n, &tca, s));
-  if (tca) {
-    HORA_TRY(tc_assign(h, *tca, v.centers.as<float>(), v.cnorm.as<float>(), v.n_list, keys.as<uint64_t>(), s));
-  } else {
-    TileParams p;
-    p.Q = h->base.as<float>();
-    p.ldq = h->ld;
-    p.nq = n;
-    p.X = v.centers.as<float>();
-    p.ldx = h->ld;
-    p.r_begin = 0;
-    p.r_end = v.n_list;
-    p.ld = h->ld;
-    p.qnorm = h->xnorm.as<float>();
-    p.xnorm = v.cnorm.as<float>();
-    p.out_key = keys.as<uint64_t>();
-    HORA_TRY(launch_dist_tile(h->metric, TILE_ARGMIN, p, s));
-  }
+  TileParams p;
+  p.Q = h->base.as<float>();
+  p.ldq = h->ld;
+  p.nq = n;
+  p.X = v.centers.as<float>();
+  p.ldx = h->ld;
+  p.r_begin = 0;
+  p.r_end = v.n_list;
+  p.ld = h->ld;
+  p.qnorm = h->xnorm.as<float>();
+  p.xnorm = v.cnorm.as<float>();
+  p.out_key = keys.as<uint64_t>();
+  HORA_TRY(launch_dist_tile(h->metric, TILE_ARGMIN, p, s));
   HORA_TRY(v.offsets.reserve(sizeof(int64_t) * (v.n_list + 1)));
   HORA_TRY(v.items.reserve(sizeof(uint32_t) * std::max<int64_t>(n, 1)));
   HORA_TRY(sort_labels(keys.as<uint64_t>(), nullptr, n, (int)v.n_list, blk, cnt,
@@ -1471,29 +1465,22 @@ int ivf_build(hora_index *h) {
     HORA_TRY(ensure_norms(h, s));
     HORA_TRY(v.cnorm.reserve(sizeof(float) * C));
   }
-  // the items' nearest centres: certified on the tensor cores, or the FP32 pass
-  std::unique_ptr<TcAssign, TcAssignDeleter> tca;
-  if (!flat) HORA_TRY(tc_assign_prepare(h, X, T, &tca, s));
   for (int ep = 0; ep < (flat ? 0 : epochs); ++ep) {
     if (h->metric == M_COS)
       HORA_TRY(launch_row_norms(v.centers.as<float>(), C, h->ld, h->dim, v.cnorm.as<float>(), nullptr, s));
-    if (tca) {
-      HORA_TRY(tc_assign(h, *tca, v.centers.as<float>(), v.cnorm.as<float>(), C, keys.as<uint64_t>(), s));
-    } else {
-      TileParams p;
-      p.Q = X;
-      p.ldq = h->ld;
-      p.nq = T;
-      p.X = v.centers.as<float>();
-      p.ldx = h->ld;
-      p.r_begin = 0;
-      p.r_end = C;
-      p.ld = h->ld;
-      p.qnorm = h->xnorm.as<float>();
-      p.xnorm = v.cnorm.as<float>();
-      p.out_key = keys.as<uint64_t>();
-      HORA_TRY(launch_dist_tile(h->metric, TILE_ARGMIN, p, s));
-    }
+    TileParams p;
+    p.Q = X;
+    p.ldq = h->ld;
+    p.nq = T;
+    p.X = v.centers.as<float>();
+    p.ldx = h->ld;
+    p.r_begin = 0;
+    p.r_end = C;
+    p.ld = h->ld;
+    p.qnorm = h->xnorm.as<float>();
+    p.xnorm = v.cnorm.as<float>();
+    p.out_key = keys.as<uint64_t>();
+    HORA_TRY(launch_dist_tile(h->metric, TILE_ARGMIN, p, s));
     HORA_TRY(sort_labels(keys.as<uint64_t>(), nullptr, T, C, blk, cnt, moff.as<int64_t>(),
                          members.as<uint32_t>(), s));
     {

@@ -214,26 +214,3 @@ def test_coarse_probe_on_tensor_cores_equals_fp32(hora, gpu, metric):
         ids0, d0 = ix.search_batch(q, 10, nprobe=nprobe)
         np.testing.assert_array_equal(ids1, ids0, err_msg=f"nprobe {nprobe}")
         np.testing.assert_array_equal(d1, d0, err_msg=f"nprobe {nprobe}")
-
-
-@pytest.mark.parametrize("metric", [3, 2, 4])
-def test_kmeans_assignment_on_tensor_cores_equals_fp32(hora, gpu, metric):
-    """On 65,536 or more training items the coarse k-means assigns items to
-    centres with a BF16 pass, certifying each item whose runner-up lies
-    beyond the rounding bound and rescoring the others exactly: the same
-    assignment as the FP32 pass, so the two builds (EXACT_TC 1, the
-    default, and 0) give identical indexes and identical searches."""
-    from hora_gb300 import synth
-    X = synth.mixture(90_000, 32, 128, stream=73)
-    q = synth.mixture(300, 32, 128, stream=74)
-    out = []
-    for tc in (1, 0):
-        ix = hora.IVFPQIndex(32, hora.IVFPQParams(n_sub=8, sub_bits=8, n_kmeans_center=128,
-                                                  search_n_center=4, train_epoch=4))
-        ix.set_option(hora.Option.EXACT_TC, tc)
-        ix.madd(X, None)
-        ix.build(hora.Metric(metric))
-        out.append([ix.search_batch(q, 10, nprobe=p) for p in (1, 7, 128)])
-    for (i1, d1), (i0, d0) in zip(out[0], out[1]):
-        np.testing.assert_array_equal(i1, i0)
-        np.testing.assert_array_equal(d1, d0)
