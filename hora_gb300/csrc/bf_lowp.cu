@@ -29,8 +29,11 @@
 #include <cuda_fp8.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "dist_tile.cuh"
 #include "index.h"
@@ -133,6 +136,9 @@ struct LpParams {
   // FP8 filter: per 32 image rows {min |x|^2, min scale, max scale, 0}, or
   // null (see group_meta_kernel)
   const float4 *gmeta;
+  // BF16 filter passes: CTA pairs that share each base tile's L2 read
+  // (the PAIR form of lowp_tile_kernel), where clusters of two fit
+  int pair;
 };
 
 // BF16 Euclidean folds the row norm into the MMA: one extra K = 16 step
@@ -335,7 +341,13 @@ __device__ __forceinline__ void stage_hits(const uint32_t (&v)[32], uint32_t hit
   }
 }
 
-template <int PREC, int MT, int MODE>
+// PAIR: launched in clusters of two CTAs on consecutive query blocks and
+// the same base rows; each CTA loads one of the two halves of every base
+// tile (K block 0; the rest) and multicasts it into both CTAs' rings, so the
+// pair reads each tile from L2 once.  A ring slot is refilled once both
+// CTAs' MMAs are done with it: every MMA commit that frees a slot arrives
+// on the slot's barrier in both CTAs (count 2).
+template <int PREC, int MT, int MODE, bool PAIR = false>
 __global__ void __launch_bounds__(kLpThreads, 1)
     lowp_tile_kernel(const __grid_constant__ CUtensorMap tmap_a, LpParams p) {
   constexpr bool FOLD = PREC == HORA_PREC_BF16 && MT == M_L2;
@@ -381,9 +393,9 @@ __global__ void __launch_bounds__(kLpThreads, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       tc::mbar_init(full + s, 1);
-      tc::mbar_init(empty + s, 1);
+      tc::mbar_init(empty + s, PAIR ? 2 : 1);
       tc::mbar_init(full2 + s, 1);
-      tc::mbar_init(empty2 + s, 1);
+      tc::mbar_init(empty2 + s, PAIR ? 2 : 1);
     }
     tc::mbar_init(a_full, 1);
     for (int b = 0; b < kLpNB; ++b) {
@@ -407,6 +419,8 @@ __global__ void __launch_bounds__(kLpThreads, 1)
   if (warp == 1) tc::tmem_alloc(tmem_slot, kLpNB * kLpBN);
   tc::fence_before_sync();
   __syncthreads();
+  // PAIR: the peer's barriers are initialised before anything arrives on them
+  if (PAIR) tc::cluster_sync();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
@@ -421,17 +435,27 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       // stage's layout; the first half (K block 0) and the rest separately
       const uint8_t *img = p.tiles + (row0 / kLpBN) * (int64_t)stage_bytes;
       const uint32_t rest = stage_bytes - b_kb_bytes;
+      // PAIR: rank 0 copies K block 0 into both CTAs, rank 1 the rest (all
+      // of it with a single K block and no norm block); each CTA expects
+      // both halves on its own barriers
+      const uint32_t rank = PAIR ? tc::cluster_ctarank() : 0u;
       for (int t = 0; t < T; ++t) {
         const int s = t % S, j = t / S;
         uint8_t *st = sB + (size_t)s * stage_bytes;
         const uint8_t *src = img + (int64_t)t * stage_bytes;
         if (j > 0 && !tc::mbar_wait(empty + s, (j - 1) & 1, abort)) break;
         tc::mbar_arrive_expect_tx(full + s, b_kb_bytes);
-        tc::bulk_load(st, src, b_kb_bytes, full + s);
+        if (!PAIR)
+          tc::bulk_load(st, src, b_kb_bytes, full + s);
+        else if (rank == (rest ? 0u : 1u))
+          tc::bulk_load_multicast(st, src, b_kb_bytes, full + s, 0x3);
         if (rest) {
           if (j > 0 && !tc::mbar_wait(empty2 + s, (j - 1) & 1, abort)) break;
           tc::mbar_arrive_expect_tx(full2 + s, rest);
-          tc::bulk_load(st + b_kb_bytes, src + b_kb_bytes, rest, full2 + s);
+          if (!PAIR)
+            tc::bulk_load(st + b_kb_bytes, src + b_kb_bytes, rest, full2 + s);
+          else if (rank == 1u)
+            tc::bulk_load_multicast(st + b_kb_bytes, src + b_kb_bytes, rest, full2 + s, 0x3);
         }
       }
     }
@@ -452,7 +476,10 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         for (int kb = 0; kb < nkb; ++kb) {
           if (kb == 1) {
             // K block 0 read: its half of the stage may be refilled
-            tc::mma_commit(empty + s);
+            if (PAIR)
+              tc::mma_commit_multicast(empty + s, 0x3);
+            else
+              tc::mma_commit(empty + s);
             if (!tc::mbar_wait(full2 + s, j & 1, abort)) {
               ok2 = false;
               break;
@@ -475,7 +502,10 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         if (!ok2) break;
         if (FOLD) {
           if (nkb == 1) {
-            tc::mma_commit(empty + s);
+            if (PAIR)
+              tc::mma_commit_multicast(empty + s, 0x3);
+            else
+              tc::mma_commit(empty + s);
             if (!tc::mbar_wait(full2 + s, j & 1, abort)) break;
             tc::fence_after_sync();
           }
@@ -483,7 +513,10 @@ __global__ void __launch_bounds__(kLpThreads, 1)
           const uint64_t bd = tc::sdesc_kmajor_none(tc::smem_u32(st + nkb * b_kb_bytes), kNormHalfB, 128);
           tc::mma_bf16(d, ad, bd, idesc, 1u);
         }
-        tc::mma_commit(rest ? empty2 + s : empty + s);
+        if (PAIR)
+          tc::mma_commit_multicast(rest ? empty2 + s : empty + s, 0x3);
+        else
+          tc::mma_commit(rest ? empty2 + s : empty + s);
         tc::mma_commit(acc_full + b);
       }
       // all MMAs of this thread complete before TMEM is released
@@ -695,6 +728,9 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     tc::tmem_dealloc(tmem, kLpNB * kLpBN);
   }
   if (threadIdx.x == 0 && *abort) atomicExch(p.err, 1);
+  // PAIR: neither CTA leaves while the other may still copy into its ring
+  // or arrive on its barriers
+  if (PAIR) tc::cluster_sync();
 }
 
 // ---- conversions -------------------------------------------------------------------
@@ -1196,6 +1232,40 @@ static int lp_tiles_per_cta(int64_t nq, int64_t rows) {
   return kLpMinTilesPerCta;
 }
 
+// Co-resident clusters of two CTAs of `kernel` (smem bytes each) on the
+// current device, queried once per (kernel, device); 0 when none fit.
+std::atomic<int> g_pair_clusters{-1};  // the last answer, for hora_idx_info
+static int pair_clusters(const void *kernel, int smem, int *n_out) {
+  int dev = 0;
+  HORA_CUDA_TRY(cudaGetDevice(&dev));
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, int> known;
+  std::lock_guard<std::mutex> g(mu);
+  auto it = known.find({kernel, dev});
+  if (it == known.end()) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * 152, 1, 1);
+    cfg.blockDim = dim3(kLpThreads, 1, 1);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kernel, &cfg) != cudaSuccess) {
+      cudaGetLastError();  // not an error of the search: the unpaired form runs
+      n = 0;
+    }
+    it = known.emplace(std::make_pair(kernel, dev), n).first;
+  }
+  *n_out = it->second;
+  g_pair_clusters.store(it->second);
+  return HORA_OK;
+}
+
 template <int PREC, int MT, int MODE>
 static int launch_lp3(const CUtensorMap &ta, const LpParams &p, cudaStream_t s) {
   const int smem = lp_smem_bytes(p.nkb, p.stages, PREC == HORA_PREC_BF16 && MT == M_L2);
@@ -1204,6 +1274,34 @@ static int launch_lp3(const CUtensorMap &ta, const LpParams &p, cudaStream_t s) 
   dim3 grid((unsigned)ceil_div(p.nq, kLpBM), (unsigned)ceil_div(rows, (int64_t)kLpBN * p.tpc));
   if (grid.x == 0 || grid.y == 0) return HORA_OK;
   ProfScope ps(PREC == HORA_PREC_BF16 ? "bf16_tc_scan" : "fp8_tc_scan", s);
+  if constexpr (PREC == HORA_PREC_BF16 && MODE == TILE_FILTER) {
+    if (p.pair && !p.items) {
+      // clusters of two on consecutive query blocks: an odd block count
+      // gets one more block past the queries (it loads its half of every
+      // tile for its peer and keeps nothing)
+      const void *kp = reinterpret_cast<const void *>(lowp_tile_kernel<PREC, MT, MODE, true>);
+      HORA_SMEM_ATTR(kp, smem);
+      int nc = 0;
+      HORA_TRY(pair_clusters(kp, smem, &nc));
+      if (nc > 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((grid.x + 1u) & ~1u, grid.y, 1);
+        cfg.blockDim = dim3(kLpThreads, 1, 1);
+        cfg.dynamicSmemBytes = (size_t)smem;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 2;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        HORA_CUDA_TRY(cudaLaunchKernelEx(&cfg, lowp_tile_kernel<PREC, MT, MODE, true>, ta, p));
+        HORA_LAUNCHED();
+        return HORA_OK;
+      }
+    }
+  }
   lowp_tile_kernel<PREC, MT, MODE><<<grid, kLpThreads, smem, s>>>(ta, p);
   HORA_LAUNCHED();
   return HORA_OK;
@@ -1849,6 +1947,7 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   LpParams p{};
   p.nq = nq;
   p.qmap = nullptr;
+  p.pair = h->scan_pairs;
   p.nkb = nkb;
   p.stages = stages;
   p.xsq = L.xsq.as<float>();
@@ -2107,6 +2206,10 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
 // op order) and the k best returned.  A query whose cluster has fewer than k
 // members, or whose kept rows overflow the candidate capacity, is answered
 // by the CUDA-core exact scan instead; either way the result is exact.
+// DotProduct and CosineSimilarity take the same steps with their own scan
+// keys, the bound eps of rerank_slack_kernel (the scan key against the
+// reference's f32 dot, or its -ab / (sqrt(aa) sqrt(bb))) and the probe's
+// delta for the metric (probe_bound).
 
 // 2 eps(q) per query (rounded up), from the staged f32 query rows.
 __global__ void exact_tc_slack_kernel(const float *Q, int64_t nq, int64_t ld, int64_t dim, int64_t Dp,
@@ -2159,7 +2262,8 @@ __global__ void scatter_keys_kernel(const uint64_t *src, int k, const int *list,
 }
 
 bool exact_tc_eligible(const hora_index *h, int k) {
-  return h->exact_tc && h->precision == HORA_PREC_FP32 && h->metric == M_L2 && h->n >= kProbeMinRows &&
+  return h->exact_tc && h->precision == HORA_PREC_FP32 &&
+         (h->metric == M_L2 || h->metric == M_IP || h->metric == M_COS) && h->n >= kProbeMinRows &&
          round_up((int64_t)h->dim, 64) / 64 <= 2 && k <= kExactTcMaxK;
 }
 
@@ -2176,8 +2280,10 @@ int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, 
   LowpState &L = *h->lowp;
   HORA_TRY(ensure_pivots(h, L, s));
   const int cap = (int)round_up(std::max(h->cand_cap, 2 * k), 128);
-  const int stages = lp_stages(nkb, true);
-  // BF16 queries, their f32 squared norms and the certified slack
+  const int mt = h->metric;
+  const int stages = lp_stages(nkb, mt == M_L2);
+  // BF16 queries (unit rows for CosineSimilarity), their f32 squared norms
+  // and the certified slack
   HORA_TRY(ws.lq.reserve(std::max<int64_t>(nq, 1) * Dp * 2));
   HORA_TRY(ws.lerr.reserve(16));
   HORA_TRY(ws.lqsq.reserve(sizeof(float) * std::max<int64_t>(nq, 1)));
@@ -2185,12 +2291,18 @@ int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, 
   const double *qsq64 = reinterpret_cast<const double *>(ws.qnorm.as<char>() + round_up(sizeof(float) * nq, 16));
   {
     ProfScope ps("lowp_convert", s);
-    to_bf16_kernel<<<ceil_div(nq * Dp, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, nullptr,
+    to_bf16_kernel<<<ceil_div(nq * Dp, 256), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp,
+                                                          mt == M_COS ? qsq64 : nullptr,
                                                           ws.lq.as<__nv_bfloat16>());
     HORA_LAUNCHED();
     f64_to_f32_kernel<<<ceil_div(nq, 256), 256, 0, s>>>(qsq64, nq, ws.lqsq.as<float>());
     HORA_LAUNCHED();
-    exact_tc_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, qsq64,
+    if (mt == M_L2)
+      exact_tc_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, qsq64,
+                                                            L.dxmax.as<float>(), L.xsqmax.as<float>(),
+                                                            ws.xslack.as<float>());
+    else
+      rerank_slack_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(ws.q.as<float>(), nq, h->ld, h->dim, Dp, mt, qsq64,
                                                           L.dxmax.as<float>(), L.xsqmax.as<float>(),
                                                           ws.xslack.as<float>());
     HORA_LAUNCHED();
@@ -2215,6 +2327,7 @@ int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, 
   LpParams p{};
   p.nq = nq;
   p.nkb = nkb;
+  p.pair = h->scan_pairs;
   p.stages = stages;
   p.xsq = L.xsq.as<float>();
   p.xnorm = h->xnorm.as<float>();
@@ -2234,15 +2347,15 @@ int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, 
     p.r_begin = lo;
     p.r_end = std::min<int64_t>(n, lo + max_chunk);
     p.tpc = lp_tiles_per_cta(nq, p.r_end - p.r_begin);
-    HORA_TRY(launch_lp(HORA_PREC_BF16, M_L2, TILE_FILTER, ta, L, p, s));
+    HORA_TRY(launch_lp(HORA_PREC_BF16, mt, TILE_FILTER, ta, L, p, s));
   }
   // the queries the pass cannot answer (read before the merge, which
   // consumes the counts), every kept row rescored exactly, then the k best
   exact_tc_fallback_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(count, nq, k, cap, lerr + 1,
                                                                      ws.xlist.as<int>());
   HORA_LAUNCHED();
-  HORA_TRY(launch_rerank_exact(M_L2, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim, nullptr, nullptr,
-                               p.cand, nq, cap, p.cand, s, count));
+  HORA_TRY(launch_rerank_exact(mt, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(),
+                               h->xnorm.as<float>(), p.cand, nq, cap, p.cand, s, count));
   HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
   HORA_TRY(launch_merge_topk(d_best, k, p.cand, count, cap, 0, nullptr, nq, flags, ovc, s));
   int hs[2] = {0, 0};
@@ -2256,14 +2369,20 @@ int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, 
     // the queries the certified pass could not answer: the CUDA-core scan
     h->last_probe = 2;
     const int64_t nl = hs[1];
-    HORA_TRY(ws.xq.reserve(sizeof(float) * nl * h->ld));
+    // their rows (pitch ld, a multiple of 4) and then their norms
+    HORA_TRY(ws.xq.reserve(sizeof(float) * nl * (h->ld + 1)));
     HORA_TRY(ws.xkeys.reserve(sizeof(uint64_t) * nl * k));
+    float *xq = ws.xq.as<float>(), *xqn = xq + nl * h->ld;
     gather_rows_f32_kernel<<<ceil_div(nl * (int64_t)h->ld, 256), 256, 0, s>>>(ws.q.as<float>(), h->ld,
-                                                                             ws.xlist.as<int>(), nl,
-                                                                             ws.xq.as<float>());
+                                                                             ws.xlist.as<int>(), nl, xq);
     HORA_LAUNCHED();
+    if (mt == M_COS) {
+      gather_rows_f32_kernel<<<ceil_div(nl, 256), 256, 0, s>>>(ws.qnorm.as<float>(), 1, ws.xlist.as<int>(), nl,
+                                                               xqn);
+      HORA_LAUNCHED();
+    }
     int retries = 0;
-    HORA_TRY(bf_topk_exact(base_view(h), M_L2, ws.xq.as<float>(), nullptr, nl, k, h->cand_cap, ws,
+    HORA_TRY(bf_topk_exact(base_view(h), mt, xq, mt == M_COS ? xqn : nullptr, nl, k, h->cand_cap, ws,
                            ws.xkeys.as<uint64_t>(), s, &retries));
     scatter_keys_kernel<<<ceil_div(nl * (int64_t)k, 256), 256, 0, s>>>(ws.xkeys.as<uint64_t>(), k,
                                                                       ws.xlist.as<int>(), nl, d_best);

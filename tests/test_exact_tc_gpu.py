@@ -1,5 +1,5 @@
-"""Exact FP32 Euclidean brute force with the BF16 tensor-core scan as a
-certified filter (HORA_OPT_EXACT_TC): the result must be the CUDA-core exact
+"""Exact FP32 brute force (Euclidean, DotProduct, CosineSimilarity) with the
+BF16 tensor-core scan as a certified filter (HORA_OPT_EXACT_TC): the result must be the CUDA-core exact
 scan's, bit for bit (distances, and ids including ties), on bases large
 enough for pivot clusters, including the queries the certified pass hands
 back to the CUDA-core scan (candidate overflow, duplicates at the k-th
@@ -13,13 +13,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _pair(hora, X, k, q, **opts):
+def _pair(hora, X, k, q, metric=None, **opts):
     import torch
     out = []
     for xtc in (1, 0):
         ix = hora.BruteForceIndex(X.shape[1])
         ix.madd(torch.from_numpy(X).cuda(), None)
-        ix.build(hora.Metric.Euclidean)
+        ix.build(hora.Metric.Euclidean if metric is None else metric)
         ix.set_option(hora.Option.EXACT_TC, xtc)
         for key, v in opts.items():
             ix.set_option(getattr(hora.Option, key), v)
@@ -72,5 +72,41 @@ def test_exact_tc_small_base_uses_cuda_cores(hora, gpu):
     X = synth.mixture(20_000, 32, 64, stream=75)
     (ia, da, pa, _), (ib, db, _, _) = _pair(hora, X, 10, X[:50])
     assert pa == 0
+    np.testing.assert_array_equal(da, db)
+    np.testing.assert_array_equal(ia, ib)
+
+
+@pytest.mark.parametrize("k", [1, 10, 100, 256])
+@pytest.mark.parametrize("mname", ["DotProduct", "CosineSimilarity"])
+def test_exact_tc_dot_and_cosine_equal_cuda_core_scan(hora, oracle, gpu, k, mname):
+    """DotProduct and CosineSimilarity through the certified pass: the keys
+    are the scan's dot (of unit rows for the cosine), the bound is the
+    windowed rerank's; the result is the CUDA-core scan's bit for bit and
+    the oracle's distances bit for bit."""
+    from hora_gb300 import synth
+    X = synth.mixture(131_072, 96, 256, stream=76)
+    q = synth.mixture(1_200, 96, 256, stream=77)
+    mt = getattr(hora.Metric, mname)
+    (ia, da, pa, fa), (ib, db, pb, _) = _pair(hora, X, k, q, metric=mt)
+    assert pa in (1, 2) and pb == 0, (pa, pb)
+    np.testing.assert_array_equal(da, db)
+    np.testing.assert_array_equal(ia, ib)
+    om = oracle.DOT if mname == "DotProduct" else oracle.COSINE
+    oi, od = oracle.bf_search(X, q[:32], k, om, threads=os.cpu_count() or 4)
+    np.testing.assert_array_equal(da[:32], od)
+
+
+def test_exact_tc_cosine_fallback_queries_keep_their_norms(hora, gpu):
+    """400 copies of one row and a candidate capacity of 256 at k = 100: the
+    queries beside the copies keep more rows than the capacity and go back
+    to the CUDA-core scan, which needs each gathered query's norm; the
+    result is still the CUDA-core scan's."""
+    from hora_gb300 import synth
+    X = synth.mixture(100_000, 64, 128, stream=78)
+    X[50_000:50_400] = X[7]
+    q = np.concatenate([synth.mixture(400, 64, 128, stream=79) * 3.0, X[7:8] * 2.0 + 1e-3],
+                       axis=0).astype(np.float32)
+    (ia, da, pa, fa), (ib, db, _, _) = _pair(hora, X, 100, q, metric=hora.Metric.CosineSimilarity, CAND_CAP=256)
+    assert pa == 2 and fa > 0, (pa, fa)
     np.testing.assert_array_equal(da, db)
     np.testing.assert_array_equal(ia, ib)
