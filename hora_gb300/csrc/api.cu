@@ -571,8 +571,6 @@ int hora_idx_info(const hora_index *h, char *buf, uint64_t cap) {
   s += ",\"last_overflow_queries\":" + std::to_string(h->last_overflow_queries.load());
   s += ",\"last_short_lists\":" + std::to_string(h->last_short_lists.load());
   s += ",\"last_fallback_queries\":" + std::to_string(h->last_fallback.load());
-  // clusters of two scan CTAs co-resident on the device (-1: not queried yet)
-  s += ",\"scan_pair_clusters\":" + std::to_string(g_pair_clusters.load());
   if (h->kind != HORA_INDEX_BRUTE_FORCE) {
     std::string iv;
     ivf_info(h, iv);
@@ -714,7 +712,6 @@ int hora_set_option(hora_index *h, int key, double v) {
       return HORA_OK;
     case HORA_OPT_BF_PROBE: h->bf_probe = v != 0; return HORA_OK;
     case HORA_OPT_EXACT_TC: h->exact_tc = v != 0; return HORA_OK;
-    case HORA_OPT_SCAN_PAIRS: h->scan_pairs = v != 0; return HORA_OK;
   }
   return fail(HORA_EINVAL, "unknown option");
 }
@@ -735,7 +732,6 @@ int hora_get_option(const hora_index *h, int key, double *out) {
     case HORA_OPT_NPROBE_PHASE1: *out = h->nprobe_phase1; return HORA_OK;
     case HORA_OPT_BF_PROBE: *out = h->bf_probe; return HORA_OK;
     case HORA_OPT_EXACT_TC: *out = h->exact_tc; return HORA_OK;
-    case HORA_OPT_SCAN_PAIRS: *out = h->scan_pairs; return HORA_OK;
   }
   return fail(HORA_EINVAL, "unknown option");
 }

@@ -29,11 +29,8 @@
 #include <cuda_fp8.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cfloat>
 #include <cstring>
-#include <map>
-#include <mutex>
 
 #include "dist_tile.cuh"
 #include "index.h"
@@ -136,9 +133,6 @@ struct LpParams {
   // FP8 filter: per 32 image rows {min |x|^2, min scale, max scale, 0}, or
   // null (see group_meta_kernel)
   const float4 *gmeta;
-  // BF16 filter passes: CTA pairs that share each base tile's L2 read
-  // (the PAIR form of lowp_tile_kernel), where clusters of two fit
-  int pair;
 };
 
 // BF16 Euclidean folds the row norm into the MMA: one extra K = 16 step
@@ -341,13 +335,7 @@ __device__ __forceinline__ void stage_hits(const uint32_t (&v)[32], uint32_t hit
   }
 }
 
-// PAIR: launched in clusters of two CTAs on consecutive query blocks and
-// the same base rows; each CTA loads one of the two halves of every base
-// tile (K block 0; the rest) and multicasts it into both CTAs' rings, so the
-// pair reads each tile from L2 once.  A ring slot is refilled once both
-// CTAs' MMAs are done with it: every MMA commit that frees a slot arrives
-// on the slot's barrier in both CTAs (count 2).
-template <int PREC, int MT, int MODE, bool PAIR = false>
+template <int PREC, int MT, int MODE>
 __global__ void __launch_bounds__(kLpThreads, 1)
     lowp_tile_kernel(const __grid_constant__ CUtensorMap tmap_a, LpParams p) {
   constexpr bool FOLD = PREC == HORA_PREC_BF16 && MT == M_L2;
@@ -393,9 +381,9 @@ __global__ void __launch_bounds__(kLpThreads, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       tc::mbar_init(full + s, 1);
-      tc::mbar_init(empty + s, PAIR ? 2 : 1);
+      tc::mbar_init(empty + s, 1);
       tc::mbar_init(full2 + s, 1);
-      tc::mbar_init(empty2 + s, PAIR ? 2 : 1);
+      tc::mbar_init(empty2 + s, 1);
     }
     tc::mbar_init(a_full, 1);
     for (int b = 0; b < kLpNB; ++b) {
@@ -419,8 +407,6 @@ __global__ void __launch_bounds__(kLpThreads, 1)
   if (warp == 1) tc::tmem_alloc(tmem_slot, kLpNB * kLpBN);
   tc::fence_before_sync();
   __syncthreads();
-  // PAIR: the peer's barriers are initialised before anything arrives on them
-  if (PAIR) tc::cluster_sync();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
@@ -435,27 +421,17 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       // stage's layout; the first half (K block 0) and the rest separately
       const uint8_t *img = p.tiles + (row0 / kLpBN) * (int64_t)stage_bytes;
       const uint32_t rest = stage_bytes - b_kb_bytes;
-      // PAIR: rank 0 copies K block 0 into both CTAs, rank 1 the rest (all
-      // of it with a single K block and no norm block); each CTA expects
-      // both halves on its own barriers
-      const uint32_t rank = PAIR ? tc::cluster_ctarank() : 0u;
       for (int t = 0; t < T; ++t) {
         const int s = t % S, j = t / S;
         uint8_t *st = sB + (size_t)s * stage_bytes;
         const uint8_t *src = img + (int64_t)t * stage_bytes;
         if (j > 0 && !tc::mbar_wait(empty + s, (j - 1) & 1, abort)) break;
         tc::mbar_arrive_expect_tx(full + s, b_kb_bytes);
-        if (!PAIR)
-          tc::bulk_load(st, src, b_kb_bytes, full + s);
-        else if (rank == (rest ? 0u : 1u))
-          tc::bulk_load_multicast(st, src, b_kb_bytes, full + s, 0x3);
+        tc::bulk_load(st, src, b_kb_bytes, full + s);
         if (rest) {
           if (j > 0 && !tc::mbar_wait(empty2 + s, (j - 1) & 1, abort)) break;
           tc::mbar_arrive_expect_tx(full2 + s, rest);
-          if (!PAIR)
-            tc::bulk_load(st + b_kb_bytes, src + b_kb_bytes, rest, full2 + s);
-          else if (rank == 1u)
-            tc::bulk_load_multicast(st + b_kb_bytes, src + b_kb_bytes, rest, full2 + s, 0x3);
+          tc::bulk_load(st + b_kb_bytes, src + b_kb_bytes, rest, full2 + s);
         }
       }
     }
@@ -476,10 +452,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         for (int kb = 0; kb < nkb; ++kb) {
           if (kb == 1) {
             // K block 0 read: its half of the stage may be refilled
-            if (PAIR)
-              tc::mma_commit_multicast(empty + s, 0x3);
-            else
-              tc::mma_commit(empty + s);
+            tc::mma_commit(empty + s);
             if (!tc::mbar_wait(full2 + s, j & 1, abort)) {
               ok2 = false;
               break;
@@ -502,10 +475,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         if (!ok2) break;
         if (FOLD) {
           if (nkb == 1) {
-            if (PAIR)
-              tc::mma_commit_multicast(empty + s, 0x3);
-            else
-              tc::mma_commit(empty + s);
+            tc::mma_commit(empty + s);
             if (!tc::mbar_wait(full2 + s, j & 1, abort)) break;
             tc::fence_after_sync();
           }
@@ -513,10 +483,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
           const uint64_t bd = tc::sdesc_kmajor_none(tc::smem_u32(st + nkb * b_kb_bytes), kNormHalfB, 128);
           tc::mma_bf16(d, ad, bd, idesc, 1u);
         }
-        if (PAIR)
-          tc::mma_commit_multicast(rest ? empty2 + s : empty + s, 0x3);
-        else
-          tc::mma_commit(rest ? empty2 + s : empty + s);
+        tc::mma_commit(rest ? empty2 + s : empty + s);
         tc::mma_commit(acc_full + b);
       }
       // all MMAs of this thread complete before TMEM is released
@@ -728,9 +695,6 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     tc::tmem_dealloc(tmem, kLpNB * kLpBN);
   }
   if (threadIdx.x == 0 && *abort) atomicExch(p.err, 1);
-  // PAIR: neither CTA leaves while the other may still copy into its ring
-  // or arrive on its barriers
-  if (PAIR) tc::cluster_sync();
 }
 
 // ---- conversions -------------------------------------------------------------------
@@ -1232,40 +1196,6 @@ static int lp_tiles_per_cta(int64_t nq, int64_t rows) {
   return kLpMinTilesPerCta;
 }
 
-// Co-resident clusters of two CTAs of `kernel` (smem bytes each) on the
-// current device, queried once per (kernel, device); 0 when none fit.
-std::atomic<int> g_pair_clusters{-1};  // the last answer, for hora_idx_info
-static int pair_clusters(const void *kernel, int smem, int *n_out) {
-  int dev = 0;
-  HORA_CUDA_TRY(cudaGetDevice(&dev));
-  static std::mutex mu;
-  static std::map<std::pair<const void *, int>, int> known;
-  std::lock_guard<std::mutex> g(mu);
-  auto it = known.find({kernel, dev});
-  if (it == known.end()) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(2 * 152, 1, 1);
-    cfg.blockDim = dim3(kLpThreads, 1, 1);
-    cfg.dynamicSmemBytes = (size_t)smem;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = 2;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, kernel, &cfg) != cudaSuccess) {
-      cudaGetLastError();  // not an error of the search: the unpaired form runs
-      n = 0;
-    }
-    it = known.emplace(std::make_pair(kernel, dev), n).first;
-  }
-  *n_out = it->second;
-  g_pair_clusters.store(it->second);
-  return HORA_OK;
-}
-
 template <int PREC, int MT, int MODE>
 static int launch_lp3(const CUtensorMap &ta, const LpParams &p, cudaStream_t s) {
   const int smem = lp_smem_bytes(p.nkb, p.stages, PREC == HORA_PREC_BF16 && MT == M_L2);
@@ -1274,34 +1204,6 @@ static int launch_lp3(const CUtensorMap &ta, const LpParams &p, cudaStream_t s) 
   dim3 grid((unsigned)ceil_div(p.nq, kLpBM), (unsigned)ceil_div(rows, (int64_t)kLpBN * p.tpc));
   if (grid.x == 0 || grid.y == 0) return HORA_OK;
   ProfScope ps(PREC == HORA_PREC_BF16 ? "bf16_tc_scan" : "fp8_tc_scan", s);
-  if constexpr (PREC == HORA_PREC_BF16 && MODE == TILE_FILTER) {
-    if (p.pair && !p.items) {
-      // clusters of two on consecutive query blocks: an odd block count
-      // gets one more block past the queries (it loads its half of every
-      // tile for its peer and keeps nothing)
-      const void *kp = reinterpret_cast<const void *>(lowp_tile_kernel<PREC, MT, MODE, true>);
-      HORA_SMEM_ATTR(kp, smem);
-      int nc = 0;
-      HORA_TRY(pair_clusters(kp, smem, &nc));
-      if (nc > 0) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((grid.x + 1u) & ~1u, grid.y, 1);
-        cfg.blockDim = dim3(kLpThreads, 1, 1);
-        cfg.dynamicSmemBytes = (size_t)smem;
-        cfg.stream = s;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = 2;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        HORA_CUDA_TRY(cudaLaunchKernelEx(&cfg, lowp_tile_kernel<PREC, MT, MODE, true>, ta, p));
-        HORA_LAUNCHED();
-        return HORA_OK;
-      }
-    }
-  }
   lowp_tile_kernel<PREC, MT, MODE><<<grid, kLpThreads, smem, s>>>(ta, p);
   HORA_LAUNCHED();
   return HORA_OK;
@@ -1947,7 +1849,6 @@ int lowp_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint
   LpParams p{};
   p.nq = nq;
   p.qmap = nullptr;
-  p.pair = h->scan_pairs;
   p.nkb = nkb;
   p.stages = stages;
   p.xsq = L.xsq.as<float>();
@@ -2327,7 +2228,6 @@ int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, 
   LpParams p{};
   p.nq = nq;
   p.nkb = nkb;
-  p.pair = h->scan_pairs;
   p.stages = stages;
   p.xsq = L.xsq.as<float>();
   p.xnorm = h->xnorm.as<float>();

@@ -52,7 +52,6 @@ struct hora_index {
   int nprobe_phase1 = 4;
   int bf_probe = 1;
   int exact_tc = 1;
-  int scan_pairs = 0;  // HORA_OPT_SCAN_PAIRS
 
   cudaStream_t stream = nullptr;
   std::mutex mu;
@@ -118,9 +117,6 @@ bool coarse_tc_eligible(const hora_index *h);
 int coarse_tc_probe(hora_index *h, const float *centers, const float *cnorm, int64_t C, int64_t nq, int pmax,
                     SearchWorkspace &ws, float *dist, uint64_t *probes, cudaStream_t s);
 int exact_tc_prepare(hora_index *h, cudaStream_t s);
-// Co-resident clusters of two BF16 filter-pass CTAs on the device the last
-// paired launch ran on (-1 before the first).
-extern std::atomic<int> g_pair_clusters;
 int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, uint64_t *d_best,
                          cudaStream_t s);
 

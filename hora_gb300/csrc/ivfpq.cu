@@ -871,13 +871,17 @@ __device__ __forceinline__ void lut_build_g(const float *book, const float *zq, 
 // Per list of a group, the selection state (ints): the range of the
 // distance words, the radix digit position, keys still to take, prefix and
 // mask of the digits fixed so far, done, phase (0: distance digits, 1: row
-// digits among the keys equal to tau), tau, the row bound, the compaction
-// count.
+// digits among the keys equal to tau, 2: the keys of the k-th key's bin
+// ranked in one warp), tau, the row bound, the compaction count, the keys
+// of that bin gathered for the rank.
 enum : int {
   kStMin = 0, kStMax, kStShift, kStRem, kStPrefix, kStMask, kStDone, kStPhase, kStTau, kStRBound,
-  kStCnt, kStWords = 16
+  kStCnt, kStBCnt, kStWords = 16
 };
 constexpr int kSelDigitBits = 11, kSelNB = 1 << kSelDigitBits;
+// A bin holding the k-th key and at most this many keys in all is settled
+// by ranking its keys instead of another radix pass over the list.
+constexpr int kSelRankMax = 32;
 
 // Every lane of the warp: the bin of a kSelNB-bin histogram whose
 // cumulative count first reaches rem (1 <= rem <= total) and the count below
@@ -929,15 +933,20 @@ __device__ __forceinline__ void warp_find_bin_all(const uint32_t *hist, uint32_t
 // distinct within a list, so the selection is exact.  A radix select for
 // all lists at once (every thread works in every pass): 11-bit digits of
 // the distance word minus the list's minimum, from the top of its range,
-// stopping per list once the k-th key's bin is taken whole; a list whose
-// k-th distance is tied past the last digit continues on the row digits of
-// the tied keys.  The kept keys go through od / orow to the head.  st holds
-// the per-list state (kStWords ints per list, kStMin / kStMax already set by
-// the caller); hist is zero on entry and on return.  0 < k < L.
+// stopping per list once the k-th key's bin is taken whole, or once that
+// bin holds at most kSelRankMax keys: the compaction then gathers them
+// (bd / brow, kSelRankMax words per list) and one warp ranks them by
+// (distance, row), which saves the further passes over the whole list; a
+// list whose k-th distance is tied past the last digit in a larger bin
+// continues on the row digits of the tied keys.  The kept keys go through
+// od / orow to the head.  st holds the per-list state (kStWords ints per
+// list, kStMin / kStMax already set by the caller); hist is zero on entry
+// and on return.  0 < k < L.
 template <int G>
 __device__ __forceinline__ void cta_select_group(uint32_t *dk, int stride, uint32_t *hrow,
                                                  const uint32_t *crow, int held, int gc, int L, int k,
-                                                 uint32_t *hist, int *st, uint32_t *od, uint32_t *orow) {
+                                                 uint32_t *hist, int *st, uint32_t *od, uint32_t *orow,
+                                                 uint32_t *bd, uint32_t *brow) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x < gc) {
     int *q = st + threadIdx.x * kStWords;
@@ -952,6 +961,7 @@ __device__ __forceinline__ void cta_select_group(uint32_t *dk, int stride, uint3
     q[kStTau] = 0;
     q[kStRBound] = -1;
     q[kStCnt] = 0;
+    q[kStBCnt] = 0;
   }
   __syncthreads();
   for (int pass = 0; pass < 2 * (32 + kSelDigitBits - 1) / kSelDigitBits; ++pass) {
@@ -1002,6 +1012,13 @@ __device__ __forceinline__ void cta_select_group(uint32_t *dk, int stride, uint3
             q[kStRBound] = (int)(prefix | low);
           }
           q[kStDone] = 1;
+        } else if (q[kStPhase] == 0 && at <= (uint32_t)kSelRankMax) {
+          // few keys share the bin: the compaction gathers them and one
+          // warp takes the rem smallest (distance, row) among them
+          q[kStPrefix] = (int)prefix;
+          q[kStMask] = (int)((uint32_t)q[kStMask] | ((uint32_t)(kSelNB - 1) << shift));
+          q[kStPhase] = 2;
+          q[kStDone] = 1;
         } else if (shift == 0 && q[kStPhase] == 0) {
           // the k-th distance itself, tied: the smallest rows among the ties
           q[kStTau] = (int)((uint32_t)q[kStMin] + prefix);
@@ -1024,12 +1041,35 @@ __device__ __forceinline__ void cta_select_group(uint32_t *dk, int stride, uint3
     for (int g = 0; g < gc; ++g) all = all && st[g * kStWords + kStDone];
     if (all) break;
   }
-  // kept: distance below tau, or equal with the row at or below the bound
+  // kept: distance below tau, or equal with the row at or below the bound;
+  // a list in phase 2 keeps the keys below its bin and gathers the bin's
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     if (g >= gc) break;
-    const uint32_t tau = (uint32_t)st[g * kStWords + kStTau], rb = (uint32_t)st[g * kStWords + kStRBound];
     int *cnt = st + g * kStWords + kStCnt;
+    if (st[g * kStWords + kStPhase] == 2) {
+      const uint32_t kmin = (uint32_t)st[g * kStWords + kStMin];
+      const uint32_t prefix = (uint32_t)st[g * kStWords + kStPrefix], mask = (uint32_t)st[g * kStWords + kStMask];
+      int *bcnt = st + g * kStWords + kStBCnt;
+      for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        const uint32_t d = dk[g * stride + i], dd = d - kmin;
+        if (dd < prefix) {
+          const int pos = atomicAdd(cnt, 1);
+          if (pos < k) {
+            od[g * k + pos] = d;
+            orow[g * k + pos] = i < held ? hrow[g * k + i] : crow[i - held];
+          }
+        } else if ((dd & mask) == prefix) {
+          const int b = atomicAdd(bcnt, 1);
+          if (b < kSelRankMax) {
+            bd[g * kSelRankMax + b] = d;
+            brow[g * kSelRankMax + b] = i < held ? hrow[g * k + i] : crow[i - held];
+          }
+        }
+      }
+      continue;
+    }
+    const uint32_t tau = (uint32_t)st[g * kStWords + kStTau], rb = (uint32_t)st[g * kStWords + kStRBound];
     for (int i = threadIdx.x; i < L; i += blockDim.x) {
       const uint32_t d = dk[g * stride + i];
       if (d > tau) continue;
@@ -1041,6 +1081,26 @@ __device__ __forceinline__ void cta_select_group(uint32_t *dk, int stride, uint3
           orow[g * k + pos] = r;
         }
       }
+    }
+  }
+  __syncthreads();
+  // phase 2: the rank of each gathered key among them by (distance, row);
+  // the rem smallest follow the keys below the bin
+  if (warp < gc && st[warp * kStWords + kStPhase] == 2) {
+    const int *q = st + warp * kStWords;
+    const int n = min(q[kStBCnt], kSelRankMax), rem = q[kStRem], base = q[kStCnt];
+    const uint32_t d = lane < n ? bd[warp * kSelRankMax + lane] : 0xffffffffu;
+    const uint32_t r = lane < n ? brow[warp * kSelRankMax + lane] : 0xffffffffu;
+    int rank = 0;
+#pragma unroll
+    for (int j = 0; j < kSelRankMax; ++j) {
+      const uint32_t dj = __shfl_sync(0xffffffffu, d, j), rj = __shfl_sync(0xffffffffu, r, j);
+      rank += j < n && (dj < d || (dj == d && rj < r));
+    }
+    const int pos = base + rank;
+    if (lane < n && rank < rem && pos < k) {
+      od[warp * k + pos] = d;
+      orow[warp * k + pos] = r;
     }
   }
   __syncthreads();
@@ -1060,13 +1120,13 @@ __host__ __device__ inline size_t adc_lut_floats(int G, int M, int K) {
 
 // Dynamic shared memory of adc_group_kernel: the G-wide LUT, the G residual
 // queries, per query the distance words of the kept R plus a chunk and the
-// rows of the kept R, the rows of a chunk, per query a selection histogram
-// and 2 R words of selection output, the selection state, the subspace
-// table.
+// rows of the kept R, the rows of a chunk, per query a selection histogram,
+// 2 R words of selection output and 2 kSelRankMax words of ranked keys, the
+// selection state, the subspace table.
 __host__ __device__ inline size_t adc_group_smem(int G, int M, int K, int dz, int R) {
   return sizeof(float) * (adc_lut_floats(G, M, K) + (size_t)G * dz) +
          sizeof(uint32_t) * ((size_t)G * (kAdcChunk + R) + (size_t)G * R + kAdcChunk +
-                             (size_t)G * kSelNB + (size_t)2 * G * R) +
+                             (size_t)G * kSelNB + (size_t)2 * G * R + (size_t)2 * G * kSelRankMax) +
          sizeof(int) * ((size_t)kStWords * G + 2 * M);
 }
 
@@ -1103,7 +1163,9 @@ __global__ void __launch_bounds__(kAdcThreads, 1) adc_group_kernel(
   uint32_t *hist = crow + kAdcChunk;                                   // G * kSelNB
   uint32_t *od = hist + G * kSelNB;                                    // G * R
   uint32_t *orow = od + G * R;                                         // G * R
-  int *st = reinterpret_cast<int *>(orow + G * R);                     // G * kStWords
+  uint32_t *bd = orow + G * R;                                         // G * kSelRankMax
+  uint32_t *brow = bd + G * kSelRankMax;                               // G * kSelRankMax
+  int *st = reinterpret_cast<int *>(brow + G * kSelRankMax);           // G * kStWords
   int *sbs = st + G * kStWords;                                        // M
   int *sls = sbs + M;                                                  // M
   for (int m = threadIdx.x; m < M; m += blockDim.x) {
@@ -1243,7 +1305,7 @@ __global__ void __launch_bounds__(kAdcThreads, 1) adc_group_kernel(
           }
         }
         __syncthreads();
-        cta_select_group<G>(dk, stride, hrow, crow, held, gc, tot, R, hist, st, od, orow);
+        cta_select_group<G>(dk, stride, hrow, crow, held, gc, tot, R, hist, st, od, orow, bd, brow);
         held = R;
       } else {
         // short so far: the chunk's rows join the head as they are

@@ -53,7 +53,6 @@ class Option(enum.IntEnum):
     NPROBE_PHASE1 = 11
     BF_PROBE = 12
     EXACT_TC = 13
-    SCAN_PAIRS = 14
 
 
 @dataclass

@@ -133,7 +133,7 @@ typedef enum {
                                   lists, up to 4,096), then one pass over the base
                                   (default 1; 0 = chunked schedule only; same
                                   results either way) */
-  HORA_OPT_EXACT_TC = 13,      /* exact FP32 brute force (Euclidean, DotProduct,
+  HORA_OPT_EXACT_TC = 13       /* exact FP32 brute force (Euclidean, DotProduct,
                                   CosineSimilarity) on >= 65,536 rows, dim <=
                                   128, k <= 256: the BF16 tensor-core scan as a
                                   filter certified by a rounding-error bound, then
@@ -143,12 +143,6 @@ typedef enum {
                                   the nprobe-th rescored exactly (default 1; 0 =
                                   the CUDA-core FP32 passes; same results either
                                   way) */
-  HORA_OPT_SCAN_PAIRS = 14     /* BF16 filter passes of the tensor-core scan in
-                                  clusters of two CTAs that share each base
-                                  tile's read (each loads half and multicasts
-                                  it to both), where such clusters fit on the
-                                  device (1; default 0 = one CTA per query
-                                  block; same results either way) */
 } hora_option;
 
 typedef struct hora_index hora_index;
