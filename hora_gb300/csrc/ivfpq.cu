@@ -706,11 +706,37 @@ __device__ __forceinline__ void adc_row_g(const uint8_t *code, const float *lut,
 // group each, and every 16-byte gather is conflict-free; each lane still adds
 // its subspaces in order 0..31 (bit-identical sums).  The code row is
 // shifted by sk bytes once, so that step s reads byte s of it.
+// Two f32 operations in one instruction (sm_100 and later), each lane
+// rounded to nearest-even as __fadd_rn / __fsub_rn / __fmul_rn round it:
+// the same bits as the two scalar operations.
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
+  float2 r;
+  asm("{ .reg .b64 x, y, z; mov.b64 x, {%2, %3}; mov.b64 y, {%4, %5}; add.rn.f32x2 z, x, y; mov.b64 {%0, %1}, z; }"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+  float2 r;
+  asm("{ .reg .b64 x, y, z; mov.b64 x, {%2, %3}; mov.b64 y, {%4, %5}; sub.rn.f32x2 z, x, y; mov.b64 {%0, %1}, z; }"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
+  float2 r;
+  asm("{ .reg .b64 x, y, z; mov.b64 x, {%2, %3}; mov.b64 y, {%4, %5}; mul.rn.f32x2 z, x, y; mov.b64 {%0, %1}, z; }"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+
 template <int G>
 __device__ __forceinline__ void adc_row32_skew_g(const uint4 w0, const uint4 w1, const float *lut, int sk,
                                                  float (&d)[G]) {
 #pragma unroll
   for (int g = 0; g < G; ++g) d[g] = 0.0f;
+  float2 d01 = make_float2(0.0f, 0.0f), d23 = d01;  // G = 4: two queries per packed add
   const uint32_t c[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
   // B = the 32 code bytes moved up by sk bytes (10 words, zero filled)
   const int q = sk >> 2, r = 8 * (sk & 3);
@@ -731,10 +757,8 @@ __device__ __forceinline__ void adc_row32_skew_g(const uint4 w0, const uint4 w1,
       const int e = j * 32 + m;
       if (G == 4) {
         const float4 v = reinterpret_cast<const float4 *>(lut)[e];
-        d[0] = __fadd_rn(d[0], v.x);
-        d[1 % G] = __fadd_rn(d[1 % G], v.y);
-        d[2 % G] = __fadd_rn(d[2 % G], v.z);
-        d[3 % G] = __fadd_rn(d[3 % G], v.w);
+        d01 = add2_rn(d01, make_float2(v.x, v.y));
+        d23 = add2_rn(d23, make_float2(v.z, v.w));
       } else if (G == 2) {
         const float2 v = reinterpret_cast<const float2 *>(lut)[e];
         d[0] = __fadd_rn(d[0], v.x);
@@ -743,6 +767,12 @@ __device__ __forceinline__ void adc_row32_skew_g(const uint4 w0, const uint4 w1,
         d[0] = __fadd_rn(d[0], lut[e]);
       }
     }
+  }
+  if (G == 4) {
+    d[0] = d01.x;
+    d[1 % G] = d01.y;
+    d[2 % G] = d23.x;
+    d[3 % G] = d23.y;
   }
 }
 
@@ -803,12 +833,34 @@ __device__ __forceinline__ void lut_build_g(const float *book, const float *zq, 
         const int i = i0 + u * blockDim.x;
         if (i < MK) {
           float acc[G];
+          if (MT == M_L2 && G == 4) {
+            // two queries per packed sub / mul / add, each query's sum in
+            // the order and rounding of dist_op
+            float2 a01 = make_float2(0.0f, 0.0f), a23 = a01;
+            const float cd[4] = {cv[u].x, cv[u].y, cv[u].z, cv[u].w};
+            const float z0[4] = {z[0].x, z[0].y, z[0].z, z[0].w}, z1[4] = {z[1 % G].x, z[1 % G].y, z[1 % G].z, z[1 % G].w};
+            const float z2[4] = {z[2 % G].x, z[2 % G].y, z[2 % G].z, z[2 % G].w};
+            const float z3[4] = {z[3 % G].x, z[3 % G].y, z[3 % G].z, z[3 % G].w};
 #pragma unroll
-          for (int g = 0; g < G; ++g) {
-            float a = dist_op<MT>(0.0f, z[g].x, cv[u].x);
-            a = dist_op<MT>(a, z[g].y, cv[u].y);
-            a = dist_op<MT>(a, z[g].z, cv[u].z);
-            acc[g] = dist_op<MT>(a, z[g].w, cv[u].w);
+            for (int t = 0; t < 4; ++t) {
+              const float2 c2 = make_float2(cd[t], cd[t]);
+              const float2 t01 = sub2_rn(make_float2(z0[t], z1[t]), c2);
+              const float2 t23 = sub2_rn(make_float2(z2[t], z3[t]), c2);
+              a01 = add2_rn(a01, mul2_rn(t01, t01));
+              a23 = add2_rn(a23, mul2_rn(t23, t23));
+            }
+            acc[0] = a01.x;
+            acc[1 % G] = a01.y;
+            acc[2 % G] = a23.x;
+            acc[3 % G] = a23.y;
+          } else {
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+              float a = dist_op<MT>(0.0f, z[g].x, cv[u].x);
+              a = dist_op<MT>(a, z[g].y, cv[u].y);
+              a = dist_op<MT>(a, z[g].z, cv[u].z);
+              acc[g] = dist_op<MT>(a, z[g].w, cv[u].w);
+            }
           }
           lut_store_g<G, MT>(lut, (((i >> 3) & 3) | ((i >> 7) << 2)) * 32 + m, acc);
         }
