@@ -706,9 +706,9 @@ __device__ __forceinline__ void adc_row_g(const uint8_t *code, const float *lut,
 // group each, and every 16-byte gather is conflict-free; each lane still adds
 // its subspaces in order 0..31 (bit-identical sums).  The code row is
 // shifted by sk bytes once, so that step s reads byte s of it.
-// Two f32 operations in one instruction (sm_100 and later), each lane
-// rounded to nearest-even as __fadd_rn / __fsub_rn / __fmul_rn round it:
-// the same bits as the two scalar operations.
+// Two f32 additions / subtractions in one instruction (sm_100 and later),
+// each lane rounded to nearest-even as __fadd_rn / __fsub_rn round it: the
+// same bits as the two scalar operations.
 __device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
   float2 r;
   asm("{ .reg .b64 x, y, z; mov.b64 x, {%2, %3}; mov.b64 y, {%4, %5}; add.rn.f32x2 z, x, y; mov.b64 {%0, %1}, z; }"
@@ -723,12 +723,12 @@ __device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
   return r;
 }
+// The products stay scalar: with a packed multiply feeding a packed add,
+// distances came out one rounding away from the scalar sequence's (the pair
+// was fused), while a scalar multiply with an explicit rounding is never
+// fused.
 __device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
-  float2 r;
-  asm("{ .reg .b64 x, y, z; mov.b64 x, {%2, %3}; mov.b64 y, {%4, %5}; mul.rn.f32x2 z, x, y; mov.b64 {%0, %1}, z; }"
-      : "=f"(r.x), "=f"(r.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return r;
+  return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
 }
 
 template <int G>

@@ -58,6 +58,25 @@ def test_build_matches_oracle(hora, oracle, gpu, mt):
         same_up_to_ties(ids.astype(np.int64), d, oi, od)
 
 
+@pytest.mark.parametrize("mt", [3, 2])
+def test_adc_bit_exact_32_subspaces_of_256(hora, oracle, gpu, mt):
+    """dim 128 with 32 x 8-bit sub-quantizers (the bench's layout): the
+    code-major LUT built for groups of 4 queries, the skewed code-row scan
+    with two queries per packed add; ADC distances equal the oracle's bit for
+    bit at nprobe 1 and 4."""
+    rng = np.random.default_rng(77 + mt)
+    cen = (rng.standard_normal((16, 128)) * 3).astype(np.float32)
+    X = (cen[rng.integers(0, 16, 12000)] + rng.standard_normal((12000, 128))).astype(np.float32)
+    ix = ivf(hora, X, 32, 8, 16, 3, mt=mt, nprobe=4)
+    ref = dict(ix.export(), metric=mt)
+    q = (X[:64] + 0.1 * rng.standard_normal((64, 128))).astype(np.float32)
+    for nprobe in (1, 4):
+        ids, d = ix.search_batch(q, 10, nprobe=nprobe)
+        oi, od = oracle.ivfpq_search(ref, q, 10, nprobe)
+        np.testing.assert_array_equal(d, od)
+        same_up_to_ties(ids.astype(np.int64), d, oi, od)
+
+
 def test_codes_bit_exact_given_codebooks(hora, oracle, gpu):
     rng = np.random.default_rng(5)
     X = rng.standard_normal((4000, 32)).astype(np.float32)
