@@ -329,6 +329,17 @@ def run_ivf(a, H, base, q, exact):
                                "qps": ns / dt, "seconds": dt,
                                "recall@10": recall_at(ci, ex10[:ns], 10) if ex10 is not None else None,
                                "note": "ADC distances only (reference semantics, no rerank)"}
+        # as shipped: one query per call on one thread, latency sum
+        # (examples/src/ann_bench.rs:195-218; the reference's LUT loop may use
+        # rayon threads, this port's is serial)
+        lat = []
+        for i in range(200):
+            t1 = time.perf_counter()
+            O.ivfpq_search(ex, q[i:i + 1], 10, 2, threads=1)
+            lat.append(time.perf_counter() - t1)
+        out["cpu_baseline"]["as_shipped"] = {"value": len(lat) / sum(lat), "unit": "queries/s", "cores": 1,
+                                             "kind": "port", "sample": "200 queries one at a time, nprobe 2",
+                                             "p50_ms": float(np.percentile(lat, 50) * 1e3)}
         del ex
     except Exception as e:  # the CPU leg is a reported baseline only
         out["cpu_baseline"] = {"error": str(e)}
