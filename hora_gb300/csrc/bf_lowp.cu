@@ -963,9 +963,24 @@ __global__ void probe_select_kernel(const uint64_t *pkeys, const int64_t *coff, 
     const int m = lane + 32 * i;
     v[i] = m < L ? f2ord(pq[m]) : 0xffffffffu;
   }
-  // the largest a with fewer than R values below it is the R-th smallest
-  uint32_t a = 0;
-  for (int b = 31; b >= kSelectSkip; --b) {
+  // the largest a with fewer than R values below it is the R-th smallest;
+  // the bits above the highest one in which the members' values differ are
+  // theirs in common (a descent through them would take exactly those: a
+  // set bit leaves no value below, a clear one all L >= R), so it starts
+  // below them
+  uint32_t lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+  for (int i = 0; i < kProbeMaxMembers / 32; ++i) {
+    if (lane + 32 * i < L) {
+      lo = min(lo, v[i]);
+      hi = max(hi, v[i]);
+    }
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  const int top = 31 - __clz((int)(lo ^ hi));  // -1 when every value is equal
+  uint32_t a = top < 0 ? lo : top >= 31 ? 0u : lo & ~((2u << top) - 1u);
+  for (int b = top; b >= kSelectSkip; --b) {
     const uint32_t tt = a | (1u << b);
     int cnt = 0;
 #pragma unroll

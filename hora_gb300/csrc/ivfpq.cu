@@ -122,13 +122,13 @@ __global__ void coarse_init_kernel(const float *X, int64_t ld, int64_t n, int64_
 // whose label is outside [0, C) (an empty key) is left out of every bucket.
 constexpr int kSortBlock = 1024;
 
-__global__ void label_hist_kernel(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
+__global__ void label_hist_kernel(const uint64_t *keys, const uint32_t *labels, int64_t n, int C, int bs,
                                   uint32_t *block_counts) {
   extern __shared__ uint32_t hist[];
   for (int c = threadIdx.x; c < C; c += blockDim.x) hist[c] = 0;
   __syncthreads();
-  int64_t lo = (int64_t)blockIdx.x * kSortBlock;
-  for (int64_t i = lo + threadIdx.x; i < min(n, lo + kSortBlock); i += blockDim.x) {
+  int64_t lo = (int64_t)blockIdx.x * bs;
+  for (int64_t i = lo + threadIdx.x; i < min(n, lo + bs); i += blockDim.x) {
     uint32_t l = keys ? key_row(keys[i]) : labels[i];
     if (l < (uint32_t)C) atomicAdd(&hist[l], 1u);
   }
@@ -136,48 +136,66 @@ __global__ void label_hist_kernel(const uint64_t *keys, const uint32_t *labels, 
   for (int c = threadIdx.x; c < C; c += blockDim.x) block_counts[(int64_t)blockIdx.x * C + c] = hist[c];
 }
 
-// per label: running offsets over blocks; totals -> counts[c]
+// per label: running offsets over blocks; totals -> counts[c].  One warp
+// per label, 32 blocks per step (a warp scan of their counts).
 __global__ void label_block_scan_kernel(uint32_t *block_counts, int64_t nblocks, int C,
                                         int64_t *counts) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (c >= C) return;
   uint32_t run = 0;
-  for (int64_t b = 0; b < nblocks; ++b) {
-    uint32_t v = block_counts[b * C + c];
-    block_counts[b * C + c] = run;
-    run += v;
+  for (int64_t b0 = 0; b0 < nblocks; b0 += 32) {
+    const int64_t b = b0 + lane;
+    const uint32_t v = b < nblocks ? block_counts[b * C + c] : 0u;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (b < nblocks) block_counts[b * C + c] = run + inc - v;
+    run += __shfl_sync(0xffffffffu, inc, 31);
   }
-  counts[c] = run;
+  if (lane == 0) counts[c] = run;
 }
 
 // exclusive scan of C counts into offsets[0..C] (one CTA)
 __global__ void offsets_scan_kernel(const int64_t *counts, int C, int64_t *offsets) {
-  __shared__ int64_t part[1024];
-  int t = threadIdx.x;
-  int per = (C + blockDim.x - 1) / blockDim.x;
-  int lo = t * per, hi = min(C, lo + per);
+  __shared__ int64_t wsum[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = (int)(blockDim.x >> 5);
+  const int per = (C + blockDim.x - 1) / blockDim.x;
+  const int lo = t * per, hi = min(C, lo + per);
   int64_t s = 0;
   for (int c = lo; c < hi; ++c) s += counts[c];
-  part[t] = s;
+  // block scan of the threads' sums: within each warp, then over the warps
+  int64_t inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) wsum[w] = inc;
   __syncthreads();
-  if (t == 0) {
-    int64_t run = 0;
-    for (int i = 0; i < (int)blockDim.x; ++i) {
-      int64_t v = part[i];
-      part[i] = run;
-      run += v;
+  if (w == 0) {
+    const int64_t x = lane < nw ? wsum[lane] : 0;
+    int64_t xi = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += y;
     }
-    offsets[C] = run;
+    if (lane < nw) wsum[lane] = xi - x;
   }
   __syncthreads();
-  int64_t run = part[t];
+  int64_t run = wsum[w] + inc - s;
   for (int c = lo; c < hi; ++c) {
     offsets[c] = run;
     run += counts[c];
   }
+  if (t == (int)blockDim.x - 1) offsets[C] = run;
 }
 
-__global__ void label_scatter_kernel(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
+__global__ void label_scatter_kernel(const uint64_t *keys, const uint32_t *labels, int64_t n, int C, int bs,
                                      const uint32_t *block_counts, const int64_t *offsets,
                                      uint32_t *members) {
   extern __shared__ uint32_t rank[];
@@ -185,8 +203,8 @@ __global__ void label_scatter_kernel(const uint64_t *keys, const uint32_t *label
   __syncthreads();
   if (threadIdx.x >= 32) return;
   const int lane = threadIdx.x;
-  int64_t lo = (int64_t)blockIdx.x * kSortBlock;
-  int64_t hi = min(n, lo + kSortBlock);
+  int64_t lo = (int64_t)blockIdx.x * bs;
+  int64_t hi = min(n, lo + bs);
   for (int64_t base = lo; base < hi; base += 32) {
     int64_t i = base + lane;
     uint32_t l = i < hi ? (keys ? key_row(keys[i]) : labels[i]) : 0xffffffffu;
@@ -1393,7 +1411,12 @@ __global__ void group_map_kernel(const int64_t *grp_off, int C, uint32_t *gmap) 
 int sort_labels(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
                        DevBuf &blk, DevBuf &counts, int64_t *d_offsets, uint32_t *d_members,
                        cudaStream_t s) {
-  int64_t nb = ceil_div(n, kSortBlock);
+  // items per block: kSortBlock, or for small sets (a search's queries)
+  // fewer, so that the scatter's serial walk of each block is spread over
+  // the SMs; the order (stable by item) is the same either way
+  const int bs = n > (int64_t)2 * 152 * kSortBlock ? kSortBlock
+                                                   : (int)std::max<int64_t>(128, round_up(ceil_div(n, (int64_t)2 * 152), 32));
+  int64_t nb = ceil_div(n, (int64_t)bs);
   HORA_TRY(blk.reserve(sizeof(uint32_t) * nb * C));
   HORA_TRY(counts.reserve(sizeof(int64_t) * C));
   int smem = C * 4;
@@ -1401,13 +1424,14 @@ int sort_labels(const uint64_t *keys, const uint32_t *labels, int64_t n, int C,
   HORA_SMEM_ATTR(label_scatter_kernel, smem);
   {
     ProfScope ps("ivf_sort", s);
-    label_hist_kernel<<<(unsigned)nb, 256, smem, s>>>(keys, labels, n, C, blk.as<uint32_t>());
+    label_hist_kernel<<<(unsigned)nb, 256, smem, s>>>(keys, labels, n, C, bs, blk.as<uint32_t>());
     HORA_LAUNCHED();
-    label_block_scan_kernel<<<ceil_div(C, 256), 256, 0, s>>>(blk.as<uint32_t>(), nb, C, counts.as<int64_t>());
+    label_block_scan_kernel<<<ceil_div((int64_t)C * 32, 256), 256, 0, s>>>(blk.as<uint32_t>(), nb, C,
+                                                                            counts.as<int64_t>());
     HORA_LAUNCHED();
     offsets_scan_kernel<<<1, 1024, 0, s>>>(counts.as<int64_t>(), C, d_offsets);
     HORA_LAUNCHED();
-    label_scatter_kernel<<<(unsigned)nb, 256, smem, s>>>(keys, labels, n, C, blk.as<uint32_t>(),
+    label_scatter_kernel<<<(unsigned)nb, 256, smem, s>>>(keys, labels, n, C, bs, blk.as<uint32_t>(),
                                                         d_offsets, d_members);
     HORA_LAUNCHED();
   }

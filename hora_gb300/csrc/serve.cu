@@ -94,10 +94,12 @@ static size_t request_bytes(const hora_index *h, uint64_t nq, uint64_t k) {
     per_q += Dp * 2 + cap * 8 + (size_t)R * 16 + 64;
     // starting thresholds: per query (a power of two >= 1,024 of them) the
     // pivot key, bucket slot, member keys, threshold, position, query copy
-    // and share of a work item (4,096 pivots at most); for wide lists the
-    // sample pass's list and candidates (at most 180 + 2,048 keys)
+    // and share of a work item (4,096 pivots at most), and the bucketing's
+    // per-block pivot counts (a block per 128 queries at most); for wide
+    // lists the sample pass's list and candidates (at most 180 + 2,048 keys)
     const size_t nres = std::max<size_t>(1024, nq);
-    fixed += 2 * nres * (8 + 4 + 1024 * 4 + 4 + 4 + Dp + 1) + (size_t)4097 * 48;
+    fixed += 2 * nres * (8 + 4 + 1024 * 4 + 4 + 4 + Dp + 1) + (size_t)4097 * 48 +
+             (2 * nres / 128 + 1) * (size_t)4097 * 4;
     if (lowp_probe_kind(h, R) == 2) per_q += 8 * (180 + 2048 + 32) + 8;
   } else {
     const size_t C = h->ivf.n_kmeans_center;
