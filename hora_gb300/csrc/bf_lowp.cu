@@ -437,14 +437,16 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
+    // (its waits poll instead of sleeping in try_wait: the thread's wake-up
+    // after a slot fills or an accumulator frees gates the tensor pipe)
     if (tc::elect_one()) {
       constexpr uint32_t idesc = tc::idesc_f32acc(PREC == HORA_PREC_BF16 ? 1u : 0u, kLpBM, kLpBN);
       bool ok = tc::mbar_wait(a_full, 0, abort);
       const bool rest = nkb > 1 || FOLD;  // a second half exists
       for (int t = 0; ok && t < T; ++t) {
         const int s = t % S, j = t / S, b = t % kLpNB, jb = t / kLpNB;
-        if (!tc::mbar_wait(full + s, j & 1, abort)) break;
-        if (jb > 0 && !tc::mbar_wait(acc_empty + b, (jb - 1) & 1, abort)) break;
+        if (!tc::mbar_wait_poll(full + s, j & 1, abort)) break;
+        if (jb > 0 && !tc::mbar_wait_poll(acc_empty + b, (jb - 1) & 1, abort)) break;
         tc::fence_after_sync();
         const uint32_t d = tmem + (uint32_t)(b * kLpBN);
         uint8_t *st = sB + (size_t)s * stage_bytes;
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
           if (kb == 1) {
             // K block 0 read: its half of the stage may be refilled
             tc::mma_commit(empty + s);
-            if (!tc::mbar_wait(full2 + s, j & 1, abort)) {
+            if (!tc::mbar_wait_poll(full2 + s, j & 1, abort)) {
               ok2 = false;
               break;
             }
@@ -476,7 +478,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
         if (FOLD) {
           if (nkb == 1) {
             tc::mma_commit(empty + s);
-            if (!tc::mbar_wait(full2 + s, j & 1, abort)) break;
+            if (!tc::mbar_wait_poll(full2 + s, j & 1, abort)) break;
             tc::fence_after_sync();
           }
           const uint64_t ad = tc::sdesc_kmajor_none(tc::smem_u32(sAn), kNormHalfA, 128);

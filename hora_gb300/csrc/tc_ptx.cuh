@@ -65,6 +65,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
   return false;
 }
 
+// mbar_wait without the suspend hint: the thread polls (try_wait without a
+// time hint), for the one thread whose wake-up latency gates the tensor pipe.
+__device__ __forceinline__ bool mbar_wait_poll(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                               long long max_cycles = kWaitCycles) {
+  const long long t0 = clock64();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+    if (clock64() - t0 > max_cycles) break;
+  }
+  *abort = 1;
+  return false;
+}
+
 // ---- TMA ------------------------------------------------------------------------
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar,
                                             int x, int y) {
