@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(kLpThreads, 1)
     tc::mbar_init(a_full, 1);
     for (int b = 0; b < kLpNB; ++b) {
       tc::mbar_init(acc_full + b, 1);
-      tc::mbar_init(acc_empty + b, kLpEpiThreads);
+      tc::mbar_init(acc_empty + b, kLpEpiThreads / 32);  // one arrival per drain warp
     }
     tc::mbar_init(done, 1);
     *abort = 0;
@@ -566,8 +566,11 @@ __global__ void __launch_bounds__(kLpThreads, 1)
       tc::tmem_ld32(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(b * kLpBN + (h * kLpSlices + sl) * 32), v);
       tc::tmem_ld_wait();
       if (sl == kLpSlices - 1) {
+        // every lane's loads are complete (tcgen05.wait::ld): one arrival
+        // for the warp instead of one per thread on the same barrier word
         tc::fence_before_sync();
-        tc::mbar_arrive(acc_empty + b);
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(acc_empty + b);
       }
       if (FAST) {
         if constexpr (MODE == TILE_ARGMIN) {
