@@ -43,10 +43,12 @@ constexpr int kLpBN = 256;           // base rows per tile (accumulator columns,
 constexpr int kLpNB = 2;             // TMEM accumulator buffers (2 x 256 columns)
 constexpr int kLpThreads = 576;      // 18 warps
 constexpr int kLpEpiThreads = 512;   // warps 2..17
-// Base tiles per CTA: 32 (8,192 rows) amortises the CTA prologue (measured
-// best of 16-64 at 10k queries); a launch with few query blocks takes 16 or
-// 8 so that it still spreads over every SM (see lp_tiles_per_cta).
-constexpr int kLpTilesPerCta = 32;
+// Base tiles per CTA: up to 128 (32,768 rows) amortises the CTA prologue
+// and epilogue, which no other CTA overlaps at one CTA per SM (the probed
+// pass over 1M rows at 10k queries: 1.98 ms at 32, 1.88 at 64, 1.84 at 128,
+// 1.87 at 256); a launch with few query blocks takes fewer, down to 8, so
+// that it still spreads over every SM (see lp_tiles_per_cta).
+constexpr int kLpTilesPerCta = 128;
 constexpr int kLpMinTilesPerCta = 8;
 constexpr int kLpSlices = kLpBN / 4 / 32;  // 32-column slices per drain warp and tile
 constexpr int kLpMaxStages = 8;
