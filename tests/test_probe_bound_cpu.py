@@ -90,3 +90,43 @@ def test_probe_margin_covers_summation_order():
     s = np.where(np.arange(128) % 2, 1.0, -1.0).astype(np.float32)
     Xs = (np.abs(X) + 1.0) * s
     assert worst_ratio((np.abs(q) + 1.0) * s, Xs[:, ::-1].copy()) < 0.05
+
+
+def _descent(v, R, skip, start_bit, a0):
+    a = a0
+    for b in range(start_bit, skip - 1, -1):
+        tt = a | (1 << b)
+        if int((v < tt).sum()) < R:
+            a = tt
+    return a | ((1 << skip) - 1)
+
+
+def test_threshold_descent_starts_below_the_common_bits():
+    """probe_select_kernel takes a query's R-th smallest probe key (ordered
+    32-bit encoding, rounded up below bit 12) by a bitwise descent.  It
+    starts below the highest bit in which the members' keys differ, with
+    their common higher bits as the start: a descent through those bits
+    would set exactly the ones the keys share (a set bit leaves no key below
+    it, a clear one all L >= R).  The shortcut must give the full descent's
+    value for every key set: random words, float-like distances, ties, one
+    distinct key, and keys differing only below the rounding bit."""
+    rng = np.random.default_rng(11)
+    skip = 12
+    for it in range(4000):
+        L = int(rng.integers(1, 1025))
+        R = int(rng.integers(1, L + 1))
+        kind = it % 5
+        if kind == 0:
+            v = rng.integers(0, 2**32, L, dtype=np.uint64)
+        elif kind == 1:
+            v = rng.uniform(100, 300, L).astype(np.float32).view(np.uint32).astype(np.uint64)
+        elif kind == 2:
+            v = np.full(L, int(rng.integers(0, 2**32)), dtype=np.uint64)
+        elif kind == 3:
+            v = (int(rng.integers(0, 2**31)) + rng.integers(0, 5000, L)).astype(np.uint64)
+        else:
+            v = (int(rng.integers(0, 2**20)) * 4096 + rng.integers(0, 4096, L)).astype(np.uint64)
+        lo, hi = int(v.min()), int(v.max())
+        top = (lo ^ hi).bit_length() - 1
+        a0 = lo if top < 0 else (0 if top >= 31 else lo & ~((2 << top) - 1) & 0xFFFFFFFF)
+        assert _descent(v, R, skip, top, a0) == _descent(v, R, skip, 31, 0), (it, L, R)
