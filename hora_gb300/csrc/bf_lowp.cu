@@ -102,6 +102,9 @@ struct LowpState {
   // BF16 Euclidean and DotProduct: the largest |x - bf16(x)| over the rows
   // (1 f32, rounded up), the rows' share of the certified error bounds
   DevBuf dxmax;
+  // BF16 Euclidean: each row's |x - bf16(x)| (n f32, rounded up), for the
+  // per-row window of the certified exact search
+  DevBuf dxrow;
 };
 
 void lowp_state_free(LowpState *p) { delete p; }
@@ -735,7 +738,8 @@ __global__ void norm_block_kernel(const double *sq, int64_t n, __nv_bfloat16 *ou
 
 // The largest Euclidean norm of x - bf16(x) over the rows (one warp per row,
 // f64 sums, rounded up to the next f32) into *out as ordered bits.
-__global__ void bf16_residual_max_kernel(const float *X, int64_t n, int64_t ld, int64_t dim, unsigned *out) {
+__global__ void bf16_residual_max_kernel(const float *X, int64_t n, int64_t ld, int64_t dim, unsigned *out,
+                                         float *row_out = nullptr) {
   const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (r >= n) return;
@@ -747,7 +751,11 @@ __global__ void bf16_residual_max_kernel(const float *X, int64_t n, int64_t ld, 
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) atomicMax(out, __float_as_uint(nextafterf((float)sqrt(acc), INFINITY)));
+  const float e = nextafterf((float)sqrt(acc), INFINITY);
+  if (lane == 0) {
+    atomicMax(out, __float_as_uint(e));
+    if (row_out) row_out[r] = e;
+  }
 }
 
 // one warp per row: per-row absmax scale so the row's largest entry maps to 448
@@ -1351,8 +1359,10 @@ static int ensure_lowp(hora_index *h, int prec, cudaStream_t s) {
         HORA_LAUNCHED();
         HORA_TRY(st->dxmax.reserve(sizeof(float)));
         HORA_CUDA_TRY(cudaMemsetAsync(st->dxmax.ptr, 0, sizeof(float), s));
-        bf16_residual_max_kernel<<<ceil_div(h->n, 8), 256, 0, s>>>(h->base.as<float>(), h->n, h->ld, h->dim,
-                                                                   st->dxmax.as<unsigned>());
+        if (h->metric == M_L2) HORA_TRY(st->dxrow.reserve(sizeof(float) * std::max<int64_t>(h->n, 1)));
+        bf16_residual_max_kernel<<<ceil_div(h->n, 8), 256, 0, s>>>(
+            h->base.as<float>(), h->n, h->ld, h->dim, st->dxmax.as<unsigned>(),
+            h->metric == M_L2 ? st->dxrow.as<float>() : nullptr);
       }
     } else {
       HORA_TRY(st->xscale.reserve(sizeof(float) * std::max<int64_t>(h->n, 1)));
@@ -2167,6 +2177,103 @@ __global__ void exact_tc_slack_kernel(const float *Q, int64_t nq, int64_t ld, in
   slack[q] = nextafterf((float)(2.0 * eps * (1.0 + 0x1p-10)), INFINITY);
 }
 
+// The certified pass keeps every row whose scan value s is within 2 eps of
+// the probed threshold, eps the largest over all rows (exact_tc_slack_kernel).
+// With a kept row's own norm |x| and residual |x - bf16(x)| in place of the
+// largest, the same terms give its own bound e_r: its exact distance lies in
+// [s - e_r, s + e_r].  The k-th smallest upper end U over the kept rows
+// bounds the exact k-th distance (k rows have exact distances at most U), so
+// a row with s - e_r > U is not among the exact k best.  One warp per query
+// keeps the others at the front of its slots, in order, and lowers its count
+// before the exact rescoring; queries with k or fewer rows, or more than
+// kExactTcWindowMax (their values would not fit in the warp's registers) or
+// than the capacity, keep theirs.  The bound is evaluated in f32 and widened
+// by a relative 2^-8, far beyond the roundings of its dozen operations.
+constexpr int kExactTcWindowMax = 1024;
+__global__ void exact_tc_window_kernel(const float *Q, int64_t ld, int64_t dim, int64_t Dp, const double *qsq64,
+                                       const float *xsq, const float *dxrow, int64_t nq, int k, int cap,
+                                       uint64_t *cand, uint32_t *count) {
+  const int64_t q = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  const int n = (int)count[q];
+  if (n <= k || n > cap || n > kExactTcWindowMax) return;
+  double sb = 0.0, sd = 0.0;
+  for (int64_t t = lane; t < dim; t += 32) {
+    const float x = Q[q * ld + t];
+    const double b = (double)__bfloat162float(__float2bfloat16_rn(x));
+    sb += b * b;
+    sd += ((double)x - b) * ((double)x - b);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    sb += __shfl_xor_sync(0xffffffffu, sb, o);
+    sd += __shfl_xor_sync(0xffffffffu, sd, o);
+  }
+  const float qb = (float)(sqrt(sb) * (1.0 + 0x1p-40)), dq = (float)(sqrt(sd) * (1.0 + 0x1p-40));
+  const float qsq = (float)(qsq64[q] * (1.0 + 0x1p-40)), qn = (float)(sqrt(qsq64[q]) * (1.0 + 0x1p-40));
+  const float cb = (float)(Dp + 16) * 0x1p-22f, ce = (float)(dim + 4) * 0x1p-23f;
+  uint64_t *kq = cand + q * (int64_t)cap;
+  // e_r: exact_tc_slack_kernel's eps with the row's own |x| and residual
+  auto bound = [&](uint32_t r) -> float {
+    const float xs = xsq[r] * (1.0f + 0x1p-22f);
+    const float xn = sqrtf(xs) * (1.0f + 0x1p-22f);
+    const float dx = dxrow[r];
+    const float xb = xn * (1.0f + 0x1p-8f) + dx;
+    const float A = qb * dx + dq * xn;
+    const float B = cb * (qb * xb + 0.5f * xs);
+    const float C = 0x1p-22f * (qsq + 2.0f * qb * xb + xs);
+    const float E = ce * (qn + xn) * (qn + xn);
+    return (2.0f * A + 2.0f * B + C + E) * (1.0f + 0x1p-8f);
+  };
+  // each lane's upper ends s + e_r, ordered encoding (padding: the largest)
+  uint32_t u[kExactTcWindowMax / 32];
+  uint32_t lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+  for (int i = 0; i < kExactTcWindowMax / 32; ++i) {
+    const int j = lane + 32 * i;
+    u[i] = 0xffffffffu;
+    if (j < n) {
+      const uint64_t key = kq[j];
+      u[i] = f2ord(key_dist(key) + bound(key_row(key)));
+      lo = min(lo, u[i]);
+      hi = max(hi, u[i]);
+    }
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  // the k-th smallest upper end by a bitwise descent below the bits all of
+  // them share (see probe_select_kernel), rounded up below bit 8
+  const int top = 31 - __clz((int)(lo ^ hi));
+  uint32_t a = top < 0 ? lo : top >= 31 ? 0u : lo & ~((2u << top) - 1u);
+  for (int b = top; b >= 8; --b) {
+    const uint32_t tt = a | (1u << b);
+    int cnt = 0;
+#pragma unroll
+    for (int i = 0; i < kExactTcWindowMax / 32; ++i) cnt += u[i] < tt;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (cnt < k) a = tt;
+  }
+  const float U = ord2f(a | 0xffu);
+  // keep s - e_r <= U, in order, at the front (a write never passes a read:
+  // the slot written is at most the slot just read)
+  int m = 0;
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int j = j0 + lane;
+    uint64_t key = 0;
+    bool keep = false;
+    if (j < n) {
+      key = kq[j];
+      keep = key_dist(key) - bound(key_row(key)) <= U;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (keep) kq[m + __popc(bal & ((1u << lane) - 1u))] = key;
+    m += __popc(bal);
+  }
+  if (lane == 0) count[q] = (uint32_t)m;
+}
+
 // Queries the certified pass cannot answer: fewer than k rows kept (no
 // valid probe) or more than the capacity (overflow).
 __global__ void exact_tc_fallback_kernel(const uint32_t *count, int64_t nq, int k, int cap, int *n, int *list) {
@@ -2276,6 +2383,12 @@ int exact_tc_search_keys(hora_index *h, int64_t nq, int k, SearchWorkspace &ws, 
   exact_tc_fallback_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(count, nq, k, cap, lerr + 1,
                                                                      ws.xlist.as<int>());
   HORA_LAUNCHED();
+  if (mt == M_L2 && L.dxrow.ptr) {
+    exact_tc_window_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(
+        ws.q.as<float>(), h->ld, h->dim, Dp, qsq64, L.xsq.as<float>(), L.dxrow.as<float>(), nq, k, cap, p.cand,
+        count);
+    HORA_LAUNCHED();
+  }
   HORA_TRY(launch_rerank_exact(mt, ws.q.as<float>(), h->ld, h->base.as<float>(), h->dim, ws.qnorm.as<float>(),
                                h->xnorm.as<float>(), p.cand, nq, cap, p.cand, s, count));
   HORA_CUDA_TRY(cudaMemsetAsync(d_best, 0xff, sizeof(uint64_t) * nq * k, s));
