@@ -160,11 +160,13 @@ class Clocks:
 # DRAM traffic of the BF16 scan in one step of the headline form (1M x 128,
 # 10k queries, R = 132: the pivot pass and the probed pass over the base),
 # from an ncu capture of dram__bytes_read.sum + dram__bytes_write.sum of the
-# same kernel build (ncu --metrics ... -k regex:lowp_tile -s 2 -c 2 over this
-# script with --forms bf16r132 --no-ivf --no-extras): pivot pass (argmin)
-# 3.0 MB read, base pass 292.1 MB read + 12.8 MB written.  ncu is not run
-# inside the bench; the value is reported beside the live timing as the
-# capture's figure.
+# kernel (ncu --metrics ... -k regex:lowp_tile -s 2 -c 2 over this script
+# with --forms bf16r132 --no-ivf --no-extras): pivot pass (argmin) 3.0 MB
+# read, base pass 292.1 MB read + 12.8 MB written.  Captured while a CTA
+# walked 32 tiles and before the MMA issuer polled its barriers; those
+# change when the bytes move, not which (the base image is read once, the
+# candidates written once).  ncu is not run inside the bench; the value is
+# reported beside the live timing as the capture's figure.
 SCAN_TRAFFIC_BYTES_PER_STEP = 307.9e6
 
 
